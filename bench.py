@@ -1,0 +1,406 @@
+"""Benchmark: Mrays/s of nearest-hit + any-hit queries on one GB300.
+
+Workload (one "step" = one frame of HeavyRT's RTAO renderer on the
+1024 x 1024-quad heightfield, 2,097,152 triangles):
+  * 1920 x 1080 eye rays, RayQuery_NearestHit;
+  * 16 cosine-weighted AO rays per primary hit, RayQuery_AnyHit.
+value = (eye rays + AO rays) / step time, inputs resident in HBM.
+e2e   = the same through the host-pointer C-ABI calls: every step copies the
+        step's rays from pinned host memory and the results back.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU algorithm (the oracle restatement
+of HeavyRT's BVH2CommonRT traversal, OpenMP over rays on every host core) on
+the same frame.  N > 1 (torchrun) runs independent replicas, one per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s nearest/any-hit on 1 GB300, served+batched vs plain; p99 latency"
+UNIT = "Mrays/s"
+FALLBACK_HBM_GBS = 6800.0
+NODE_PAIR_BYTES = 64   # one pair record: two child boxes + refs
+TRI_BYTES = 36         # three float3 (vertex A and two edges)
+RAY_BYTES = 32         # {posAndNear, dirAndFar}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--nx", type=int, default=1024, help="heightfield quads per side")
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(name: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_frame(args):
+    """Scene + eye rays of the heightfield RTAO frame (host arrays)."""
+    from heavyrt_gb300 import workload as wl
+
+    w = wl.config1(args.nx, args.width, args.height)
+    return w
+
+
+def ao_from_hits(w, hits, sorted_idx):
+    from heavyrt_gb300 import workload as wl
+
+    p = w.params
+    ao, _ = wl.ao_rays(p["ao_seed"], w.eye_rays, hits, w.verts, sorted_idx, p["ao_per_hit"], p["ao_length"],
+                       p["ao_offset"])
+    return ao
+
+
+# ---------------------------------------------------------------- CPU (reference algorithm)
+
+def cpu_trace_rate(o, eye, ao, seconds: float, threads: int = 0):
+    """Mrays/s of the oracle traversal over a bounded sample of the frame
+    (eye and AO rays in the frame's proportion)."""
+    n_eye, n_ao = eye.shape[0], ao.shape[0]
+    frac = 0.02
+    t0 = time.perf_counter()
+    e_s = eye[: max(1, int(n_eye * frac))]
+    a_s = ao[:: max(1, int(1 / frac))]
+    o.trace(e_s, threads=threads)
+    o.trace(a_s, any_hit=True, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = (e_s.shape[0] + a_s.shape[0]) / dt
+    # sample size for the target duration
+    frac = min(1.0, seconds * rate / (n_eye + n_ao))
+    e_s = eye[: max(1, int(n_eye * frac))]
+    step = max(1, int(round(1 / frac))) if frac < 1.0 else 1
+    a_s = ao[::step]
+    t0 = time.perf_counter()
+    _, _, used = o.trace(e_s, threads=threads, counters=True)
+    o.trace(a_s, any_hit=True, threads=threads)
+    dt = time.perf_counter() - t0
+    n = e_s.shape[0] + a_s.shape[0]
+    return n / dt / 1e6, used, f"{e_s.shape[0]} eye rays (first rows) + {a_s.shape[0]} AO rays (every {step}th) " \
+                               f"of the frame, {dt:.1f} s"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+
+    w = make_frame(args)
+    o = orc.OracleBVH(w.verts, w.idx)
+    eye_hits = o.trace(w.eye_rays)
+    ao = ao_from_hits(w, eye_hits, o.sorted_indices())
+    n_eye, n_ao = w.eye_rays.shape[0], ao.shape[0]
+    # each step: a bounded sample of the frame, eye and AO rays in proportion
+    per_step = max(1.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    rate0, used, _ = cpu_trace_rate(o, w.eye_rays, ao, 1.0)
+    frac = min(1.0, per_step * rate0 * 1e6 / (n_eye + n_ao))
+    e_s = w.eye_rays[: max(1, int(n_eye * frac))]
+    stride = max(1, int(round(1 / frac))) if frac < 1.0 else 1
+    a_s = ao[::stride]
+    for _ in range(args.warmup):
+        o.trace(e_s)
+        o.trace(a_s, any_hit=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.trace(e_s)
+        o.trace(a_s, any_hit=True)
+    dt = time.perf_counter() - t0
+    n = (e_s.shape[0] + a_s.shape[0]) * args.steps
+    value = n / dt / 1e6
+    sample = (f"per step {e_s.shape[0]} of {n_eye} eye rays + {a_s.shape[0]} of {n_ao} AO rays "
+              f"(every {stride}th); oracle restatement of BVH2CommonRT, OpenMP over rays")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "tris": int(w.idx.size // 3), "eye_rays": int(n_eye), "ao_rays": int(n_ao),
+                   "parallelism": "cpu", "l2": "n/a (host)"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": int(used), "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU engine
+
+def run_engine(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from heavyrt_gb300 import Context, PinnedBuffer, SceneRT
+    from heavyrt_gb300 import engine as E
+
+    w = make_frame(args)
+    ctx = Context(local)
+    scene = SceneRT(ctx)
+    gid = scene.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+    scene.AddInstance(gid)
+    scene.CommitScene()
+    info = scene.geom_info(gid)
+    # build time: a few more builds of the same geometry
+    build_ms = [info["build_ms"]]
+    for _ in range(3):
+        s2 = SceneRT(ctx)
+        g2 = s2.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+        build_ms.append(s2.geom_info(g2)["build_ms"])
+        s2.close()
+
+    eye_hits = scene.RayQuery_NearestHit(w.eye_rays)
+    ao = ao_from_hits(w, eye_hits, scene.export(gid, E.EXPORT_SORTED_INDICES))
+    n_eye, n_ao = w.eye_rays.shape[0], ao.shape[0]
+
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_eye = torch.from_numpy(w.eye_rays).cuda()
+    d_ao = torch.from_numpy(ao).cuda()
+    d_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
+    d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
+
+    # algorithmic bytes per launch from the counting traversal (same decisions)
+    eye_pairs, eye_tris = scene.query_counters(0, d_eye.data_ptr(), n_eye, sh)
+    ao_pairs, ao_tris = scene.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+    eye_bytes = NODE_PAIR_BYTES * eye_pairs + TRI_BYTES * eye_tris + RAY_BYTES * n_eye + 32 * n_eye
+    ao_bytes = NODE_PAIR_BYTES * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        scene.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+        if ev:
+            ev[1].record(stream)
+        scene.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    eye_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    ao_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    rays_per_step = n_eye + n_ao
+    value = world * rays_per_step / (ms_per_step * 1e-3) / 1e6
+
+    # e2e: host pinned rays in, results out, through the host-pointer C-ABI calls
+    pin_eye = PinnedBuffer(w.eye_rays.nbytes)
+    pin_ao = PinnedBuffer(ao.nbytes)
+    pin_hits = PinnedBuffer(32 * n_eye)
+    pin_any = PinnedBuffer(n_ao)
+    pe = pin_eye.array(np.float32).reshape(-1, 8)
+    pa = pin_ao.array(np.float32).reshape(-1, 8)
+    pe[:] = w.eye_rays
+    pa[:] = ao
+    L = E.lib()
+    import ctypes as C
+
+    def e2e_step():
+        ctx.check(L.hrt_query_nearest_host(scene._h, C.c_void_p(pin_eye.ptr), n_eye, C.c_void_p(pin_hits.ptr)), "e2e")
+        ctx.check(L.hrt_query_any_host(scene._h, C.c_void_p(pin_ao.ptr), n_ao, C.c_void_p(pin_any.ptr)), "e2e")
+
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_value = world * rays_per_step / e2e_s / 1e6
+    got_any = pin_any.array(np.uint8)[:n_ao].copy()
+    for b in (pin_eye, pin_ao, pin_hits, pin_any):
+        b.free()
+
+    # roofline of the dominant kernel
+    eye_avg, ao_avg = statistics.mean(eye_ms), statistics.mean(ao_ms)
+    if ao_avg >= eye_avg:
+        dom, dom_ms, dom_bytes, dom_name = "any", ao_avg, ao_bytes, "k_trace<any>"
+    else:
+        dom, dom_ms, dom_bytes, dom_name = "nearest", eye_avg, eye_bytes, "k_trace<nearest>"
+    peak, peak_kind = measured_peak()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = profile_traffic(f"trace_{dom}_heightfield2M.txt")
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "tris": int(w.idx.size // 3), "eye_rays": int(n_eye), "ao_rays": int(n_ao),
+                   "layout": "BVH2 pair records (64 B) + sorted triangle records", "parallelism": f"replicas{world}",
+                   "l2": f"inputs larger than L2: rays {(d_eye.nbytes + d_ao.nbytes) / 1e6:.0f} MB, "
+                         f"BVH+triangles {info['bytes'] / 1e6:.0f} MB",
+                   "build_ms_median": round(statistics.median(build_ms), 3),
+                   "eye_ms": round(eye_avg, 4), "ao_ms": round(ao_avg, 4),
+                   "eye_mrays_s": round(n_eye / eye_avg / 1e3, 2), "ao_mrays_s": round(n_ao / ao_avg / 1e3, 2),
+                   "node_pairs_per_eye_ray": round(eye_pairs / n_eye, 3),
+                   "node_pairs_per_ao_ray": round(ao_pairs / n_ao, 3)},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(RAY_BYTES * (n_eye + n_ao)),
+                "d2h_bytes_per_step": int(32 * n_eye + n_ao)},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "algorithmic_bytes_per_launch": int(dom_bytes),
+                     "note": "algorithmic bytes = 64 B per node pair + 36 B per triangle test + ray in/out; "
+                             "node fetches mostly hit L1/L2, so frac can exceed 1 (see traffic)"},
+        "clocks": clk,
+    }
+
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as orc
+
+        o = orc.OracleBVH(w.verts, w.idx)
+        rate, used, sample = cpu_trace_rate(o, w.eye_rays, ao, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": round(rate, 3), "unit": UNIT, "cores": int(used), "kind": "port",
+                                "sample": sample}
+        # the frame's any-hit flags from the e2e leg agree with the oracle on the sample rows
+        step_ao = max(1, n_ao // 20000)
+        want = o.trace(ao[::step_ao], any_hit=True)
+        line["config"]["e2e_anyhit_matches_oracle_sample"] = bool(np.array_equal(got_any[::step_ao].astype(bool), want))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_engine(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

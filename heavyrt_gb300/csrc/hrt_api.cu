@@ -1,0 +1,719 @@
+// C ABI of the engine (include/hrt.h): contexts, scenes, geometry builds,
+// instances and batched queries.  Host-side bookkeeping mirrors
+// BVH2CommonRT's (core/BVH2CommonRT.h:70-87, core/BVH2CommonRT_host.cpp); every
+// array it keeps lives in device memory.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hrt_kernels.cuh"
+#include "../../include/hrt.h"
+
+using namespace hrt;
+
+struct hrt_context
+{
+  int          device = 0;
+  int          numSMs = 0;
+  cudaStream_t stream = nullptr;
+  std::string  lastError;
+  std::mutex   mu;
+};
+
+namespace
+{
+
+struct Geom
+{
+  uint32_t     nTris = 0, nVerts = 0, nLeaves = 0;
+  float4*      verts = nullptr;
+  uint32_t*    keys = nullptr;          // sorted Morton codes
+  uint32_t*    vals = nullptr;          // sorted triangle ids (= prim indices)
+  uint32_t*    keysUnsorted = nullptr;
+  uint32_t*    compressed = nullptr;
+  uint32_t*    runStarts = nullptr;
+  BVHNode32*   lr = nullptr;
+  uint32_t*    lrCount = nullptr;
+  PairRec*     recs = nullptr;
+  TriRec*      tris = nullptr;
+  uint32_t*    sortedIdx = nullptr;
+  BuildParams* params = nullptr;
+  BuildParams  host{};
+  float        buildMs = 0.0f;
+  uint64_t     bytes = 0;
+  float        box[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+struct Instance
+{
+  uint32_t geomId = 0;
+  float    m[16];     // column-major
+  float    inv[12];   // rows 0..2 of the inverse, row-major
+  bool     identity = true;
+};
+
+}  // namespace
+
+struct hrt_scene
+{
+  hrt_context*          ctx = nullptr;
+  std::vector<Geom>     geoms;
+  std::vector<Instance> insts;
+  bool                  committed = false;
+  InstanceDesc*         dInst = nullptr;
+  uint32_t              nInstDev = 0;
+  uint32_t*             dError = nullptr;
+  unsigned long long*   dCounters = nullptr;
+  // staging for the host-pointer queries
+  void*                 stageRays = nullptr;
+  void*                 stageOut = nullptr;
+  uint64_t              stageCap = 0;
+  std::mutex            mu;
+};
+
+namespace
+{
+
+int fail(hrt_context* ctx, int status, const std::string& msg)
+{
+  if (ctx)
+  {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->lastError = msg;
+  }
+  return status;
+}
+
+int cuda_fail(hrt_context* ctx, cudaError_t e, const char* what)
+{
+  const int st = (e == cudaErrorMemoryAllocation) ? HRT_ERR_OUT_OF_MEMORY : HRT_ERR_CUDA;
+  return fail(ctx, st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define HRT_CUDA(ctx, call)                               \
+  do                                                      \
+  {                                                       \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+void free_geom(Geom& g)
+{
+  void* ptrs[] = {g.verts, g.keys, g.vals, g.keysUnsorted, g.compressed, g.runStarts, g.lr,
+                  g.lrCount, g.recs, g.tris, g.sortedIdx, g.params};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  g = Geom();
+}
+
+template <typename T> cudaError_t dalloc(T** p, size_t count, uint64_t* bytes)
+{
+  const size_t b = sizeof(T) * (count ? count : 1);
+  if (bytes) *bytes += b;
+  return cudaMalloc((void**)p, b);
+}
+
+__global__ void k_pack_verts(const uint8_t* __restrict__ raw, uint64_t n, uint64_t stride, float4* __restrict__ out)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+  {
+    const float* p = reinterpret_cast<const float*>(raw + i * stride);
+    out[i] = make_float4(p[0], p[1], p[2], 1.0f);
+  }
+}
+
+// Inverse of a column-major 4x4 through the adjugate, in float, the same
+// evaluation as the reference checker's LiteMath stand-in.
+void inverse4x4(const float* mc, float* inv12)
+{
+  float a[4][4];
+  for (int r = 0; r < 4; r++)
+    for (int c = 0; c < 4; c++) a[r][c] = mc[c * 4 + r];
+  auto minor3 = [&](int skipR, int skipC) {
+    float s[3][3];
+    int rr = 0;
+    for (int r = 0; r < 4; r++)
+    {
+      if (r == skipR) continue;
+      int cc = 0;
+      for (int c = 0; c < 4; c++)
+      {
+        if (c == skipC) continue;
+        s[rr][cc++] = a[r][c];
+      }
+      rr++;
+    }
+    const float m0 = s[1][1] * s[2][2] - s[1][2] * s[2][1];
+    const float m1 = s[1][0] * s[2][2] - s[1][2] * s[2][0];
+    const float m2 = s[1][0] * s[2][1] - s[1][1] * s[2][0];
+    return s[0][0] * m0 - s[0][1] * m1 + s[0][2] * m2;
+  };
+  float cof[4][4];
+  for (int r = 0; r < 4; r++)
+    for (int c = 0; c < 4; c++) cof[r][c] = (((r + c) & 1) ? -1.0f : 1.0f) * minor3(r, c);
+  const float det = a[0][0] * cof[0][0] + a[0][1] * cof[0][1] + a[0][2] * cof[0][2] + a[0][3] * cof[0][3];
+  const float invDet = 1.0f / det;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 4; c++) inv12[r * 4 + c] = cof[c][r] * invDet;
+}
+
+bool is_identity(const float* m)
+{
+  for (int c = 0; c < 4; c++)
+    for (int r = 0; r < 4; r++)
+    {
+      const float want = (r == c) ? 1.0f : 0.0f;
+      uint32_t a, b;
+      std::memcpy(&a, &m[c * 4 + r], 4);
+      std::memcpy(&b, &want, 4);
+      if (a != b) return false;
+    }
+  return true;
+}
+
+int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
+                   uint64_t stride)
+{
+  hrt_context* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  const uint32_t N = (uint32_t)(nIdx / 3);
+  g.nTris = N;
+  g.nVerts = (uint32_t)nVert;
+  uint64_t* bytes = &g.bytes;
+  HRT_CUDA(ctx, dalloc(&g.verts, nVert, bytes));
+  HRT_CUDA(ctx, dalloc(&g.params, 1, bytes));
+  HRT_CUDA(ctx, cudaMemsetAsync(g.params, 0, sizeof(BuildParams), st));
+  if (nVert)
+  {
+    if (stride == 16)
+      HRT_CUDA(ctx, cudaMemcpyAsync(g.verts, vpos, 16 * nVert, cudaMemcpyHostToDevice, st));
+    uint8_t* raw = nullptr;
+    if (stride != 16)
+    {
+      HRT_CUDA(ctx, cudaMallocAsync((void**)&raw, stride * nVert, st));
+      HRT_CUDA(ctx, cudaMemcpyAsync(raw, vpos, stride * nVert, cudaMemcpyHostToDevice, st));
+    }
+    const uint8_t* src = raw ? raw : reinterpret_cast<const uint8_t*>(g.verts);
+    uint64_t blocks = (nVert + 255) / 256;
+    if (blocks > 65535) blocks = 65535;
+    k_pack_verts<<<(uint32_t)blocks, 256, 0, st>>>(src, nVert, stride, g.verts);
+    HRT_CUDA(ctx, cudaGetLastError());
+    if (raw) HRT_CUDA(ctx, cudaFreeAsync(raw, st));
+  }
+  if (N == 0)
+  {
+    HRT_CUDA(ctx, cudaStreamSynchronize(st));
+    for (int c = 0; c < 4; c++)
+    {
+      g.box[c] = INFINITY;
+      g.box[4 + c] = -INFINITY;
+    }
+    return HRT_OK;
+  }
+
+  uint32_t* dIdx = nullptr;
+  uint32_t *keysAlt = nullptr, *valsAlt = nullptr, *parent = nullptr, *visit = nullptr;
+  void* scratch = nullptr;
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&dIdx, sizeof(uint32_t) * nIdx, st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * nIdx, cudaMemcpyHostToDevice, st));
+  HRT_CUDA(ctx, dalloc(&g.keys, N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.vals, N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.keysUnsorted, N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.compressed, N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.runStarts, N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.lr, 2 * (size_t)N - 1, bytes));
+  HRT_CUDA(ctx, dalloc(&g.lrCount, 2 * (size_t)N - 1, bytes));
+  HRT_CUDA(ctx, dalloc(&g.recs, N > 1 ? N - 1 : 1, bytes));
+  HRT_CUDA(ctx, dalloc(&g.tris, N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.sortedIdx, 3 * (size_t)N, bytes));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&keysAlt, sizeof(uint32_t) * N, st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&valsAlt, sizeof(uint32_t) * N, st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * (2 * (size_t)N - 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * N, st));
+  HRT_CUDA(ctx, cudaMallocAsync(&scratch, build_scratch_bytes(N), st));
+
+  BuildBuffers b;
+  b.verts = g.verts;
+  b.idx = dIdx;
+  b.nVerts = g.nVerts;
+  b.nTris = N;
+  b.keys = g.keys;
+  b.vals = g.vals;
+  b.keysAlt = keysAlt;
+  b.valsAlt = valsAlt;
+  b.keysUnsorted = g.keysUnsorted;
+  b.compressed = g.compressed;
+  b.runStarts = g.runStarts;
+  b.lr = g.lr;
+  b.lrCount = g.lrCount;
+  b.parent = parent;
+  b.visit = visit;
+  b.recs = g.recs;
+  b.tris = g.tris;
+  b.sortedIdx = g.sortedIdx;
+  b.params = g.params;
+  b.scratch = scratch;
+
+  cudaEvent_t e0, e1;
+  HRT_CUDA(ctx, cudaEventCreate(&e0));
+  HRT_CUDA(ctx, cudaEventCreate(&e1));
+  HRT_CUDA(ctx, cudaEventRecord(e0, st));
+  cudaError_t be = build_lbvh(b, ctx->numSMs, st);
+  HRT_CUDA(ctx, cudaEventRecord(e1, st));
+  if (be != cudaSuccess) return cuda_fail(ctx, be, "build_lbvh");
+  HRT_CUDA(ctx, cudaMemcpyAsync(&g.host, g.params, sizeof(BuildParams), cudaMemcpyDeviceToHost, st));
+  HRT_CUDA(ctx, cudaFreeAsync(dIdx, st));
+  HRT_CUDA(ctx, cudaFreeAsync(keysAlt, st));
+  HRT_CUDA(ctx, cudaFreeAsync(valsAlt, st));
+  HRT_CUDA(ctx, cudaFreeAsync(parent, st));
+  HRT_CUDA(ctx, cudaFreeAsync(visit, st));
+  HRT_CUDA(ctx, cudaFreeAsync(scratch, st));
+  HRT_CUDA(ctx, cudaStreamSynchronize(st));
+  cudaEventElapsedTime(&g.buildMs, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g.nLeaves = g.host.nLeaves;
+  for (int c = 0; c < 4; c++)
+  {
+    g.box[c] = g.host.bmin[c];
+    g.box[4 + c] = g.host.bmax[c];
+  }
+  const uint32_t err = g.host.error;
+  if (err & kErrIndexRange) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "triangle index >= vertex count");
+  if (err & kErrLeafCount)
+    return fail(ctx, HRT_ERR_CAPACITY, "more than 127 triangles share one Morton code (leaf count field overflows)");
+  if (err & kErrWaitTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "device look-back wait timed out during the build");
+  if (err & kErrLayout) return fail(ctx, HRT_ERR_DEVICE_CHECK, "refit did not reach the root exactly twice");
+  if (g.nLeaves == 0 || g.nLeaves > N) return fail(ctx, HRT_ERR_DEVICE_CHECK, "leaf count out of range");
+  return HRT_OK;
+}
+
+bool lbvh_builder_name(const char* name)
+{
+  if (!name || !*name) return true;
+  const std::string s(name);
+  return s.find("lbvh") != std::string::npos;  // "cbvh_lbvh", "lbvh", "cbvh_lbvh_gpu" (core/builders/cbvh.cpp:45-55)
+}
+
+int ensure_stage(hrt_scene* s, uint64_t n)
+{
+  if (n <= s->stageCap) return HRT_OK;
+  if (s->stageRays) cudaFree(s->stageRays);
+  if (s->stageOut) cudaFree(s->stageOut);
+  s->stageRays = s->stageOut = nullptr;
+  s->stageCap = 0;
+  HRT_CUDA(s->ctx, cudaMalloc(&s->stageRays, 32 * n));
+  HRT_CUDA(s->ctx, cudaMalloc(&s->stageOut, sizeof(hrt_hit) * n));
+  s->stageCap = n;
+  return HRT_OK;
+}
+
+int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out, int counting, cudaStream_t st)
+{
+  if (!s->committed) return fail(s->ctx, HRT_ERR_STATE, "query before hrt_commit_scene");
+  if (n == 0) return HRT_OK;
+  if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
+  TraceArgs a;
+  a.rays = reinterpret_cast<const float4*>(rays);
+  a.n = n;
+  a.inst = s->dInst;
+  a.nInst = s->nInstDev;
+  a.hits = out;
+  a.counters = s->dCounters;
+  a.errorWord = s->dError;
+  cudaError_t e = trace(a, kind, counting, s->ctx->numSMs, st);
+  if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
+  return HRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hrt_version(void) { return "heavyrt-gb300 0.1 (sm_103a)"; }
+
+const char* hrt_status_string(int status)
+{
+  switch (status)
+  {
+    case HRT_OK: return "ok";
+    case HRT_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case HRT_ERR_CUDA: return "CUDA error";
+    case HRT_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case HRT_ERR_CAPACITY: return "format capacity exceeded";
+    case HRT_ERR_STATE: return "call out of order";
+    case HRT_ERR_TIMEOUT: return "device wait timed out";
+    case HRT_ERR_DEVICE_CHECK: return "device-side check failed";
+    case HRT_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int hrt_context_create(int device, hrt_context** out)
+{
+  if (!out) return HRT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) return HRT_ERR_CUDA;
+  if (device < 0 || device >= count) return HRT_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(device) != cudaSuccess) return HRT_ERR_CUDA;
+  hrt_context* c = new hrt_context();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+  {
+    delete c;
+    return HRT_ERR_CUDA;
+  }
+  *out = c;
+  return HRT_OK;
+}
+
+int hrt_context_destroy(hrt_context* ctx)
+{
+  if (!ctx) return HRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HRT_OK;
+}
+
+const char* hrt_context_last_error(const hrt_context* ctx) { return ctx ? ctx->lastError.c_str() : "null context"; }
+
+int hrt_scene_create(hrt_context* ctx, const char* buildName, hrt_scene** out)
+{
+  if (!ctx || !out) return HRT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!lbvh_builder_name(buildName))
+    return fail(ctx, HRT_ERR_UNSUPPORTED, std::string("builder '") + buildName + "' is not an LBVH builder");
+  cudaSetDevice(ctx->device);
+  hrt_scene* s = new hrt_scene();
+  s->ctx = ctx;
+  if (cudaMalloc((void**)&s->dError, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc((void**)&s->dCounters, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(s->dError, 0, sizeof(uint32_t)) != cudaSuccess)
+  {
+    if (s->dError) cudaFree(s->dError);
+    if (s->dCounters) cudaFree(s->dCounters);
+    delete s;
+    return fail(ctx, HRT_ERR_OUT_OF_MEMORY, "scene allocation");
+  }
+  *out = s;
+  return HRT_OK;
+}
+
+int hrt_clear_geom(hrt_scene* s)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(s->mu);
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
+  for (Geom& gm : s->geoms) free_geom(gm);
+  s->geoms.clear();
+  s->insts.clear();
+  s->committed = false;
+  return HRT_OK;
+}
+
+int hrt_scene_destroy(hrt_scene* s)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  hrt_clear_geom(s);
+  if (s->dInst) cudaFree(s->dInst);
+  if (s->dError) cudaFree(s->dError);
+  if (s->dCounters) cudaFree(s->dCounters);
+  if (s->stageRays) cudaFree(s->stageRays);
+  if (s->stageOut) cudaFree(s->stageOut);
+  delete s;
+  return HRT_OK;
+}
+
+int hrt_add_geom_triangles3f(hrt_scene* s, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
+                             int quality, uint64_t vByteStride, uint32_t* geomId)
+{
+  (void)quality;
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  hrt_context* ctx = s->ctx;
+  if (vByteStride == 0) vByteStride = 12;
+  if (vByteStride < 12 || vByteStride % 4 != 0) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "vByteStride must be >= 12 and a multiple of 4");
+  if (nIdx % 3 != 0) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "index count is not a multiple of 3");
+  if ((nVert && !vpos) || (nIdx && !idx)) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "null vertex or index pointer");
+  if (nIdx / 3 > HRT_MAX_TRIS_PER_GEOM) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^24-1 triangles in one geometry");
+  if (nVert > 0xFFFFFFFFull) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^32-1 vertices in one geometry");
+  std::lock_guard<std::mutex> lk(s->mu);
+  cudaSetDevice(ctx->device);
+  Geom g;
+  const int st = build_geometry(s, g, vpos, nVert, idx, nIdx, vByteStride);
+  if (st != HRT_OK)
+  {
+    cudaStreamSynchronize(ctx->stream);
+    free_geom(g);
+    return st;
+  }
+  s->geoms.push_back(g);
+  s->committed = false;
+  if (geomId) *geomId = (uint32_t)(s->geoms.size() - 1);
+  return HRT_OK;
+}
+
+int hrt_update_geom_triangles3f(hrt_scene* s, uint32_t, const float*, uint64_t, const uint32_t*, uint64_t, int, uint64_t)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  return fail(s->ctx, HRT_ERR_UNSUPPORTED, "UpdateGeom_Triangles3f is not provided (the reference stubs it too)");
+}
+
+int hrt_clear_scene(hrt_scene* s)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(s->mu);
+  s->insts.clear();
+  s->committed = false;
+  return HRT_OK;
+}
+
+int hrt_add_instance(hrt_scene* s, uint32_t geomId, const float m[16], uint32_t* instId)
+{
+  if (!s || !m) return HRT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(s->mu);
+  if (geomId >= s->geoms.size()) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown geometry id");
+  Instance in;
+  in.geomId = geomId;
+  std::memcpy(in.m, m, sizeof(in.m));
+  in.identity = is_identity(m);
+  if (in.identity)
+  {
+    const float id12[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    std::memcpy(in.inv, id12, sizeof(id12));
+  }
+  else
+    inverse4x4(m, in.inv);
+  s->insts.push_back(in);
+  s->committed = false;
+  if (instId) *instId = (uint32_t)(s->insts.size() - 1);
+  return HRT_OK;
+}
+
+int hrt_update_instance(hrt_scene* s, uint32_t instId, const float m[16])
+{
+  if (!s || !m) return HRT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(s->mu);
+  if (instId >= s->insts.size()) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown instance id");
+  Instance& in = s->insts[instId];
+  std::memcpy(in.m, m, sizeof(in.m));
+  in.identity = is_identity(m);
+  if (!in.identity) inverse4x4(m, in.inv);
+  else
+  {
+    const float id12[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    std::memcpy(in.inv, id12, sizeof(id12));
+  }
+  s->committed = false;
+  return HRT_OK;
+}
+
+int hrt_commit_scene(hrt_scene* s, int quality)
+{
+  (void)quality;
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(s->mu);
+  hrt_context* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  std::vector<InstanceDesc> d(s->insts.size());
+  for (size_t i = 0; i < s->insts.size(); i++)
+  {
+    const Instance& in = s->insts[i];
+    const Geom& gm = s->geoms[in.geomId];
+    d[i].recs = gm.recs;
+    d[i].tris = gm.tris;
+    d[i].geomId = in.geomId;
+    d[i].instId = (uint32_t)i;
+    d[i].identity = in.identity ? 1u : 0u;
+    d[i].valid = gm.nTris > 0 ? 1u : 0u;
+    std::memcpy(d[i].inv, in.inv, sizeof(in.inv));
+  }
+  if (s->dInst) cudaFree(s->dInst);
+  s->dInst = nullptr;
+  s->nInstDev = (uint32_t)d.size();
+  if (!d.empty())
+  {
+    HRT_CUDA(ctx, cudaMalloc((void**)&s->dInst, sizeof(InstanceDesc) * d.size()));
+    HRT_CUDA(ctx, cudaMemcpy(s->dInst, d.data(), sizeof(InstanceDesc) * d.size(), cudaMemcpyHostToDevice));
+  }
+  s->committed = true;
+  return HRT_OK;
+}
+
+int hrt_query_nearest(hrt_scene* s, const float* rays, uint64_t n, hrt_hit* hits, void* stream)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  return launch_query(s, 0, rays, n, hits, 0, (cudaStream_t)stream);
+}
+
+int hrt_query_any(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out, void* stream)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  return launch_query(s, 1, rays, n, out, 0, (cudaStream_t)stream);
+}
+
+static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  if (n == 0) return HRT_OK;
+  if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
+  std::lock_guard<std::mutex> g(s->mu);
+  hrt_context* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  int st = ensure_stage(s, n);
+  if (st != HRT_OK) return st;
+  cudaStream_t cs = ctx->stream;
+  HRT_CUDA(ctx, cudaMemcpyAsync(s->stageRays, rays, 32 * n, cudaMemcpyHostToDevice, cs));
+  st = launch_query(s, kind, (const float*)s->stageRays, n, s->stageOut, 0, cs);
+  if (st != HRT_OK) return st;
+  const size_t outBytes = kind == 0 ? sizeof(hrt_hit) * n : n;
+  HRT_CUDA(ctx, cudaMemcpyAsync(out, s->stageOut, outBytes, cudaMemcpyDeviceToHost, cs));
+  HRT_CUDA(ctx, cudaStreamSynchronize(cs));
+  return HRT_OK;
+}
+
+int hrt_query_nearest_host(hrt_scene* s, const float* rays, uint64_t n, hrt_hit* hits)
+{
+  return query_host(s, 0, rays, n, hits);
+}
+
+int hrt_query_any_host(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out) { return query_host(s, 1, rays, n, out); }
+
+int hrt_query_counters(hrt_scene* s, int kind, const float* rays, uint64_t n, uint64_t counters[2], void* stream)
+{
+  if (!s || !counters || (kind != 0 && kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
+  hrt_context* ctx = s->ctx;
+  cudaStream_t cs = (cudaStream_t)stream;
+  void* out = nullptr;
+  HRT_CUDA(ctx, cudaMallocAsync(&out, kind == 0 ? sizeof(hrt_hit) * (n ? n : 1) : (n ? n : 1), cs));
+  HRT_CUDA(ctx, cudaMemsetAsync(s->dCounters, 0, 2 * sizeof(unsigned long long), cs));
+  HRT_CUDA(ctx, cudaMemsetAsync(s->dError, 0, sizeof(uint32_t), cs));
+  int st = launch_query(s, kind, rays, n, out, 1, cs);
+  unsigned long long c[2] = {0, 0};
+  uint32_t err = 0;
+  HRT_CUDA(ctx, cudaMemcpyAsync(c, s->dCounters, sizeof(c), cudaMemcpyDeviceToHost, cs));
+  HRT_CUDA(ctx, cudaMemcpyAsync(&err, s->dError, sizeof(err), cudaMemcpyDeviceToHost, cs));
+  HRT_CUDA(ctx, cudaFreeAsync(out, cs));
+  HRT_CUDA(ctx, cudaStreamSynchronize(cs));
+  if (st != HRT_OK) return st;
+  counters[0] = c[0];
+  counters[1] = c[1];
+  if (err & kErrStack) return fail(ctx, HRT_ERR_DEVICE_CHECK, "traversal stack bound exceeded");
+  return HRT_OK;
+}
+
+int hrt_get_geom_num(const hrt_scene* s, uint32_t* out)
+{
+  if (!s || !out) return HRT_ERR_INVALID_ARGUMENT;
+  *out = (uint32_t)s->geoms.size();
+  return HRT_OK;
+}
+
+int hrt_get_inst_num(const hrt_scene* s, uint32_t* out)
+{
+  if (!s || !out) return HRT_ERR_INVALID_ARGUMENT;
+  *out = (uint32_t)s->insts.size();
+  return HRT_OK;
+}
+
+int hrt_get_geom_boxes(const hrt_scene* s, float* boxes, uint32_t capacity)
+{
+  if (!s || (!boxes && capacity)) return HRT_ERR_INVALID_ARGUMENT;
+  const uint32_t n = (uint32_t)s->geoms.size();
+  for (uint32_t i = 0; i < n && i < capacity; i++) std::memcpy(boxes + 8 * i, s->geoms[i].box, 8 * sizeof(float));
+  return HRT_OK;
+}
+
+int hrt_geom_info(const hrt_scene* s, uint32_t geomId, uint64_t out[4], float* build_ms)
+{
+  if (!s || !out || geomId >= s->geoms.size()) return HRT_ERR_INVALID_ARGUMENT;
+  const Geom& g = s->geoms[geomId];
+  out[0] = g.nTris;
+  out[1] = g.nLeaves;
+  out[2] = g.nLeaves > 1 ? g.nLeaves - 1 : (g.nTris ? 1 : 0);
+  out[3] = g.bytes;
+  if (build_ms) *build_ms = g.buildMs;
+  return HRT_OK;
+}
+
+int hrt_geom_export(const hrt_scene* s, uint32_t geomId, int what, void* dst, uint64_t capacityBytes, uint64_t* sizeBytes)
+{
+  if (!s || geomId >= s->geoms.size()) return HRT_ERR_INVALID_ARGUMENT;
+  hrt_context* ctx = s->ctx;
+  const Geom& g = s->geoms[geomId];
+  const uint64_t N = g.nTris, L = g.nLeaves, nLR = L ? 2 * L - 1 : 0;
+  uint64_t size = 0;
+  switch (what)
+  {
+    case HRT_EXPORT_SCENE_BOX: size = 12 * sizeof(float); break;
+    case HRT_EXPORT_MORTON_SORTED:
+    case HRT_EXPORT_MORTON_UNSORTED: size = 8 * N; break;
+    case HRT_EXPORT_COMPRESSED:
+    case HRT_EXPORT_RUN_STARTS: size = 4 * L; break;
+    case HRT_EXPORT_LR_NODES: size = 32 * nLR; break;
+    case HRT_EXPORT_LR_COUNTS: size = 4 * nLR; break;
+    case HRT_EXPORT_PRIM_INDICES: size = 4 * N; break;
+    case HRT_EXPORT_SORTED_INDICES: size = 12 * N; break;
+    default: return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "unknown export id");
+  }
+  if (sizeBytes) *sizeBytes = size;
+  if (!dst) return HRT_OK;
+  if (capacityBytes < size) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "export buffer too small");
+  if (size == 0) return HRT_OK;
+  cudaSetDevice(ctx->device);
+  switch (what)
+  {
+    case HRT_EXPORT_SCENE_BOX:
+      std::memcpy(dst, g.host.bmin, 12 * sizeof(float));
+      return HRT_OK;
+    case HRT_EXPORT_MORTON_SORTED:
+    case HRT_EXPORT_MORTON_UNSORTED:
+    {
+      std::vector<uint32_t> k(N), v(N);
+      const uint32_t* src = what == HRT_EXPORT_MORTON_SORTED ? g.keys : g.keysUnsorted;
+      HRT_CUDA(ctx, cudaMemcpy(k.data(), src, 4 * N, cudaMemcpyDeviceToHost));
+      if (what == HRT_EXPORT_MORTON_SORTED) HRT_CUDA(ctx, cudaMemcpy(v.data(), g.vals, 4 * N, cudaMemcpyDeviceToHost));
+      else
+        for (uint64_t i = 0; i < N; i++) v[i] = (uint32_t)i;
+      uint32_t* o = (uint32_t*)dst;
+      for (uint64_t i = 0; i < N; i++)
+      {
+        o[2 * i] = k[i];
+        o[2 * i + 1] = v[i];
+      }
+      return HRT_OK;
+    }
+    case HRT_EXPORT_COMPRESSED: HRT_CUDA(ctx, cudaMemcpy(dst, g.compressed, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_RUN_STARTS: HRT_CUDA(ctx, cudaMemcpy(dst, g.runStarts, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_LR_NODES: HRT_CUDA(ctx, cudaMemcpy(dst, g.lr, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_LR_COUNTS: HRT_CUDA(ctx, cudaMemcpy(dst, g.lrCount, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_PRIM_INDICES: HRT_CUDA(ctx, cudaMemcpy(dst, g.vals, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_SORTED_INDICES: HRT_CUDA(ctx, cudaMemcpy(dst, g.sortedIdx, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    default: break;
+  }
+  return HRT_ERR_INVALID_ARGUMENT;
+}
+
+int hrt_host_alloc(uint64_t bytes, void** out)
+{
+  if (!out) return HRT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) return HRT_ERR_OUT_OF_MEMORY;
+  return HRT_OK;
+}
+
+int hrt_host_free(void* p)
+{
+  if (p && cudaFreeHost(p) != cudaSuccess) return HRT_ERR_CUDA;
+  return HRT_OK;
+}
+
+}  // extern "C"

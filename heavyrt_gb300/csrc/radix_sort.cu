@@ -1,0 +1,263 @@
+// Onesweep LSD radix sort of (Morton code, triangle id) pairs.
+//
+// Replaces the reference's std::sort on the code (core/builders/lbvh.cpp:755)
+// with a stable GPU sort (Adinets & Merrill, "Onesweep: A Faster Least
+// Significant Digit Radix Sort for GPUs", 2022):
+//   1. one histogram pass counts all four 8-bit digits of every key;
+//   2. a one-block kernel turns the four histograms into exclusive digit bases;
+//   3. four digit passes, each ONE kernel: a tile of 4096 pairs is ranked in
+//      shared memory (warp-level __match_any_sync ranking, stable), the tile's
+//      per-digit counts are published and the exclusive prefix over earlier
+//      tiles is found by decoupled look-back, then the tile is written out
+//      grouped by digit.
+// Tiles are numbered in the order blocks start (atomic ticket), so every tile
+// a block waits on belongs to a block that is already resident; each wait is
+// still bounded and reports kErrWaitTimeout instead of spinning forever.
+#include "hrt_kernels.cuh"
+
+namespace hrt
+{
+namespace
+{
+
+constexpr int      kThreads    = 256;
+constexpr int      kWarps      = kThreads / 32;
+constexpr int      kItems      = 16;
+constexpr uint32_t kTile       = kThreads * kItems;  // 4096 pairs
+constexpr int      kRadix      = 256;
+constexpr int      kPasses     = 4;
+constexpr uint32_t kFlagAgg    = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValueMask  = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit  = 1u << 22;
+
+__device__ __forceinline__ void store_relaxed(uint32_t* p, uint32_t v)
+{
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t load_relaxed(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_histogram(const uint32_t* __restrict__ keys, uint32_t n,
+                                                        uint32_t* __restrict__ hist)
+{
+  __shared__ uint32_t sh[kPasses * kRadix];
+  for (int i = threadIdx.x; i < kPasses * kRadix; i += kThreads) sh[i] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+  {
+    const uint32_t k = keys[i];
+#pragma unroll
+    for (int p = 0; p < kPasses; p++) atomicAdd(&sh[p * kRadix + ((k >> (8 * p)) & 0xFF)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kPasses * kRadix; i += kThreads)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// Exclusive scan of a value held by each of the 256 threads; returns the
+// exclusive prefix, *total receives the sum.  Uses `warpSums` (8 entries).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warpSums, uint32_t* total)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warpSums[warp] = incl;
+  __syncthreads();
+  if (warp == 0)
+  {
+    uint32_t w = (lane < kWarps) ? warpSums[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kWarps) warpSums[lane] = wi - w;  // exclusive per warp
+    if (lane == kWarps - 1) warpSums[kWarps] = wi;
+  }
+  __syncthreads();
+  const uint32_t r = incl - v + warpSums[warp];
+  *total = warpSums[kWarps];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kThreads) k_scan_histograms(uint32_t* __restrict__ hist)
+{
+  __shared__ uint32_t warpSums[kWarps + 1];
+  for (int p = 0; p < kPasses; p++)
+  {
+    uint32_t total;
+    const uint32_t v = hist[p * kRadix + threadIdx.x];
+    const uint32_t e = block_exclusive_scan(v, warpSums, &total);
+    hist[p * kRadix + threadIdx.x] = e;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restrict__ keysIn,
+                                                       const uint32_t* __restrict__ valsIn,
+                                                       uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
+                                                       uint32_t n, uint32_t shift, const uint32_t* __restrict__ digitBase,
+                                                       uint32_t* tileStatus, uint32_t* tileCounter, uint32_t* errorWord)
+{
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warpHist[kWarps][kRadix];  // counts, then per-warp exclusive offsets
+  __shared__ uint32_t s_digitStart[kRadix];        // tile-local start of each digit
+  __shared__ uint32_t s_dst[kRadix];               // global position = s_dst[d] + tile-local position
+  __shared__ uint32_t s_warpSums[kWarps + 1];
+  __shared__ uint32_t s_keys[kTile];
+  __shared__ uint32_t s_vals[kTile];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(tileCounter, 1u);
+  for (int i = tid; i < kWarps * kRadix; i += kThreads) (&s_warpHist[0][0])[i] = 0u;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t tileBase = tile * kTile;
+  const uint32_t warpBase = tileBase + warp * (kItems * 32);
+
+  // Warp-striped load: item k of lane l is element warpBase + 32k + l, so the
+  // (warp, k, lane) order is the input order and the ranking below is stable.
+  uint32_t key[kItems], val[kItems], rank[kItems];
+#pragma unroll
+  for (int k = 0; k < kItems; k++)
+  {
+    const uint32_t i = warpBase + k * 32 + lane;
+    const bool valid = i < n;
+    key[k] = valid ? keysIn[i] : 0xFFFFFFFFu;
+    val[k] = valid ? valsIn[i] : 0u;
+  }
+  const uint32_t ltMask = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < kItems; k++)
+  {
+    const bool valid = (warpBase + k * 32 + lane) < n;
+    const uint32_t digit = (key[k] >> shift) & 0xFF;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? digit : (0x100u + lane));
+    const uint32_t before = s_warpHist[warp][digit];
+    rank[k] = before + __popc(peers & ltMask);
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) s_warpHist[warp][digit] = before + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // Thread d owns digit d: per-warp offsets, tile total, publish, look back.
+  const uint32_t d = tid;
+  uint32_t total = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++)
+  {
+    const uint32_t c = s_warpHist[w][d];
+    s_warpHist[w][d] = total;
+    total += c;
+  }
+  uint32_t* myStatus = tileStatus + (size_t)tile * kRadix + d;
+  store_relaxed(myStatus, (tile == 0 ? kFlagPrefix : kFlagAgg) | total);
+  uint32_t blockTotal;
+  s_digitStart[d] = block_exclusive_scan(total, s_warpSums, &blockTotal);
+
+  uint32_t excl = 0;
+  if (tile > 0)
+  {
+    int64_t t = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (t >= 0)
+    {
+      const uint32_t s = load_relaxed(tileStatus + (size_t)t * kRadix + d);
+      const uint32_t flag = s & ~kValueMask;
+      if (flag == 0u)
+      {
+        if (++spins > kSpinLimit)
+        {
+          atomicOr(errorWord, kErrWaitTimeout);
+          break;
+        }
+        if (spins > 64) __nanosleep(32);
+        continue;
+      }
+      excl += s & kValueMask;
+      if (flag == kFlagPrefix) break;
+      t--;
+    }
+    store_relaxed(myStatus, kFlagPrefix | (excl + total));
+  }
+  s_dst[d] = digitBase[d] + excl - s_digitStart[d];
+  __syncthreads();
+
+#pragma unroll
+  for (int k = 0; k < kItems; k++)
+  {
+    if ((warpBase + k * 32 + lane) < n)
+    {
+      const uint32_t digit = (key[k] >> shift) & 0xFF;
+      const uint32_t pos = s_digitStart[digit] + s_warpHist[warp][digit] + rank[k];
+      s_keys[pos] = key[k];
+      s_vals[pos] = val[k];
+    }
+  }
+  __syncthreads();
+
+  const uint32_t count = (n - tileBase < kTile) ? (n - tileBase) : kTile;
+  for (uint32_t i = tid; i < count; i += kThreads)
+  {
+    const uint32_t k = s_keys[i];
+    const uint32_t dst = s_dst[(k >> shift) & 0xFF] + i;
+    if (dst < n)  // always true unless a look-back wait gave up (reported through errorWord)
+    {
+      keysOut[dst] = k;
+      valsOut[dst] = s_vals[i];
+    }
+  }
+}
+
+}  // namespace
+
+size_t radix_sort_scratch_bytes(uint32_t n)
+{
+  const size_t tiles = (n + kTile - 1) / kTile;
+  return sizeof(uint32_t) * (kPasses * kRadix + kPasses + 4 + (size_t)kPasses * tiles * kRadix);
+}
+
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, uint32_t* valsAlt, uint32_t n,
+                             void* scratch, uint32_t* errorWord, int numSMs, cudaStream_t stream)
+{
+  if (n <= 1) return cudaSuccess;
+  const uint32_t tiles = (n + kTile - 1) / kTile;
+  uint32_t* hist = (uint32_t*)scratch;
+  uint32_t* counters = hist + kPasses * kRadix;
+  uint32_t* status = counters + kPasses + 4;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, radix_sort_scratch_bytes(n), stream);
+  if (e != cudaSuccess) return e;
+  uint32_t hb = (n + kThreads - 1) / kThreads;
+  const uint32_t maxHb = (uint32_t)numSMs * 4u;
+  if (hb > maxHb) hb = maxHb;
+  k_histogram<<<hb, kThreads, 0, stream>>>(keys, n, hist);
+  k_scan_histograms<<<1, kThreads, 0, stream>>>(hist);
+  uint32_t* srcK = keys;
+  uint32_t* srcV = vals;
+  uint32_t* dstK = keysAlt;
+  uint32_t* dstV = valsAlt;
+  for (int p = 0; p < kPasses; p++)
+  {
+    k_onesweep<<<tiles, kThreads, 0, stream>>>(srcK, srcV, dstK, dstV, n, 8u * p, hist + p * kRadix,
+                                               status + (size_t)p * tiles * kRadix, counters + p, errorWord);
+    uint32_t* t = srcK; srcK = dstK; dstK = t;
+    t = srcV; srcV = dstV; dstV = t;
+  }
+  return cudaGetLastError();  // four passes: the result is back in keys/vals
+}
+
+}  // namespace hrt

@@ -1,0 +1,341 @@
+"""Python binding of the engine's C ABI (include/hrt.h) and a mirror of
+HeavyRT's ISceneObject plugin interface (core/CrossRT.h:64-196).
+
+The binding loads heavyrt_gb300/_build/libhrt.so and fails loudly when it is
+missing: there is no CPU fallback.  Method names, argument meaning and
+defaults follow ISceneObject so that code written against HeavyRT's interface
+reads the same here; the ray queries are batched (arrays of rays) because a
+per-ray call cannot be fast on a GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_BUILD = Path(__file__).resolve().parent / "_build"
+
+# statuses (include/hrt.h)
+HRT_OK = 0
+HRT_ERR_INVALID_ARGUMENT = 1
+HRT_ERR_CUDA = 2
+HRT_ERR_OUT_OF_MEMORY = 3
+HRT_ERR_CAPACITY = 4
+HRT_ERR_STATE = 5
+HRT_ERR_TIMEOUT = 6
+HRT_ERR_DEVICE_CHECK = 7
+HRT_ERR_UNSUPPORTED = 8
+
+# BuildQuality, core/CrossRT.h:9-15
+BUILD_LOW, BUILD_MEDIUM, BUILD_HIGH, BUILD_REFIT = 0, 1, 2, 3
+
+# exports (include/hrt.h)
+EXPORT_SCENE_BOX = 0
+EXPORT_MORTON_SORTED = 1
+EXPORT_COMPRESSED = 2
+EXPORT_RUN_STARTS = 3
+EXPORT_LR_NODES = 4
+EXPORT_LR_COUNTS = 5
+EXPORT_PRIM_INDICES = 6
+EXPORT_SORTED_INDICES = 7
+EXPORT_MORTON_UNSORTED = 8
+
+# CRT_Hit, core/CrossRT.h:20-27
+HIT_DTYPE = np.dtype([("t", "<f4"), ("primId", "<u4"), ("instId", "<u4"), ("geomId", "<u4"), ("coords", "<f4", (4,))])
+# BVHNode, core/builders/cbvh.h:20-26
+NODE_DTYPE = np.dtype([("boxMin", "<f4", (3,)), ("leftOffset", "<u4"), ("boxMax", "<f4", (3,)), ("escapeIndex", "<u4")])
+
+_EXPORT_DTYPES = {
+    EXPORT_SCENE_BOX: np.float32,
+    EXPORT_MORTON_SORTED: np.uint32,
+    EXPORT_MORTON_UNSORTED: np.uint32,
+    EXPORT_COMPRESSED: np.uint32,
+    EXPORT_RUN_STARTS: np.uint32,
+    EXPORT_LR_NODES: NODE_DTYPE,
+    EXPORT_LR_COUNTS: np.uint32,
+    EXPORT_PRIM_INDICES: np.uint32,
+    EXPORT_SORTED_INDICES: np.uint32,
+}
+
+
+class HrtError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"hrt status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _BUILD / "libhrt.so"
+
+
+def lib() -> C.CDLL:
+    """The loaded engine library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = library_path()
+    if not p.exists():
+        raise RuntimeError(f"native engine not built ({p} missing): run __graft_entry__.build()")
+    L = C.CDLL(str(p))
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    sig = {
+        "hrt_context_create": (i32, [i32, C.POINTER(vp)]),
+        "hrt_context_destroy": (i32, [vp]),
+        "hrt_context_last_error": (C.c_char_p, [vp]),
+        "hrt_status_string": (C.c_char_p, [i32]),
+        "hrt_version": (C.c_char_p, []),
+        "hrt_scene_create": (i32, [vp, C.c_char_p, C.POINTER(vp)]),
+        "hrt_scene_destroy": (i32, [vp]),
+        "hrt_clear_geom": (i32, [vp]),
+        "hrt_add_geom_triangles3f": (i32, [vp, vp, u64, vp, u64, i32, u64, C.POINTER(u32)]),
+        "hrt_update_geom_triangles3f": (i32, [vp, u32, vp, u64, vp, u64, i32, u64]),
+        "hrt_clear_scene": (i32, [vp]),
+        "hrt_add_instance": (i32, [vp, u32, vp, C.POINTER(u32)]),
+        "hrt_update_instance": (i32, [vp, u32, vp]),
+        "hrt_commit_scene": (i32, [vp, i32]),
+        "hrt_query_nearest": (i32, [vp, vp, u64, vp, vp]),
+        "hrt_query_any": (i32, [vp, vp, u64, vp, vp]),
+        "hrt_query_nearest_host": (i32, [vp, vp, u64, vp]),
+        "hrt_query_any_host": (i32, [vp, vp, u64, vp]),
+        "hrt_query_counters": (i32, [vp, i32, vp, u64, vp, vp]),
+        "hrt_get_geom_num": (i32, [vp, C.POINTER(u32)]),
+        "hrt_get_inst_num": (i32, [vp, C.POINTER(u32)]),
+        "hrt_get_geom_boxes": (i32, [vp, vp, u32]),
+        "hrt_geom_info": (i32, [vp, u32, vp, C.POINTER(C.c_float)]),
+        "hrt_geom_export": (i32, [vp, u32, i32, vp, u64, C.POINTER(u64)]),
+        "hrt_host_alloc": (i32, [u64, C.POINTER(vp)]),
+        "hrt_host_free": (i32, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One GPU (hrt_context)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        st = lib().hrt_context_create(device, C.byref(self._h))
+        if st != HRT_OK:
+            raise HrtError(st, f"hrt_context_create({device}): {lib().hrt_status_string(st).decode()}")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self) -> str:
+        return lib().hrt_context_last_error(self._h).decode()
+
+    def check(self, st: int, what: str):
+        if st != HRT_OK:
+            raise HrtError(st, f"{what}: {self.last_error() or lib().hrt_status_string(st).decode()}")
+
+    def close(self):
+        if self._h:
+            lib().hrt_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _as_rays(posAndNear, dirAndFar=None) -> np.ndarray:
+    """Interleaved float32 [n, 8] rays from (pos, dir) float4 arrays or an [n, 8] array."""
+    if dirAndFar is None:
+        r = np.ascontiguousarray(posAndNear, dtype=np.float32).reshape(-1, 8)
+        return r
+    p = np.asarray(posAndNear, dtype=np.float32).reshape(-1, 4)
+    d = np.asarray(dirAndFar, dtype=np.float32).reshape(-1, 4)
+    if p.shape != d.shape:
+        raise ValueError("posAndNear and dirAndFar must have the same length")
+    return np.ascontiguousarray(np.concatenate([p, d], axis=1))
+
+
+class SceneRT:
+    """GPU LBVH scene behind HeavyRT's ISceneObject interface (core/CrossRT.h:64-193)."""
+
+    def __init__(self, ctx: Context | None = None, build_name: str = "cbvh_lbvh"):
+        self.ctx = ctx or default_context()
+        self._h = C.c_void_p()
+        self.ctx.check(lib().hrt_scene_create(self.ctx.handle, build_name.encode() if build_name else None,
+                                              C.byref(self._h)), "hrt_scene_create")
+        self._build_name = build_name
+
+    # ---- ISceneObject ---------------------------------------------------
+    def Name(self) -> str:  # ISceneObject::Name, core/CrossRT.h:72
+        return "GB300_LBVH"
+
+    def BuildName(self) -> str:  # core/CrossRT.h:77
+        return self._build_name
+
+    def ClearGeom(self):  # core/CrossRT.h:82
+        self.ctx.check(lib().hrt_clear_geom(self._h), "ClearGeom")
+
+    def AddGeom_Triangles3f(self, a_vpos3f, a_vertNumber=None, a_triIndices=None, a_indNumber=None,
+                            a_qualityLevel=BUILD_HIGH, vByteStride=12) -> int:  # core/CrossRT.h:94
+        v = np.ascontiguousarray(a_vpos3f, dtype=np.float32)
+        idx = np.ascontiguousarray(a_triIndices, dtype=np.uint32).reshape(-1)
+        stride = int(vByteStride) if vByteStride else 12
+        if a_vertNumber is None:
+            a_vertNumber = v.size * 4 // stride
+        if a_indNumber is None:
+            a_indNumber = idx.size
+        if v.size * 4 < a_vertNumber * stride - (stride - 12):
+            raise ValueError("vertex array smaller than a_vertNumber * vByteStride")
+        gid = C.c_uint32()
+        self.ctx.check(lib().hrt_add_geom_triangles3f(self._h, _ptr(v), int(a_vertNumber), _ptr(idx), int(a_indNumber),
+                                                      int(a_qualityLevel), stride, C.byref(gid)),
+                       "AddGeom_Triangles3f")
+        return gid.value
+
+    def UpdateGeom_Triangles3f(self, a_geomId, a_vpos3f, a_vertNumber, a_triIndices, a_indNumber,
+                               a_qualityLevel=BUILD_HIGH, vByteStride=12):  # core/CrossRT.h:105
+        v = np.ascontiguousarray(a_vpos3f, dtype=np.float32)
+        idx = np.ascontiguousarray(a_triIndices, dtype=np.uint32)
+        self.ctx.check(lib().hrt_update_geom_triangles3f(self._h, a_geomId, _ptr(v), a_vertNumber, _ptr(idx), a_indNumber,
+                                                         a_qualityLevel, vByteStride), "UpdateGeom_Triangles3f")
+
+    def ClearScene(self):  # core/CrossRT.h:110
+        self.ctx.check(lib().hrt_clear_scene(self._h), "ClearScene")
+
+    def CommitScene(self, a_qualityLevel=BUILD_MEDIUM):  # core/CrossRT.h:115
+        self.ctx.check(lib().hrt_commit_scene(self._h, int(a_qualityLevel)), "CommitScene")
+
+    def AddInstance(self, a_geomId: int, a_matrix=None) -> int:  # core/CrossRT.h:123
+        m = np.eye(4, dtype=np.float32) if a_matrix is None else np.asarray(a_matrix, dtype=np.float32).reshape(4, 4)
+        col = np.ascontiguousarray(m.T)  # column-major storage
+        iid = C.c_uint32()
+        self.ctx.check(lib().hrt_add_instance(self._h, a_geomId, _ptr(col), C.byref(iid)), "AddInstance")
+        return iid.value
+
+    def UpdateInstance(self, a_instanceId: int, a_matrix):  # core/CrossRT.h:130
+        col = np.ascontiguousarray(np.asarray(a_matrix, dtype=np.float32).reshape(4, 4).T)
+        self.ctx.check(lib().hrt_update_instance(self._h, a_instanceId, _ptr(col)), "UpdateInstance")
+
+    def RayQuery_NearestHit(self, posAndNear, dirAndFar=None) -> np.ndarray:  # core/CrossRT.h:143 (batched)
+        rays = _as_rays(posAndNear, dirAndFar)
+        out = np.empty(rays.shape[0], dtype=HIT_DTYPE)
+        self.ctx.check(lib().hrt_query_nearest_host(self._h, _ptr(rays), rays.shape[0], _ptr(out)), "RayQuery_NearestHit")
+        return out
+
+    def RayQuery_AnyHit(self, posAndNear, dirAndFar=None) -> np.ndarray:  # core/CrossRT.h:151 (batched)
+        rays = _as_rays(posAndNear, dirAndFar)
+        out = np.empty(rays.shape[0], dtype=np.uint8)
+        self.ctx.check(lib().hrt_query_any_host(self._h, _ptr(rays), rays.shape[0], _ptr(out)), "RayQuery_AnyHit")
+        return out.astype(bool)
+
+    def GetGeomNum(self) -> int:  # core/CrossRT.h:163
+        n = C.c_uint32()
+        self.ctx.check(lib().hrt_get_geom_num(self._h, C.byref(n)), "GetGeomNum")
+        return n.value
+
+    def GetInstNum(self) -> int:  # core/CrossRT.h:164
+        n = C.c_uint32()
+        self.ctx.check(lib().hrt_get_inst_num(self._h, C.byref(n)), "GetInstNum")
+        return n.value
+
+    def GetGeomBoxes(self) -> np.ndarray:  # core/CrossRT.h:165, float4 pairs (boxMin, boxMax)
+        n = self.GetGeomNum()
+        out = np.empty((n, 8), dtype=np.float32)
+        self.ctx.check(lib().hrt_get_geom_boxes(self._h, _ptr(out), n), "GetGeomBoxes")
+        return out
+
+    # ---- engine extensions ----------------------------------------------
+    def query_device(self, kind: int, rays_ptr: int, n: int, out_ptr: int, stream: int = 0):
+        """Asynchronous query on device arrays (kind 0 nearest -> CRT_Hit[n], 1 any -> uint8[n])."""
+        f = lib().hrt_query_nearest if kind == 0 else lib().hrt_query_any
+        self.ctx.check(f(self._h, C.c_void_p(rays_ptr), n, C.c_void_p(out_ptr), C.c_void_p(stream)), "query")
+
+    def query_counters(self, kind: int, rays_ptr: int, n: int, stream: int = 0):
+        c = (C.c_uint64 * 2)()
+        self.ctx.check(lib().hrt_query_counters(self._h, kind, C.c_void_p(rays_ptr), n, c, C.c_void_p(stream)),
+                       "query_counters")
+        return int(c[0]), int(c[1])
+
+    def geom_info(self, geom_id: int = 0) -> dict:
+        out = (C.c_uint64 * 4)()
+        ms = C.c_float()
+        self.ctx.check(lib().hrt_geom_info(self._h, geom_id, out, C.byref(ms)), "geom_info")
+        return {"tris": out[0], "leaves": out[1], "pairs": out[2], "bytes": out[3], "build_ms": ms.value}
+
+    def export(self, geom_id: int, what: int) -> np.ndarray:
+        size = C.c_uint64()
+        self.ctx.check(lib().hrt_geom_export(self._h, geom_id, what, None, 0, C.byref(size)), "export size")
+        dt = np.dtype(_EXPORT_DTYPES[what])
+        out = np.empty(size.value // dt.itemsize, dtype=dt)
+        if size.value:
+            self.ctx.check(lib().hrt_geom_export(self._h, geom_id, what, _ptr(out), size.value, C.byref(size)), "export")
+        return out
+
+    def close(self):
+        if self._h:
+            lib().hrt_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def CreateSceneRT(a_implName: str = "GB300_LBVH", a_buildName: str = "cbvh_lbvh", a_layoutName: str = "") -> SceneRT:
+    """Factory mirroring CreateSceneRT (core/FactoryRT.cpp:29-78, core/CrossRT.h:195)."""
+    if a_implName not in ("GB300_LBVH", "BVH2Common"):
+        raise HrtError(HRT_ERR_UNSUPPORTED, f"implementation '{a_implName}' is not provided by this engine")
+    return SceneRT(build_name=a_buildName)
+
+
+def DeleteSceneRT(scene: SceneRT):  # core/CrossRT.h:196
+    scene.close()
+
+
+class PinnedBuffer:
+    """Page-locked host buffer (hrt_host_alloc) viewed as a numpy array."""
+
+    def __init__(self, nbytes: int):
+        self._p = C.c_void_p()
+        st = lib().hrt_host_alloc(nbytes, C.byref(self._p))
+        if st != HRT_OK:
+            raise HrtError(st, "hrt_host_alloc")
+        self.nbytes = nbytes
+
+    def array(self, dtype, count=None) -> np.ndarray:
+        dt = np.dtype(dtype)
+        count = self.nbytes // dt.itemsize if count is None else count
+        buf = (C.c_char * (count * dt.itemsize)).from_address(self._p.value)
+        return np.frombuffer(buf, dtype=dt, count=count)
+
+    @property
+    def ptr(self) -> int:
+        return self._p.value
+
+    def free(self):
+        if self._p:
+            lib().hrt_host_free(self._p)
+            self._p = C.c_void_p()

@@ -1,0 +1,190 @@
+/*
+ * hrt.h -- C ABI of the GB300 ray-query engine (LBVH build + BVH2 nearest/any-hit
+ * traversal on one GPU).
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (HRT_OK = 0).  The text of the last failure of a context is available from
+ * hrt_context_last_error().  The functions mirror HeavyRT's ISceneObject plugin
+ * interface (core/CrossRT.h:64-196); the C++ adapter in
+ * heavyrt_gb300/csrc/scene_rt_adapter.cpp implements ISceneObject on top of them.
+ *
+ * Semantics shared by all calls:
+ *   - Ray records are two float4 per ray, {posAndNear, dirAndFar}, exactly the
+ *     arguments of ISceneObject::RayQuery_NearestHit (core/CrossRT.h:143).
+ *   - Hit records are HeavyRT's CRT_Hit (core/CrossRT.h:20-27), 32 bytes:
+ *     t, primId, instId, geomId, coords[4] with (u, v) in coords[0..1].  A miss
+ *     has t = tFar and primId = instId = geomId = 0xFFFFFFFF.
+ *   - primId is the triangle's position in the BVH's Morton-sorted order, as the
+ *     reference returns it (core/BVH2CommonRT.cpp:40, REMAP_PRIM_ID off at
+ *     core/CrossRT.h:29); hrt_geom_export(HRT_EXPORT_PRIM_INDICES) maps it to the
+ *     original triangle index.
+ *   - Build calls (add/commit) must not run concurrently with queries on the
+ *     same scene; queries may run concurrently with each other.
+ *   - Device pointers and `stream` (a cudaStream_t, NULL = legacy default
+ *     stream) belong to the caller; the engine owns every BVH buffer.
+ */
+#ifndef HRT_H
+#define HRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- statuses */
+#define HRT_OK                  0
+#define HRT_ERR_INVALID_ARGUMENT 1  /* null pointer, bad id, size out of range      */
+#define HRT_ERR_CUDA            2  /* a CUDA runtime call failed                    */
+#define HRT_ERR_OUT_OF_MEMORY   3  /* device allocation refused                     */
+#define HRT_ERR_CAPACITY        4  /* input exceeds a format limit (see below)      */
+#define HRT_ERR_STATE           5  /* call out of order, e.g. query before commit   */
+#define HRT_ERR_TIMEOUT         6  /* a bounded device-side wait gave up            */
+#define HRT_ERR_DEVICE_CHECK    7  /* a device-side bounds/consistency check failed */
+#define HRT_ERR_UNSUPPORTED     8  /* feature not provided                          */
+
+/* Format limits, checked at build time (HRT_ERR_CAPACITY beyond them):
+ *   triangles per geometry  <= 2^24 - 1  (leaf start field, core/raytrace_common.h:38-51)
+ *   triangles per leaf      <= 127       (leaf count field; the reference silently
+ *                                         corrupts the leaf beyond it, core/builders/lbvh.cpp:382) */
+#define HRT_MAX_TRIS_PER_GEOM   ((1u << 24) - 1u)
+#define HRT_MAX_TRIS_PER_LEAF   127u
+
+/* Build quality, HeavyRT's BuildQuality (core/CrossRT.h:9-15).  All values
+ * build the same LBVH; BUILD_REFIT is accepted by hrt_update_geom_triangles3f. */
+#define HRT_BUILD_LOW    0
+#define HRT_BUILD_MEDIUM 1
+#define HRT_BUILD_HIGH   2
+#define HRT_BUILD_REFIT  3
+
+typedef struct hrt_context hrt_context;
+typedef struct hrt_scene   hrt_scene;
+
+/* CRT_Hit, core/CrossRT.h:20-27. */
+typedef struct hrt_hit
+{
+  float    t;
+  uint32_t primId;
+  uint32_t instId;
+  uint32_t geomId;
+  float    coords[4];
+} hrt_hit;
+
+/* ---------------------------------------------------------------- context */
+
+/* Opens the engine on CUDA device `device`.  No reference counterpart: the
+ * reference runs on the host only. */
+int hrt_context_create(int device, hrt_context** out);
+int hrt_context_destroy(hrt_context* ctx);
+/* Text of the most recent failure on this context ("" if none). */
+const char* hrt_context_last_error(const hrt_context* ctx);
+/* Static text for a status code. */
+const char* hrt_status_string(int status);
+/* Engine version string. */
+const char* hrt_version(void);
+
+/* ---------------------------------------------------------------- scenes */
+
+/* Replaces CreateSceneRT(a_implName, a_buildName, a_layoutName) for the
+ * "BVH2Common" + "cbvh_lbvh" combination (core/FactoryRT.cpp:29-78,
+ * core/CrossRT.h:195).  buildName may be NULL or any of HeavyRT's builder
+ * strings that select the LBVH ("cbvh_lbvh", "lbvh", "cbvh_lbvh_gpu");
+ * anything else is HRT_ERR_UNSUPPORTED. */
+int hrt_scene_create(hrt_context* ctx, const char* buildName, hrt_scene** out);
+/* Replaces DeleteSceneRT (core/CrossRT.h:196). */
+int hrt_scene_destroy(hrt_scene* scene);
+
+/* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */
+int hrt_clear_geom(hrt_scene* scene);
+
+/* ISceneObject::AddGeom_Triangles3f (core/CrossRT.h:94; reference implementation
+ * core/BVH2CommonRT_host.cpp:66-98).  Host arrays: vpos has nVert vertices of
+ * vByteStride bytes (0 means 12), xyz first; idx has nIdx indices (3 per
+ * triangle).  The data is copied; the LBVH is built on the GPU before the call
+ * returns.  *geomId receives the new geometry id. */
+int hrt_add_geom_triangles3f(hrt_scene* scene, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
+                             int quality, uint64_t vByteStride, uint32_t* geomId);
+
+/* ISceneObject::UpdateGeom_Triangles3f (core/CrossRT.h:105).  The reference
+ * stubs it (core/BVH2CommonRT_host.cpp:100-103); here it returns
+ * HRT_ERR_UNSUPPORTED. */
+int hrt_update_geom_triangles3f(hrt_scene* scene, uint32_t geomId, const float* vpos, uint64_t nVert,
+                                const uint32_t* idx, uint64_t nIdx, int quality, uint64_t vByteStride);
+
+/* ISceneObject::ClearScene (core/CrossRT.h:110): drops instances, keeps geometry. */
+int hrt_clear_scene(hrt_scene* scene);
+
+/* ISceneObject::AddInstance (core/CrossRT.h:123; core/BVH2CommonRT_host.cpp:131-164).
+ * m: 16 floats, column-major 4x4 (LiteMath::float4x4 layout). */
+int hrt_add_instance(hrt_scene* scene, uint32_t geomId, const float m[16], uint32_t* instId);
+
+/* ISceneObject::UpdateInstance (core/CrossRT.h:130). */
+int hrt_update_instance(hrt_scene* scene, uint32_t instId, const float m[16]);
+
+/* ISceneObject::CommitScene (core/CrossRT.h:115; core/BVH2CommonRT_host.cpp:118-129):
+ * finishes instancing.  Queries are valid after it returns. */
+int hrt_commit_scene(hrt_scene* scene, int quality);
+
+/* ---------------------------------------------------------------- queries */
+
+/* Batched ISceneObject::RayQuery_NearestHit (core/CrossRT.h:143; reference
+ * traversal core/BVH2CommonRT.cpp:49-141,228-279).  Device arrays: rays has
+ * n records of 8 floats, hits has n records.  Asynchronous on `stream`. */
+int hrt_query_nearest(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits, void* stream);
+
+/* Batched ISceneObject::RayQuery_AnyHit (core/CrossRT.h:151).  The reference's
+ * BVH2CommonRT stubs it (core/BVH2CommonRT.cpp:281-292); the semantics follow its
+ * siblings (core/BVH2CommonRTStacklessLBVH.cpp:161-165,235-240): 1 if some
+ * triangle passes the ray-triangle test with tNear < t < tFar.  out: n bytes. */
+int hrt_query_any(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out, void* stream);
+
+/* Same as the two calls above with HOST arrays: the engine copies the rays to
+ * the device, traces and copies the results back before returning. */
+int hrt_query_nearest_host(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits);
+int hrt_query_any_host(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out);
+
+/* Traversal work of a batch, the quantity behind ISceneObject::GetStats
+ * (core/CrossRT.h:154, core/FactoryRT.cpp:82-101): counters[0] = node pairs
+ * fetched (HeavyRT counts 2 nodes, 64 bytes, per pair), counters[1] = triangle
+ * tests.  kind: 0 nearest, 1 any.  Device rays; synchronous. */
+int hrt_query_counters(hrt_scene* scene, int kind, const float* rays, uint64_t n, uint64_t counters[2], void* stream);
+
+/* ---------------------------------------------------------------- scene info */
+
+/* ISceneObject::GetGeomNum / GetInstNum / GetGeomBoxes (core/CrossRT.h:163-165). */
+int hrt_get_geom_num(const hrt_scene* scene, uint32_t* out);
+int hrt_get_inst_num(const hrt_scene* scene, uint32_t* out);
+/* boxes: 8 floats per geometry (boxMin float4, boxMax float4), host memory. */
+int hrt_get_geom_boxes(const hrt_scene* scene, float* boxes, uint32_t capacity);
+
+/* Per-geometry build information: out[0] triangles, out[1] leaves, out[2]
+ * internal node pairs, out[3] device bytes held; build_ms = GPU time of the
+ * LBVH build kernels. */
+int hrt_geom_info(const hrt_scene* scene, uint32_t geomId, uint64_t out[4], float* build_ms);
+
+/* Copies an intermediate or final array of a geometry's build to host memory,
+ * for parity checks against HeavyRT's builder.  capacityBytes = size of dst;
+ * *sizeBytes receives the bytes the array holds (dst may be NULL to query). */
+#define HRT_EXPORT_SCENE_BOX       0 /* 12 floats: bboxMin4, bboxMax4, zIndexScale4 (lbvh.cpp:41-51,228-263) */
+#define HRT_EXPORT_MORTON_SORTED   1 /* uint2[N] (code, triId) after the stable sort (lbvh.cpp:755)        */
+#define HRT_EXPORT_COMPRESSED      2 /* uint32[L] unique codes (lbvh.cpp:302-319)                          */
+#define HRT_EXPORT_RUN_STARTS      3 /* uint32[L] first sorted position of each code (lbvh.cpp:302-319)    */
+#define HRT_EXPORT_LR_NODES        4 /* BVHNode[2L-1] Karras + refit tree, LR format (lbvh.cpp:350-489)    */
+#define HRT_EXPORT_LR_COUNTS       5 /* uint32[2L-1] descendant node counts (lbvh.cpp:443-489)             */
+#define HRT_EXPORT_PRIM_INDICES    6 /* uint32[N] original triangle of each sorted position                */
+#define HRT_EXPORT_SORTED_INDICES  7 /* uint32[3N] index buffer in sorted order (BVH2CommonRT_host.cpp:45-64) */
+#define HRT_EXPORT_MORTON_UNSORTED 8 /* uint2[N] (code, triId) before the sort (lbvh.cpp:259-287)           */
+int hrt_geom_export(const hrt_scene* scene, uint32_t geomId, int what, void* dst, uint64_t capacityBytes,
+                    uint64_t* sizeBytes);
+
+/* Page-locked host memory for the host-pointer queries (copies from it run at
+ * full link speed).  No reference counterpart: the reference is host-only. */
+int hrt_host_alloc(uint64_t bytes, void** out);
+int hrt_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HRT_H */

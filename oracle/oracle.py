@@ -1,0 +1,201 @@
+"""Python access to the oracle (TEST INFRASTRUCTURE ONLY).
+
+Two checkers of HeavyRT's hot path live here:
+  * the C restatement oracle/hrt_oracle.c, built as oracle/_build/liboracle.so
+    (every machine);
+  * the reference's own CPU code compiled by oracle/Makefile.ref into
+    oracle/_ref/ (only where the reference sources are present).
+Only tests, the smoke check and the benchmark's CPU-baseline leg use this
+module; the engine never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+NODE_DTYPE = np.dtype([("boxMin", "<f4", (3,)), ("leftOffset", "<u4"), ("boxMax", "<f4", (3,)), ("escapeIndex", "<u4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("primId", "<u4"), ("instId", "<u4"), ("geomId", "<u4"), ("coords", "<f4", (4,))])
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        p = HERE / "_build" / "liboracle.so"
+        if not p.exists():
+            raise RuntimeError(f"oracle not built ({p} missing): run __graft_entry__.build()")
+        L = C.CDLL(str(p))
+        vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+        L.ora_build.restype = vp
+        L.ora_build.argtypes = [vp, u32, vp, u32]
+        L.ora_free.argtypes = [vp]
+        for f in ("ora_num_tris", "ora_num_leaves", "ora_num_nodes"):
+            getattr(L, f).restype = u32
+            getattr(L, f).argtypes = [vp]
+        L.ora_status.restype = i32
+        L.ora_status.argtypes = [vp]
+        L.ora_get_box.argtypes = [vp, vp]
+        L.ora_copy_u32.argtypes = [vp, i32, vp]
+        L.ora_trace.restype = i32
+        L.ora_trace.argtypes = [vp, vp, u64, i32, vp, vp, i32, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class OracleBVH:
+    """LBVH built by the C restatement: stage arrays + peach layout + traversal."""
+
+    def __init__(self, verts: np.ndarray, idx: np.ndarray):
+        self._v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 4)
+        self._i = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1)
+        self._h = C.c_void_p(lib().ora_build(_p(self._v), self._v.shape[0], _p(self._i), self._i.size))
+        self.n_tris = lib().ora_num_tris(self._h)
+        self.n_leaves = lib().ora_num_leaves(self._h)
+        self.n_nodes = lib().ora_num_nodes(self._h)
+        self.status = lib().ora_status(self._h)
+
+    def _u32(self, which: int, count: int) -> np.ndarray:
+        out = np.empty(count, dtype=np.uint32)
+        if count:
+            lib().ora_copy_u32(self._h, which, _p(out))
+        return out
+
+    def scene_box(self) -> np.ndarray:
+        out = np.empty(12, dtype=np.float32)
+        lib().ora_get_box(self._h, _p(out))
+        return out
+
+    def morton_unsorted(self):
+        return self._u32(0, 2 * self.n_tris).reshape(-1, 2)
+
+    def morton_sorted(self):
+        return self._u32(1, 2 * self.n_tris).reshape(-1, 2)
+
+    def compressed(self):
+        return self._u32(2, self.n_leaves)
+
+    def run_starts(self):
+        return self._u32(3, self.n_leaves)
+
+    def lr_nodes(self):
+        n = 2 * self.n_leaves - 1 if self.n_leaves else 0
+        return self._u32(4, 8 * n).view(NODE_DTYPE)
+
+    def lr_counts(self):
+        return self._u32(5, 2 * self.n_leaves - 1 if self.n_leaves else 0)
+
+    def prim_indices(self):
+        return self._u32(6, self.n_tris)
+
+    def peach_nodes(self):
+        return self._u32(7, 8 * self.n_nodes).view(NODE_DTYPE)
+
+    def sorted_indices(self):
+        return self._u32(8, 3 * self.n_tris)
+
+    def trace(self, rays: np.ndarray, any_hit: bool = False, threads: int = 0, counters: bool = False):
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = r.shape[0]
+        cnt = np.zeros(2, dtype=np.uint64)
+        if any_hit:
+            out = np.empty(n, dtype=np.uint8)
+            used = lib().ora_trace(self._h, _p(r), n, 1, None, _p(out), threads, _p(cnt) if counters else None)
+            res = out.astype(bool)
+        else:
+            out = np.empty(n, dtype=HIT_DTYPE)
+            used = lib().ora_trace(self._h, _p(r), n, 0, _p(out), None, threads, _p(cnt) if counters else None)
+            res = out
+        if counters:
+            return res, (int(cnt[0]), int(cnt[1])), used
+        return res
+
+    def close(self):
+        if self._h:
+            lib().ora_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- reference checker
+
+def reference_harness(fast: bool = False) -> Path | None:
+    p = HERE / "_ref" / ("ref_harness_fast" if fast else "ref_harness")
+    return p if p.exists() else None
+
+
+def _write_scene(path, verts, idx):
+    v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 4)
+    i = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1)
+    with open(path, "wb") as f:
+        f.write(b"HRTSCN01")
+        f.write(np.array([v.shape[0], i.size], dtype=np.uint64).tobytes())
+        f.write(v.tobytes())
+        f.write(i.tobytes())
+
+
+def _write_rays(path, rays):
+    r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    with open(path, "wb") as f:
+        f.write(b"HRTRAY01")
+        f.write(np.array([r.shape[0]], dtype=np.uint64).tobytes())
+        f.write(r.tobytes())
+
+
+def run_reference(verts, idx, rays=None, fast: bool = False, threads: int = 0) -> dict:
+    """Run the reference's own builder (and traversal, if rays are given).
+
+    Returns the stage arrays (scene box, codes, compressed codes, run starts, LR
+    tree, counts), the BVH2CommonRT arrays (peach nodes, prim indices, sorted
+    indices) and, with rays, the hits / any-hit flags and its counters."""
+    exe = reference_harness(fast)
+    if exe is None:
+        raise RuntimeError("reference checker not built (reference sources absent)")
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        sp = os.path.join(td, "scene.bin")
+        _write_scene(sp, verts, idx)
+        pre = os.path.join(td, "out")
+        r = subprocess.run([str(exe), "stages", sp, pre], capture_output=True, text=True, check=True)
+        out["stages_info"] = json.loads(r.stdout.strip().splitlines()[-1])
+        rd = lambda s, dt: np.fromfile(pre + s, dtype=dt)  # noqa: E731
+        out["scene_box"] = rd(".bbox", np.float32)
+        out["morton_unsorted"] = rd(".codes_unsorted", np.uint32).reshape(-1, 2)
+        out["morton_sorted"] = rd(".codes_sorted", np.uint32).reshape(-1, 2)
+        out["compressed"] = rd(".compressed", np.uint32)
+        out["run_starts"] = rd(".runstarts", np.uint32)
+        out["lr_nodes"] = rd(".lr_nodes", NODE_DTYPE)
+        out["lr_counts"] = rd(".lr_count", np.uint32)
+        out["leaf_indices"] = rd(".leaf_indices", np.uint32)
+        r = subprocess.run([str(exe), "build", sp, pre], capture_output=True, text=True, check=True)
+        out["build_info"] = json.loads(r.stdout.strip().splitlines()[-1])
+        out["peach_nodes"] = rd(".peach_nodes", NODE_DTYPE)
+        out["prim_indices"] = rd(".prim_indices", np.uint32)
+        out["sorted_indices"] = rd(".indices_sorted", np.uint32)
+        if rays is not None:
+            rp = os.path.join(td, "rays.bin")
+            _write_rays(rp, rays)
+            cmd = [str(exe), "trace", sp, pre, rp]
+            if fast and threads:
+                cmd.append(str(threads))
+            r = subprocess.run(cmd, capture_output=True, text=True, check=True)
+            out["trace_info"] = json.loads(r.stdout.strip().splitlines()[-1])
+            out["hits"] = rd(".hits", HIT_DTYPE)
+            out["any"] = rd(".any", np.uint8).astype(bool)
+    return out

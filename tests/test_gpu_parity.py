@@ -1,0 +1,242 @@
+"""GPU engine vs the oracle / golden vectors: every build stage and every
+query result bit-exact (integer and float), through the C ABI."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases
+
+pytestmark = pytest.mark.gpu
+
+MISS = 0xFFFFFFFF
+
+
+def _load(case):
+    return dict(np.load(GOLDEN / f"golden_{case}.npz"))
+
+
+def _scene(verts, idx, stride=16, instances=None):
+    from heavyrt_gb300 import SceneRT
+
+    s = SceneRT()
+    v = np.ascontiguousarray(verts, dtype=np.float32)
+    if stride != 16:
+        v3 = v.reshape(-1, 4)[:, :3]
+        pad = stride // 4 - 3
+        v = np.ascontiguousarray(np.concatenate([v3, np.full((v3.shape[0], pad), 7.0, np.float32)], axis=1)) if pad else \
+            np.ascontiguousarray(v3)
+    gid = s.AddGeom_Triangles3f(v, v.size * 4 // stride, idx, idx.size, vByteStride=stride)
+    if instances is None:
+        s.AddInstance(gid, np.eye(4, dtype=np.float32))
+    else:
+        for m in instances:
+            s.AddInstance(gid, m)
+    s.CommitScene()
+    return s, gid
+
+
+def _check_build(s, gid, want):
+    from heavyrt_gb300 import engine as E
+
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_SCENE_BOX).view(np.uint32), want["scene_box"].view(np.uint32))
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_MORTON_UNSORTED).reshape(-1, 2), want["morton_unsorted"])
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_MORTON_SORTED).reshape(-1, 2), want["morton_sorted"])
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_COMPRESSED), want["compressed"])
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_RUN_STARTS), want["run_starts"])
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_LR_NODES).view(np.uint32).reshape(-1),
+                                  np.asarray(want["lr_nodes"]).view(np.uint32).reshape(-1))
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_LR_COUNTS), want["lr_counts"])
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_PRIM_INDICES), want["prim_indices"])
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_SORTED_INDICES), want["sorted_indices"])
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_build_and_queries(native, case):
+    g = _load(case)
+    s, gid = _scene(g["verts"], g["idx"])
+    _check_build(s, gid, g)
+    hits = s.RayQuery_NearestHit(g["rays"])
+    np.testing.assert_array_equal(hits.view(np.uint32).reshape(-1, 8), g["hits"].reshape(-1, 8))
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(g["rays"]), g["any"])
+
+
+def _oracle_expect(verts, idx):
+    from oracle import oracle as orc
+
+    o = orc.OracleBVH(verts, idx)
+    return o, {"scene_box": o.scene_box(), "morton_unsorted": o.morton_unsorted(), "morton_sorted": o.morton_sorted(),
+               "compressed": o.compressed(), "run_starts": o.run_starts(), "lr_nodes": o.lr_nodes(),
+               "lr_counts": o.lr_counts(), "prim_indices": o.prim_indices(), "sorted_indices": o.sorted_indices()}
+
+
+SIZES = [1, 2, 3, 17, 255, 256, 257, 4095, 4096, 4097, 70001]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_soup_sizes_vs_oracle(native, n):
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(900 + n, n, off=0.05)
+    rays = np.concatenate([wl.rays_at_triangles(n, v, idx, 3000, jitter=0.03), wl.sphere_rays(n, 1000)])
+    o, want = _oracle_expect(v, idx)
+    s, gid = _scene(v, idx)
+    _check_build(s, gid, want)
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), o.trace(rays).view(np.uint32))
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True))
+
+
+@pytest.mark.parametrize("stride", [12, 16, 20, 32])
+def test_vertex_strides(native, stride):
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(40 + stride, 40, 30)
+    rays = wl.rays_at_triangles(stride, v, idx, 2000, jitter=0.02)
+    o, want = _oracle_expect(v, idx)
+    s, gid = _scene(v, idx, stride=stride)
+    _check_build(s, gid, want)
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), o.trace(rays).view(np.uint32))
+
+
+def test_heightfield_runs_and_tnear(native):
+    """Multi-triangle leaves (equal Morton codes), tNear > 0, short tFar."""
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(77, 200, 200)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 160, 90),
+                           wl.rays_at_triangles(1, v, idx, 5000, jitter=0.01)])
+    rays[::2, 3] = 2.0
+    rays[1::4, 7] = 2.7
+    o, want = _oracle_expect(v, idx)
+    assert o.n_leaves < o.n_tris  # runs of equal codes are present
+    s, gid = _scene(v, idx)
+    _check_build(s, gid, want)
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), o.trace(rays).view(np.uint32))
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True))
+
+
+def test_counters_match_oracle(native):
+    """Node-pair fetches and triangle tests per batch equal the oracle's: the
+    traversal visits exactly the reference's nodes in the reference's order."""
+    import torch
+
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(8, 128, 128)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 128, 72),
+                           wl.sphere_rays(3, 2000)])
+    o, _ = _oracle_expect(v, idx)
+    s, _ = _scene(v, idx)
+    dr = torch.from_numpy(rays).cuda()
+    for kind in (0, 1):
+        _, ocnt, _ = o.trace(rays, any_hit=bool(kind), counters=True)
+        gcnt = s.query_counters(kind, dr.data_ptr(), rays.shape[0])
+        assert gcnt == ocnt
+
+
+def test_device_queries_match_host_queries(native):
+    import torch
+
+    from heavyrt_gb300 import HIT_DTYPE
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(5, 20000)
+    rays = wl.rays_at_triangles(9, v, idx, 10000, jitter=0.02)
+    s, _ = _scene(v, idx)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((rays.shape[0], 8), dtype=torch.int32, device="cuda")
+    da = torch.empty(rays.shape[0], dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    s.query_device(0, dr.data_ptr(), rays.shape[0], dh.data_ptr(), stream)
+    s.query_device(1, dr.data_ptr(), rays.shape[0], da.data_ptr(), stream)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dh.cpu().numpy().view(np.uint32), s.RayQuery_NearestHit(rays).view(np.uint32).reshape(-1, 8))
+    np.testing.assert_array_equal(da.cpu().numpy().astype(bool), s.RayQuery_AnyHit(rays))
+    assert HIT_DTYPE.itemsize == 32
+
+
+def test_instances_exact_transforms(native):
+    """Several instances of one geometry; transforms exact in binary32 so the
+    expected result is computed by tracing the oracle with transformed rays."""
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(12, 3000, off=0.05)
+    mats = [np.eye(4, dtype=np.float32)]
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = [4.0, 0.0, 0.0]
+    mats.append(m)
+    m = np.diag([2.0, 2.0, 2.0, 1.0]).astype(np.float32)
+    m[:3, 3] = [0.0, -8.0, 0.5]
+    mats.append(m)
+    rays = np.concatenate([wl.sphere_rays(4, 4000, 12.0),
+                           wl.rays_at_triangles(5, v, idx, 2000, radius=6.0)])
+    s, gid = _scene(v, idx, instances=mats)
+    got = s.RayQuery_NearestHit(rays)
+    o, _ = _oracle_expect(v, idx)
+    best = np.empty(rays.shape[0], dtype=got.dtype)
+    best["t"] = rays[:, 7]
+    best["primId"] = best["instId"] = best["geomId"] = MISS
+    best["coords"] = 0
+    for k, mm in enumerate(mats):
+        inv = np.linalg.inv(mm.astype(np.float64)).astype(np.float32)
+        r = rays.copy()
+        o3 = rays[:, 0:3].astype(np.float32)
+        d3 = rays[:, 4:7].astype(np.float32)
+        for row in range(3):
+            a = inv[row]
+            r[:, row] = ((a[0] * o3[:, 0] + a[1] * o3[:, 1]) + a[2] * o3[:, 2]) + a[3] * np.float32(1.0)
+            r[:, 4 + row] = ((a[0] * d3[:, 0] + a[1] * d3[:, 1]) + a[2] * d3[:, 2]) + a[3] * np.float32(0.0)
+        if k == 0:
+            r = rays.copy()
+        r[:, 7] = best["t"]
+        h = o.trace(r)
+        better = (h["geomId"] != MISS) & (h["t"] < best["t"])
+        best[better] = h[better]
+        best["instId"][better] = k
+    found = best["geomId"] != MISS
+    np.testing.assert_array_equal(got["geomId"] != MISS, found)
+    np.testing.assert_array_equal(got["t"][found].view(np.uint32), best["t"][found].view(np.uint32))
+    np.testing.assert_array_equal(got["instId"][found], best["instId"][found])
+    np.testing.assert_array_equal(got["primId"][found], best["primId"][found])
+
+
+def test_empty_geometry_and_errors(native):
+    from heavyrt_gb300 import HrtError, SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    s = SceneRT()
+    v = np.zeros((3, 4), np.float32)
+    gid = s.AddGeom_Triangles3f(v, 3, np.zeros(0, np.uint32), 0, vByteStride=16)
+    s.AddInstance(gid)
+    with pytest.raises(HrtError) as e:
+        s.RayQuery_NearestHit(wl.sphere_rays(1, 4))
+    assert e.value.status == E.HRT_ERR_STATE  # query before commit
+    s.CommitScene()
+    h = s.RayQuery_NearestHit(wl.sphere_rays(1, 64))
+    assert np.all(h["geomId"] == MISS) and np.all(h["t"] == np.float32(1e9))
+    # index out of range
+    with pytest.raises(HrtError) as e:
+        s.AddGeom_Triangles3f(np.zeros((3, 4), np.float32), 3, np.array([0, 1, 5], np.uint32), 3, vByteStride=16)
+    assert e.value.status == E.HRT_ERR_INVALID_ARGUMENT
+    # more than 127 triangles with one Morton code: the reference's leaf count overflows
+    tri = np.array([[0, 0, 0, 1], [1, 0, 0, 1], [0, 1, 0, 1]], dtype=np.float32)
+    vv = np.concatenate([tri] * 300 + [tri + np.array([5, 5, 5, 0], np.float32)])
+    with pytest.raises(HrtError) as e:
+        s.AddGeom_Triangles3f(vv, vv.shape[0], np.arange(vv.shape[0], dtype=np.uint32), vv.shape[0], vByteStride=16)
+    assert e.value.status == E.HRT_ERR_CAPACITY
+    # a failed add leaves the scene usable
+    assert s.GetGeomNum() == 1
+    with pytest.raises(HrtError):
+        SceneRT(build_name="cbvh_embree2")
+
+
+def test_geom_boxes_and_info(native):
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(3, 1000)
+    s, gid = _scene(v, idx)
+    box = s.GetGeomBoxes()[gid]
+    np.testing.assert_array_equal(box[:3], v[:, :3].min(axis=0))
+    np.testing.assert_array_equal(box[4:7], v[:, :3].max(axis=0))
+    info = s.geom_info(gid)
+    assert info["tris"] == 1000 and info["leaves"] <= 1000 and info["build_ms"] > 0
+    assert s.GetInstNum() == 1 and s.Name() == "GB300_LBVH"
