@@ -42,14 +42,16 @@ RAY_BYTES = 32         # {posAndNear, dirAndFar}
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
-    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
     p.add_argument("--nx", type=int, default=1024, help="heightfield quads per side")
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--ncu", action="store_true",
+                   help="profiling run: setup, warm-up and timed steps only (no extra builds, counters, e2e, CPU)")
     return p.parse_args()
 
 
@@ -171,18 +173,20 @@ def cpu_trace_rate(o, eye, ao, seconds: float, threads: int = 0):
     o.trace(a_s, any_hit=True, threads=threads)
     dt = time.perf_counter() - t0
     rate = (e_s.shape[0] + a_s.shape[0]) / dt
-    # sample size for the target duration
+    # sample size for the target duration: part of the frame, or whole frames repeated
     frac = min(1.0, seconds * rate / (n_eye + n_ao))
+    reps = max(1, int(seconds * rate / (n_eye + n_ao))) if frac >= 1.0 else 1
     e_s = eye[: max(1, int(n_eye * frac))]
     step = max(1, int(round(1 / frac))) if frac < 1.0 else 1
     a_s = ao[::step]
     t0 = time.perf_counter()
-    _, _, used = o.trace(e_s, threads=threads, counters=True)
-    o.trace(a_s, any_hit=True, threads=threads)
+    for _ in range(reps):
+        _, _, used = o.trace(e_s, threads=threads, counters=True)
+        o.trace(a_s, any_hit=True, threads=threads)
     dt = time.perf_counter() - t0
-    n = e_s.shape[0] + a_s.shape[0]
-    return n / dt / 1e6, used, f"{e_s.shape[0]} eye rays (first rows) + {a_s.shape[0]} AO rays (every {step}th) " \
-                               f"of the frame, {dt:.1f} s"
+    n = (e_s.shape[0] + a_s.shape[0]) * reps
+    return n / dt / 1e6, used, f"{reps} x ({e_s.shape[0]} eye rays (first rows) + {a_s.shape[0]} AO rays " \
+                               f"(every {step}th)) of the frame, {dt:.1f} s"
 
 
 def run_reference(args):
@@ -251,7 +255,7 @@ def run_engine(args):
     info = scene.geom_info(gid)
     # build time: a few more builds of the same geometry
     build_ms = [info["build_ms"]]
-    for _ in range(3):
+    for _ in range(0 if args.ncu else 3):
         s2 = SceneRT(ctx)
         g2 = s2.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
         build_ms.append(s2.geom_info(g2)["build_ms"])
@@ -269,8 +273,11 @@ def run_engine(args):
     d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
 
     # algorithmic bytes per launch from the counting traversal (same decisions)
-    eye_pairs, eye_tris = scene.query_counters(0, d_eye.data_ptr(), n_eye, sh)
-    ao_pairs, ao_tris = scene.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+    if args.ncu:
+        eye_pairs = eye_tris = ao_pairs = ao_tris = 0
+    else:
+        eye_pairs, eye_tris = scene.query_counters(0, d_eye.data_ptr(), n_eye, sh)
+        ao_pairs, ao_tris = scene.query_counters(1, d_ao.data_ptr(), n_ao, sh)
     eye_bytes = NODE_PAIR_BYTES * eye_pairs + TRI_BYTES * eye_tris + RAY_BYTES * n_eye + 32 * n_eye
     ao_bytes = NODE_PAIR_BYTES * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
 
@@ -284,7 +291,7 @@ def run_engine(args):
         if ev:
             ev[2].record(stream)
 
-    for _ in range(max(3, args.warmup)):
+    for _ in range(args.warmup if args.ncu else max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
@@ -314,6 +321,9 @@ def run_engine(args):
     ms_per_step = total_ms / args.steps
     rays_per_step = n_eye + n_ao
     value = world * rays_per_step / (ms_per_step * 1e-3) / 1e6
+    if args.ncu:
+        print(json.dumps({"ncu_run": True, "ms_per_step": ms_per_step, "value": value}), flush=True)
+        return 0
 
     # e2e: host pinned rays in, results out, through the host-pointer C-ABI calls
     pin_eye = PinnedBuffer(w.eye_rays.nbytes)

@@ -126,10 +126,15 @@ def test_counters_match_oracle(native):
     o, _ = _oracle_expect(v, idx)
     s, _ = _scene(v, idx)
     dr = torch.from_numpy(rays).cuda()
-    for kind in (0, 1):
-        _, ocnt, _ = o.trace(rays, any_hit=bool(kind), counters=True)
-        gcnt = s.query_counters(kind, dr.data_ptr(), rays.shape[0])
-        assert gcnt == ocnt
+    _, ocnt, _ = o.trace(rays, counters=True)
+    assert s.query_counters(0, dr.data_ptr(), rays.shape[0]) == ocnt
+    # any-hit: the reference finishes the leaf before leaving the loop
+    # (core/BVH2CommonRTStacklessLBVH.cpp:65); the engine returns at the first
+    # accepted triangle, so it visits the same node pairs and tests at most as
+    # many triangles.
+    _, ocnt, _ = o.trace(rays, any_hit=True, counters=True)
+    gpairs, gtris = s.query_counters(1, dr.data_ptr(), rays.shape[0])
+    assert gpairs == ocnt[0] and gtris <= ocnt[1]
 
 
 def test_device_queries_match_host_queries(native):
