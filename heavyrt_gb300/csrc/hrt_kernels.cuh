@@ -14,6 +14,7 @@ namespace hrt
 // 8-bit digit passes.  keys/vals hold the input and receive the output;
 // keysAlt/valsAlt are ping-pong buffers of n entries.  scratch must hold
 // radix_sort_scratch_bytes(n) bytes; it is cleared by the call.
+constexpr uint32_t kTileSize = 4096;  // pairs per onesweep tile
 size_t radix_sort_scratch_bytes(uint32_t n);
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, uint32_t* valsAlt, uint32_t n,
                              void* scratch, uint32_t* errorWord, int numSMs, cudaStream_t stream);

@@ -23,7 +23,8 @@ namespace
 constexpr int      kThreads    = 256;
 constexpr int      kWarps      = kThreads / 32;
 constexpr int      kItems      = 16;
-constexpr uint32_t kTile       = kThreads * kItems;  // 4096 pairs
+constexpr uint32_t kTile       = kTileSize;  // 4096 pairs
+static_assert(kTile == kThreads * kItems, "tile = threads x items");
 constexpr int      kRadix      = 256;
 constexpr int      kPasses     = 4;
 constexpr uint32_t kFlagAgg    = 1u << 30;
@@ -261,3 +262,81 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, 
 }
 
 }  // namespace hrt
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the pair sort (hrt_sort_morton_pairs_noalloc).
+//
+// Some callers cannot call cudaMalloc: code that records work inside a CUDA
+// stream capture (allocation calls are not allowed while a capture is active),
+// host applications whose device memory is owned by another allocator that
+// reserves it up front, and latency-bound paths that cannot afford the
+// implicit synchronisation of an allocation.  For them this entry point takes
+// its scratch (ping-pong arrays, digit histograms, look-back tile status and
+// an error word) from one file-scope device array of fixed size, so it calls
+// no allocator at all.  The array is part of the library image: every GPU that
+// loads the library holds kNoAllocScratchBytes of it until the process exits.
+#include <mutex>
+
+#include "../../include/hrt.h"
+
+namespace
+{
+
+constexpr uint32_t kNoAllocMaxPairs  = HRT_NOALLOC_MAX_PAIRS;
+constexpr uint32_t kNoAllocTiles     = (kNoAllocMaxPairs + hrt::kTileSize - 1) / hrt::kTileSize;
+constexpr size_t   kNoAllocSortBytes = sizeof(uint32_t) * (4 * 256 + 4 + 4 + (size_t)4 * kNoAllocTiles * 256);
+constexpr size_t   kNoAllocPingPong  = sizeof(uint32_t) * (size_t)kNoAllocMaxPairs;  // one array
+constexpr size_t   kNoAllocScratchBytes = 2 * kNoAllocPingPong + kNoAllocSortBytes + 256;
+constexpr int      kNoAllocMaxDevices = 64;
+
+// Scratch shared by every call on a device; in host code this name is only a
+// stand-in, the device address comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+std::mutex g_noallocMu;
+void*      g_noallocPtr[kNoAllocMaxDevices] = {};
+int        g_noallocSMs[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int hrt_sort_morton_pairs_noalloc(uint32_t* keys, uint32_t* vals, uint64_t n, void* stream)
+{
+  if (n > kNoAllocMaxPairs) return HRT_ERR_CAPACITY;
+  if (n > 0 && (!keys || !vals)) return HRT_ERR_INVALID_ARGUMENT;
+  if (n <= 1) return HRT_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return HRT_ERR_CUDA;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return HRT_ERR_UNSUPPORTED;
+  void* base = nullptr;
+  int numSMs = 0;
+  {
+    // One-time set-up per device, with that device current: resolve the
+    // device address of the scratch array.
+    std::lock_guard<std::mutex> lk(g_noallocMu);
+    if (!g_noallocPtr[dev])
+    {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noallocScratch) != cudaSuccess || !p) return HRT_ERR_CUDA;
+      int sms = 0;
+      if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return HRT_ERR_CUDA;
+      g_noallocSMs[dev] = sms;
+      g_noallocPtr[dev] = p;
+    }
+    base = g_noallocPtr[dev];
+    numSMs = g_noallocSMs[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char* b = (unsigned char*)base;
+  uint32_t* keysAlt = (uint32_t*)b;
+  uint32_t* valsAlt = (uint32_t*)(b + kNoAllocPingPong);
+  void* sortScratch = b + 2 * kNoAllocPingPong;
+  uint32_t* errorWord = (uint32_t*)(b + 2 * kNoAllocPingPong + kNoAllocSortBytes);
+  // The array keeps the previous call's contents: clear what must start at zero.
+  if (cudaMemsetAsync(errorWord, 0, sizeof(uint32_t), s) != cudaSuccess) return HRT_ERR_CUDA;
+  if (hrt::radix_sort_pairs(keys, vals, keysAlt, valsAlt, (uint32_t)n, sortScratch, errorWord, numSMs, s) != cudaSuccess)
+    return HRT_ERR_CUDA;
+  uint32_t err = 0;
+  if (cudaMemcpyAsync(&err, errorWord, sizeof(err), cudaMemcpyDeviceToHost, s) != cudaSuccess) return HRT_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return HRT_ERR_CUDA;
+  return (err & hrt::kErrWaitTimeout) ? HRT_ERR_TIMEOUT : HRT_OK;
+}

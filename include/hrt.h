@@ -183,6 +183,27 @@ int hrt_geom_export(const hrt_scene* scene, uint32_t geomId, int what, void* dst
 int hrt_host_alloc(uint64_t bytes, void** out);
 int hrt_host_free(void* p);
 
+/* Stable sort of (Morton code, triangle id) pairs by code -- the LBVH build's
+ * radix sort -- that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: work recorded inside a CUDA stream
+ * capture, host applications whose device memory is owned by another
+ * allocator, and latency-bound paths that cannot take an allocation's implicit
+ * synchronisation.  keys and vals are device arrays of n entries (input and
+ * output, sorted in place); all scratch comes from one fixed device array that
+ * the library holds on every GPU that loads it (about 2.4 MB) until the process
+ * exits.  n above HRT_NOALLOC_MAX_PAIRS is rejected with HRT_ERR_CAPACITY.
+ *
+ * Runs on the calling thread's current device and on `stream`, and returns
+ * after the stream has finished the sort (HRT_ERR_TIMEOUT if a device wait gave
+ * up).  The first call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture
+ * begins.  Every call shares the one array, so calls whose work overlaps on
+ * the GPU race with each other: serialise them (one stream, or wait between
+ * calls). */
+#define HRT_NOALLOC_MAX_PAIRS (1u << 18)
+int hrt_sort_morton_pairs_noalloc(uint32_t* keys, uint32_t* vals, uint64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
