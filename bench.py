@@ -34,7 +34,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mrays/s nearest/any-hit on 1 GB300, served+batched vs plain; p99 latency"
 UNIT = "Mrays/s"
 FALLBACK_HBM_GBS = 6800.0
-NODE_PAIR_BYTES = 64   # one pair record: two child boxes + refs
+LAYOUT_NODE_BYTES = {"bvh2": 64, "bvh4": 128, "bvh4_f16": 64, "bvh4_q8": 64}  # bytes per node fetch
+LAYOUT_DESC = {"bvh2": "BVH2 pair records (64 B) + sorted triangle records",
+               "bvh4": "BVH4 FP32 nodes (128 B) + sorted triangle records",
+               "bvh4_f16": "BVH4 FP16 nodes rounded outward (64 B) + sorted triangle records",
+               "bvh4_q8": "BVH4 8-bit nodes in per-node frames (64 B) + sorted triangle records"}
 TRI_BYTES = 36         # three float3 (vertex A and two edges)
 RAY_BYTES = 32         # {posAndNear, dirAndFar}
 
@@ -50,6 +54,8 @@ def parse():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--layout", default="bvh2", choices=["bvh2", "bvh4", "bvh4_f16", "bvh4_q8"],
+                   help="node layout of the scene (binary FP32, 4-wide FP32/FP16/8-bit)")
     p.add_argument("--ncu", action="store_true",
                    help="profiling run: setup, warm-up and timed steps only (no extra builds, counters, e2e, CPU)")
     return p.parse_args()
@@ -248,7 +254,7 @@ def run_engine(args):
 
     w = make_frame(args)
     ctx = Context(local)
-    scene = SceneRT(ctx)
+    scene = SceneRT(ctx, layout=args.layout)
     gid = scene.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
     scene.AddInstance(gid)
     scene.CommitScene()
@@ -256,7 +262,7 @@ def run_engine(args):
     # build time: a few more builds of the same geometry
     build_ms = [info["build_ms"]]
     for _ in range(0 if args.ncu else 3):
-        s2 = SceneRT(ctx)
+        s2 = SceneRT(ctx, layout=args.layout)
         g2 = s2.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
         build_ms.append(s2.geom_info(g2)["build_ms"])
         s2.close()
@@ -278,8 +284,9 @@ def run_engine(args):
     else:
         eye_pairs, eye_tris = scene.query_counters(0, d_eye.data_ptr(), n_eye, sh)
         ao_pairs, ao_tris = scene.query_counters(1, d_ao.data_ptr(), n_ao, sh)
-    eye_bytes = NODE_PAIR_BYTES * eye_pairs + TRI_BYTES * eye_tris + RAY_BYTES * n_eye + 32 * n_eye
-    ao_bytes = NODE_PAIR_BYTES * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
+    node_bytes = LAYOUT_NODE_BYTES[args.layout]
+    eye_bytes = node_bytes * eye_pairs + TRI_BYTES * eye_tris + RAY_BYTES * n_eye + 32 * n_eye
+    ao_bytes = node_bytes * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
 
     def step(ev=None):
         if ev:
@@ -361,14 +368,15 @@ def run_engine(args):
         dom, dom_ms, dom_bytes, dom_name = "nearest", eye_avg, eye_bytes, "k_trace<nearest>"
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = profile_traffic(f"trace_{dom}_heightfield2M.txt")
+    lay = "" if args.layout == "bvh2" else f"_{args.layout}"
+    traffic = profile_traffic(f"trace_{dom}{lay}_heightfield2M.txt")
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w.name, "tris": int(w.idx.size // 3), "eye_rays": int(n_eye), "ao_rays": int(n_ao),
-                   "layout": "BVH2 pair records (64 B) + sorted triangle records", "parallelism": f"replicas{world}",
+                   "layout": LAYOUT_DESC[args.layout], "parallelism": f"replicas{world}",
                    "l2": f"inputs larger than L2: rays {(d_eye.nbytes + d_ao.nbytes) / 1e6:.0f} MB, "
                          f"BVH+triangles {info['bytes'] / 1e6:.0f} MB",
                    "build_ms_median": round(statistics.median(build_ms), 3),
@@ -382,7 +390,7 @@ def run_engine(args):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "algorithmic_bytes_per_launch": int(dom_bytes),
-                     "note": "algorithmic bytes = 64 B per node pair + 36 B per triangle test + ray in/out; "
+                     "note": f"algorithmic bytes = {node_bytes} B per node fetch + 36 B per triangle test + ray in/out; "
                              "node fetches mostly hit L1/L2, so frac can exceed 1 (see traffic)"},
         "clocks": clk,
     }

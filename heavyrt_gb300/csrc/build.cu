@@ -288,7 +288,9 @@ __global__ void __launch_bounds__(kThreads) k_leaves(const float4* __restrict__ 
       mx[1] = lm_max(mx[1], lm_max(a.y, lm_max(b.y, c.y)));
       mx[2] = lm_max(mx[2], lm_max(a.z, lm_max(b.z, c.z)));
       TriRec r;
-      r.a = make_float4(a.x, a.y, a.z, __uint_as_float(j + 1 == end ? 1u : 0u));
+      // flags: bit 0 ends a binary leaf, bit 1 a 4-wide leaf (cleared later
+      // where the collapse merges two leaves)
+      r.a = make_float4(a.x, a.y, a.z, __uint_as_float(j + 1 == end ? 3u : 0u));
       r.e1 = make_float4(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z), __uint_as_float(tri));
       r.e2 = make_float4(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z), 0.0f);
       tris[j] = r;

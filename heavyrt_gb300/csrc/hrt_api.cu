@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -13,6 +14,8 @@
 #include "../../include/hrt.h"
 
 using namespace hrt;
+
+static constexpr uint32_t kCounterSlots = 256;
 
 struct hrt_context
 {
@@ -45,6 +48,8 @@ struct Geom
   float        buildMs = 0.0f;
   uint64_t     bytes = 0;
   float        box[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  void*        nodes4 = nullptr;  // 4-wide nodes of the scene's layout
+  uint32_t     nNodes4 = 0;
 };
 
 struct Instance
@@ -63,10 +68,16 @@ struct hrt_scene
   std::vector<Geom>     geoms;
   std::vector<Instance> insts;
   bool                  committed = false;
+  int                   layout = HRT_LAYOUT_BVH2;
   InstanceDesc*         dInst = nullptr;
   uint32_t              nInstDev = 0;
   uint32_t*             dError = nullptr;
   unsigned long long*   dCounters = nullptr;
+  // work counters of the persistent traversal pool: one slot per launch, taken
+  // round-robin, so up to kCounterSlots queries on one scene may be in flight
+  unsigned int*         dRayCounters = nullptr;
+  std::atomic<uint32_t> counterSlot{0};
+  TraceConfig           cfg[2];  // [0] nearest, [1] any
   // staging for the host-pointer queries
   void*                 stageRays = nullptr;
   void*                 stageOut = nullptr;
@@ -103,7 +114,7 @@ int cuda_fail(hrt_context* ctx, cudaError_t e, const char* what)
 void free_geom(Geom& g)
 {
   void* ptrs[] = {g.verts, g.keys, g.vals, g.keysUnsorted, g.compressed, g.runStarts, g.lr,
-                  g.lrCount, g.recs, g.tris, g.sortedIdx, g.params};
+                  g.lrCount, g.recs, g.tris, g.sortedIdx, g.params, g.nodes4};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   g = Geom();
@@ -175,7 +186,7 @@ bool is_identity(const float* m)
 }
 
 int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
-                   uint64_t stride)
+                   uint64_t stride, int layout)
 {
   hrt_context* ctx = s->ctx;
   cudaStream_t st = ctx->stream;
@@ -262,8 +273,33 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   HRT_CUDA(ctx, cudaEventCreate(&e1));
   HRT_CUDA(ctx, cudaEventRecord(e0, st));
   cudaError_t be = build_lbvh(b, ctx->numSMs, st);
-  HRT_CUDA(ctx, cudaEventRecord(e1, st));
   if (be != cudaSuccess) return cuda_fail(ctx, be, "build_lbvh");
+  if (layout != HRT_LAYOUT_BVH2)
+  {
+    // collapse into 4-wide nodes: plan (count), allocate, emit
+    void* scratch4 = nullptr;
+    uint32_t count4 = 0;
+    HRT_CUDA(ctx, cudaMallocAsync(&scratch4, bvh4_scratch_bytes(N), st));
+    Bvh4Buffers b4;
+    b4.nTris = N;
+    b4.params = g.params;
+    b4.lr = g.lr;
+    b4.runStarts = g.runStarts;
+    b4.parent = parent;
+    b4.tris = g.tris;
+    b4.scratch = scratch4;
+    b4.hostNodeCount = &count4;
+    HRT_CUDA(ctx, bvh4_plan(b4, ctx->numSMs, st));
+    HRT_CUDA(ctx, cudaStreamSynchronize(st));
+    if (count4 == 0) count4 = 1;  // a single leaf still gets a root node
+    const size_t nodeBytes = (layout == HRT_LAYOUT_BVH4_F32) ? sizeof(Node4F32) : sizeof(Node4F16);
+    HRT_CUDA(ctx, cudaMalloc(&g.nodes4, nodeBytes * count4));
+    g.bytes += nodeBytes * count4;
+    g.nNodes4 = count4;
+    HRT_CUDA(ctx, bvh4_emit(b4, layout - 1, g.nodes4, count4, ctx->numSMs, st));
+    HRT_CUDA(ctx, cudaFreeAsync(scratch4, st));
+  }
+  HRT_CUDA(ctx, cudaEventRecord(e1, st));
   HRT_CUDA(ctx, cudaMemcpyAsync(&g.host, g.params, sizeof(BuildParams), cudaMemcpyDeviceToHost, st));
   HRT_CUDA(ctx, cudaFreeAsync(dIdx, st));
   HRT_CUDA(ctx, cudaFreeAsync(keysAlt, st));
@@ -286,7 +322,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   if (err & kErrLeafCount)
     return fail(ctx, HRT_ERR_CAPACITY, "more than 127 triangles share one Morton code (leaf count field overflows)");
   if (err & kErrWaitTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "device look-back wait timed out during the build");
-  if (err & kErrLayout) return fail(ctx, HRT_ERR_DEVICE_CHECK, "refit did not reach the root exactly twice");
+  if (err & kErrLayout) return fail(ctx, HRT_ERR_DEVICE_CHECK, "inconsistent tree or node encoding");
   if (g.nLeaves == 0 || g.nLeaves > N) return fail(ctx, HRT_ERR_DEVICE_CHECK, "leaf count out of range");
   return HRT_OK;
 }
@@ -324,7 +360,8 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
   a.hits = out;
   a.counters = s->dCounters;
   a.errorWord = s->dError;
-  cudaError_t e = trace(a, kind, counting, s->ctx->numSMs, st);
+  a.rayCounter = s->dRayCounters + (s->counterSlot.fetch_add(1) % kCounterSlots);
+  cudaError_t e = trace(a, kind, counting, s->layout, s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
 }
@@ -396,10 +433,12 @@ int hrt_scene_create(hrt_context* ctx, const char* buildName, hrt_scene** out)
   s->ctx = ctx;
   if (cudaMalloc((void**)&s->dError, sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc((void**)&s->dCounters, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc((void**)&s->dRayCounters, kCounterSlots * sizeof(unsigned int)) != cudaSuccess ||
       cudaMemset(s->dError, 0, sizeof(uint32_t)) != cudaSuccess)
   {
     if (s->dError) cudaFree(s->dError);
     if (s->dCounters) cudaFree(s->dCounters);
+    if (s->dRayCounters) cudaFree(s->dRayCounters);
     delete s;
     return fail(ctx, HRT_ERR_OUT_OF_MEMORY, "scene allocation");
   }
@@ -427,6 +466,7 @@ int hrt_scene_destroy(hrt_scene* s)
   if (s->dInst) cudaFree(s->dInst);
   if (s->dError) cudaFree(s->dError);
   if (s->dCounters) cudaFree(s->dCounters);
+  if (s->dRayCounters) cudaFree(s->dRayCounters);
   if (s->stageRays) cudaFree(s->stageRays);
   if (s->stageOut) cudaFree(s->stageOut);
   delete s;
@@ -448,7 +488,7 @@ int hrt_add_geom_triangles3f(hrt_scene* s, const float* vpos, uint64_t nVert, co
   std::lock_guard<std::mutex> lk(s->mu);
   cudaSetDevice(ctx->device);
   Geom g;
-  const int st = build_geometry(s, g, vpos, nVert, idx, nIdx, vByteStride);
+  const int st = build_geometry(s, g, vpos, nVert, idx, nIdx, vByteStride, s->layout);
   if (st != HRT_OK)
   {
     cudaStreamSynchronize(ctx->stream);
@@ -529,6 +569,7 @@ int hrt_commit_scene(hrt_scene* s, int quality)
     const Instance& in = s->insts[i];
     const Geom& gm = s->geoms[in.geomId];
     d[i].recs = gm.recs;
+    d[i].nodes4 = gm.nodes4;
     d[i].tris = gm.tris;
     d[i].geomId = in.geomId;
     d[i].instId = (uint32_t)i;
@@ -638,7 +679,7 @@ int hrt_geom_info(const hrt_scene* s, uint32_t geomId, uint64_t out[4], float* b
   const Geom& g = s->geoms[geomId];
   out[0] = g.nTris;
   out[1] = g.nLeaves;
-  out[2] = g.nLeaves > 1 ? g.nLeaves - 1 : (g.nTris ? 1 : 0);
+  out[2] = (s->layout == HRT_LAYOUT_BVH2) ? (g.nLeaves > 1 ? g.nLeaves - 1 : (g.nTris ? 1 : 0)) : g.nNodes4;
   out[3] = g.bytes;
   if (build_ms) *build_ms = g.buildMs;
   return HRT_OK;
@@ -662,6 +703,9 @@ int hrt_geom_export(const hrt_scene* s, uint32_t geomId, int what, void* dst, ui
     case HRT_EXPORT_LR_COUNTS: size = 4 * nLR; break;
     case HRT_EXPORT_PRIM_INDICES: size = 4 * N; break;
     case HRT_EXPORT_SORTED_INDICES: size = 12 * N; break;
+    case HRT_EXPORT_NODES4:
+      size = (uint64_t)g.nNodes4 * (s->layout == HRT_LAYOUT_BVH4_F32 ? sizeof(Node4F32) : sizeof(Node4F16));
+      break;
     default: return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "unknown export id");
   }
   if (sizeBytes) *sizeBytes = size;
@@ -697,9 +741,52 @@ int hrt_geom_export(const hrt_scene* s, uint32_t geomId, int what, void* dst, ui
     case HRT_EXPORT_LR_COUNTS: HRT_CUDA(ctx, cudaMemcpy(dst, g.lrCount, size, cudaMemcpyDeviceToHost)); return HRT_OK;
     case HRT_EXPORT_PRIM_INDICES: HRT_CUDA(ctx, cudaMemcpy(dst, g.vals, size, cudaMemcpyDeviceToHost)); return HRT_OK;
     case HRT_EXPORT_SORTED_INDICES: HRT_CUDA(ctx, cudaMemcpy(dst, g.sortedIdx, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_NODES4: HRT_CUDA(ctx, cudaMemcpy(dst, g.nodes4, size, cudaMemcpyDeviceToHost)); return HRT_OK;
     default: break;
   }
   return HRT_ERR_INVALID_ARGUMENT;
+}
+
+int hrt_scene_set_layout(hrt_scene* s, int layout)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  if (layout < HRT_LAYOUT_BVH2 || layout > HRT_LAYOUT_BVH4_Q8) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown layout");
+  std::lock_guard<std::mutex> g(s->mu);
+  if (!s->geoms.empty()) return fail(s->ctx, HRT_ERR_STATE, "the layout is chosen before the first geometry is added");
+  s->layout = layout;
+  return HRT_OK;
+}
+
+int hrt_scene_get_layout(const hrt_scene* s, int* layout)
+{
+  if (!s || !layout) return HRT_ERR_INVALID_ARGUMENT;
+  *layout = s->layout;
+  return HRT_OK;
+}
+
+int hrt_scene_set_trace_config(hrt_scene* s, int kind, const hrt_trace_config* c)
+{
+  if (!s || !c || (kind != 0 && kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
+  if ((c->threadsPerBlock != 64 && c->threadsPerBlock != 128 && c->threadsPerBlock != 256) ||
+      (c->persistent != 0 && c->persistent != 1) || c->stepsPerRefill < 1 || c->stepsPerRefill > 1024 ||
+      c->refillLanes < 1 || c->refillLanes > 32)
+    return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "trace config out of range");
+  std::lock_guard<std::mutex> g(s->mu);
+  s->cfg[kind].threadsPerBlock = c->threadsPerBlock;
+  s->cfg[kind].persistent = c->persistent;
+  s->cfg[kind].stepsPerRefill = c->stepsPerRefill;
+  s->cfg[kind].refillLanes = c->refillLanes;
+  return HRT_OK;
+}
+
+int hrt_scene_get_trace_config(const hrt_scene* s, int kind, hrt_trace_config* c)
+{
+  if (!s || !c || (kind != 0 && kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
+  c->threadsPerBlock = s->cfg[kind].threadsPerBlock;
+  c->persistent = s->cfg[kind].persistent;
+  c->stepsPerRefill = s->cfg[kind].stepsPerRefill;
+  c->refillLanes = s->cfg[kind].refillLanes;
+  return HRT_OK;
 }
 
 int hrt_host_alloc(uint64_t bytes, void** out)

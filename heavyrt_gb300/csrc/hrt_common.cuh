@@ -57,6 +57,36 @@ struct __align__(16) TriRec
 };
 static_assert(sizeof(TriRec) == 48, "TriRec must be 48 bytes");
 
+// 4-wide nodes (children in slots 0..3; ref as in PairRec, kEmptyRef = unused
+// slot).  A leaf slot's triangles end at the record whose flags have bit 1 set.
+// FP32 boxes, 128 bytes: component vectors over the four slots.
+struct __align__(16) Node4F32
+{
+  float4 lox, loy, loz, hix, hiy, hiz;
+  uint4  ref;
+  uint4  pad;
+};
+static_assert(sizeof(Node4F32) == 128, "Node4F32 must be 128 bytes");
+
+// FP16 boxes rounded outward, 64 bytes: a[k] = half2(lo.x, lo.y), b[k] =
+// half2(lo.z, hi.x), c[k] = half2(hi.y, hi.z) for slot k.
+struct __align__(16) Node4F16
+{
+  uint4 a, b, c, ref;
+};
+static_assert(sizeof(Node4F16) == 64, "Node4F16 must be 64 bytes");
+
+// 8-bit boxes against a per-node frame, 64 bytes: frame.xyz = origin, frame.w
+// = three biased exponents (e + 128, one byte per axis); bound = origin +
+// q * 2^e.  q0 = bytes (lo.x, lo.y, lo.z, hi.x) per slot (slot k in byte k),
+// q1.x/q1.y = (hi.y, hi.z).
+struct __align__(16) Node4Q8
+{
+  float4 frame;
+  uint4  q0, q1, ref;
+};
+static_assert(sizeof(Node4Q8) == 64, "Node4Q8 must be 64 bytes");
+
 // Scene box, Morton scale and leaf count of one geometry, written on the device.
 struct BuildParams
 {

@@ -50,11 +50,34 @@ size_t build_scratch_bytes(uint32_t nTris);
 // device are ORed into params->error.
 cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t stream);
 
+// ---------------------------------------------------------------- bvh4.cu
+// Collapse of a finished LBVH (LR tree, parents, run starts) into 4-wide nodes.
+struct Bvh4Buffers
+{
+  uint32_t         nTris;
+  BuildParams*     params;          // device; nLeaves and the error word
+  const BVHNode32* lr;              // 2L-1
+  const uint32_t*  runStarts;       // L
+  const uint32_t*  parent;          // 2L-1
+  TriRec*          tris;            // N; bit 1 of a.w marks 4-wide leaf ends
+  void*            scratch;         // bvh4_scratch_bytes(nTris)
+  uint32_t*        hostNodeCount;   // host word receiving the node count (0 when L == 1)
+};
+size_t bvh4_scratch_bytes(uint32_t nTris);
+// Roles, depths and node numbering; copies the node count to *hostNodeCount
+// (asynchronously: synchronise before reading it).
+cudaError_t bvh4_plan(const Bvh4Buffers& b, int numSMs, cudaStream_t stream);
+// Writes the nodes in `format` (0 FP32, 1 FP16, 2 8-bit) to `nodes`, which
+// holds maxNodes nodes (the planned count).
+cudaError_t bvh4_emit(const Bvh4Buffers& b, int format, void* nodes, uint32_t maxNodes, int numSMs,
+                      cudaStream_t stream);
+
 // ---------------------------------------------------------------- trace.cu
 // One instance of a geometry as the traversal sees it.
 struct InstanceDesc
 {
-  const PairRec* recs;
+  const PairRec* recs;      // binary records (layout 0)
+  const void*    nodes4;    // 4-wide nodes (layouts 1-3)
   const TriRec*  tris;
   uint32_t       geomId;
   uint32_t       instId;
@@ -65,15 +88,29 @@ struct InstanceDesc
 
 struct TraceArgs
 {
-  const float4*       rays;       // 2 float4 per ray
+  const float4*       rays;        // 2 float4 per ray
   uint64_t            n;
-  const InstanceDesc* inst;       // device array
+  const InstanceDesc* inst;        // device array
   uint32_t            nInst;
-  void*               hits;       // hrt_hit[n] (nearest) or uint8_t[n] (any)
-  unsigned long long* counters;   // optional [2]: node pairs, triangle tests
-  uint32_t*           errorWord;  // device
+  void*               hits;        // hrt_hit[n] (nearest) or uint8_t[n] (any)
+  unsigned long long* counters;    // optional [2]: node pairs, triangle tests
+  uint32_t*           errorWord;   // device
+  unsigned int*       rayCounter;  // device, work counter of the persistent pool
 };
-// kind 0: nearest, 1: any.  counting = 1 also accumulates counters.
-cudaError_t trace(const TraceArgs& a, int kind, int counting, int numSMs, cudaStream_t stream);
+
+// Launch shape of the traversal (tuned per workload).
+struct TraceConfig
+{
+  int threadsPerBlock = 128;  // 64, 128 or 256
+  int persistent = 1;         // 1: persistent warp pool with lane refill; 0: one thread per ray
+  int stepsPerRefill = 16;    // traversal steps between refill checks
+  int refillLanes = 24;       // a warp refills when at least this many lanes are idle
+};
+
+// kind 0: nearest, 1: any.  counting = 1 also accumulates counters (node
+// fetches, triangle tests).  layout: 0 binary pair records, 1 4-wide FP32,
+// 2 4-wide FP16, 3 4-wide 8-bit.
+cudaError_t trace(const TraceArgs& a, int kind, int counting, int layout, const TraceConfig& c, int numSMs,
+                  cudaStream_t stream);
 
 }  // namespace hrt

@@ -1,0 +1,550 @@
+// Nearest-hit / any-hit traversal of the LBVH.
+//
+// Each ray makes the decisions of HeavyRT's BVH2TraverseC32
+// (core/BVH2CommonRT.cpp:49-141) on the same binary tree: load the two
+// children of the current node, slab-test both (core/raytrace_common.h:67-80),
+// descend into the nearer hit child (child 0 on equal entry distance), push
+// the other, pop when neither is hit.  The leaf test is the reference's
+// Moller-Trumbore with 1e-6 barycentric slack (core/BVH2CommonRT.cpp:9-47),
+// written with explicit round-to-nearest intrinsics in the reference's
+// evaluation order, so t/u/v match the CPU reference bit for bit.
+//
+// Slab distances only feed comparisons (hit tests, near-first choice, pruning
+// against the current t), so the slab test takes min/max with the hardware
+// fminf/fmaxf instead of the reference's std::min/std::max selects: the two
+// differ only in the sign of a zero result (and for NaN, which finite rays
+// never produce because SafeInverse keeps |1/d| <= 1e36), and +0 == -0 in
+// every comparison, so every decision is unchanged.
+//
+// Scheduling: a persistent warp pool.  Each warp keeps one ray per lane; when
+// enough lanes have finished, the warp refills them from a global ray counter
+// with one atomic per warp (ballot + popc ranking), so lanes do not idle while
+// the warp's longest ray finishes.  A ray's own visit order does not depend on
+// the schedule.  A one-thread-per-ray grid is kept as a configuration.
+//
+// Memory: a child pair is one 64-byte record (four 128-bit read-only loads), a
+// triangle one 48-byte record (three); the short stack lives in shared memory,
+// interleaved by thread so a warp's pushes and pops hit 32 different banks.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "hrt_kernels.cuh"
+#include "../../include/hrt.h"
+
+namespace hrt
+{
+namespace
+{
+
+// Stack bounds: the binary tree of distinct 30-bit codes is at most 30 levels
+// deep (each level lengthens the common prefix), one push per level; the
+// 4-wide tree halves the levels and pushes at most 3 per level.
+constexpr int      kStack2 = 32;
+constexpr int      kStack4 = 48;
+constexpr uint32_t kNoRay = 0xFFFFFFFFu;
+
+template <int LAYOUT> struct StackDepth
+{
+  static constexpr int value = LAYOUT == 0 ? kStack2 : kStack4;
+};
+
+struct Ray
+{
+  float ox, oy, oz, tNear;
+  float dx, dy, dz;
+  float ix, iy, iz;
+};
+
+// SafeInverse, core/raytrace_common.h:57-65.
+__device__ __forceinline__ float safe_inv(float d)
+{
+  const float ooeps = 1.0e-36f;
+  return __fdiv_rn(1.0f, fabsf(d) > ooeps ? d : copysignf(ooeps, d));
+}
+
+// RayBoxIntersection2, core/raytrace_common.h:67-80 (differences, products and
+// evaluation order of the reference; min/max as explained above).
+__device__ __forceinline__ void slab(const Ray& r, float bx0, float by0, float bz0, float bx1, float by1, float bz1,
+                                     float& tn, float& tf)
+{
+  const float lo = __fmul_rn(r.ix, __fsub_rn(bx0, r.ox));
+  const float hi = __fmul_rn(r.ix, __fsub_rn(bx1, r.ox));
+  const float lo1 = __fmul_rn(r.iy, __fsub_rn(by0, r.oy));
+  const float hi1 = __fmul_rn(r.iy, __fsub_rn(by1, r.oy));
+  const float lo2 = __fmul_rn(r.iz, __fsub_rn(bz0, r.oz));
+  const float hi2 = __fmul_rn(r.iz, __fsub_rn(bz1, r.oz));
+  tn = fmaxf(fmaxf(fminf(lo, hi), fminf(lo1, hi1)), fminf(lo2, hi2));
+  tf = fminf(fminf(fmaxf(lo, hi), fmaxf(lo1, hi1)), fmaxf(lo2, hi2));
+}
+
+struct Hit
+{
+  float    t, u, v;
+  uint32_t prim, inst, geom;
+};
+
+// matmul4x3 / matmul3x3 (core/raytrace_common.h:82-90) with the column sum
+// order ((m0*x + m1*y) + m2*z) + m3*w.
+__device__ __forceinline__ float row_dot(const float* m, float x, float y, float z, float w)
+{
+  return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], x), __fmul_rn(m[1], y)), __fmul_rn(m[2], z)), __fmul_rn(m[3], w));
+}
+
+__device__ __forceinline__ void make_ray(const InstanceDesc& d, const float4& po, const float4& di, Ray& r)
+{
+  r.tNear = po.w;
+  if (d.identity)
+  {
+    r.ox = po.x; r.oy = po.y; r.oz = po.z;
+    r.dx = di.x; r.dy = di.y; r.dz = di.z;
+  }
+  else
+  {
+    r.ox = row_dot(d.inv + 0, po.x, po.y, po.z, 1.0f);
+    r.oy = row_dot(d.inv + 4, po.x, po.y, po.z, 1.0f);
+    r.oz = row_dot(d.inv + 8, po.x, po.y, po.z, 1.0f);
+    r.dx = row_dot(d.inv + 0, di.x, di.y, di.z, 0.0f);
+    r.dy = row_dot(d.inv + 4, di.x, di.y, di.z, 0.0f);
+    r.dz = row_dot(d.inv + 8, di.x, di.y, di.z, 0.0f);
+  }
+  r.ix = safe_inv(r.dx);
+  r.iy = safe_inv(r.dy);
+  r.iz = safe_inv(r.dz);
+}
+
+// Moller-Trumbore leaf test over the leaf starting at sorted triangle j
+// (IntersectAllPrimitivesInLeaf, core/BVH2CommonRT.cpp:9-47); the leaf ends at
+// the record whose flags have ENDBIT set (1: binary leaf, 2: 4-wide leaf).
+// Returns true when ANY and a triangle was accepted.
+template <bool ANY, bool COUNT, uint32_t ENDBIT = 1u>
+__device__ __forceinline__ bool leaf_test(const TriRec* __restrict__ tris, uint32_t j, const Ray& r, Hit& h,
+                                          uint32_t instId, uint32_t geomId, uint64_t& nTris)
+{
+  while (true)
+  {
+    const float4* q = reinterpret_cast<const float4*>(tris + j);
+    const float4 A = __ldg(q + 0);
+    const float4 e1 = __ldg(q + 1);
+    const float4 e2 = __ldg(q + 2);
+    if (COUNT) nTris++;
+    // pvec = cross(dir, e2), tvec = pos - A, qvec = cross(tvec, e1)
+    const float px = __fsub_rn(__fmul_rn(r.dy, e2.z), __fmul_rn(r.dz, e2.y));
+    const float py = __fsub_rn(__fmul_rn(r.dz, e2.x), __fmul_rn(r.dx, e2.z));
+    const float pz = __fsub_rn(__fmul_rn(r.dx, e2.y), __fmul_rn(r.dy, e2.x));
+    const float tx = __fsub_rn(r.ox, A.x);
+    const float ty = __fsub_rn(r.oy, A.y);
+    const float tz = __fsub_rn(r.oz, A.z);
+    const float qx = __fsub_rn(__fmul_rn(ty, e1.z), __fmul_rn(tz, e1.y));
+    const float qy = __fsub_rn(__fmul_rn(tz, e1.x), __fmul_rn(tx, e1.z));
+    const float qz = __fsub_rn(__fmul_rn(tx, e1.y), __fmul_rn(ty, e1.x));
+    const float det = __fadd_rn(__fadd_rn(__fmul_rn(e1.x, px), __fmul_rn(e1.y, py)), __fmul_rn(e1.z, pz));
+    const float invDet = __fdiv_rn(1.0f, det);
+    const float v = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(tx, px), __fmul_rn(ty, py)), __fmul_rn(tz, pz)), invDet);
+    const float u = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(qx, r.dx), __fmul_rn(qy, r.dy)), __fmul_rn(qz, r.dz)), invDet);
+    const float t = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(e2.x, qx), __fmul_rn(e2.y, qy)), __fmul_rn(e2.z, qz)), invDet);
+    // 1.0f + 1e-6f rounds to 1 + 2^-20 in binary32
+    if (v >= -1e-6f && u >= -1e-6f && __fadd_rn(u, v) <= 0x1.00001p+0f && t > r.tNear && t < h.t)
+    {
+      h.t = t;
+      h.u = u;
+      h.v = v;
+      h.prim = j;
+      h.inst = instId;
+      h.geom = geomId;
+      if (ANY) return true;
+    }
+    if (__float_as_uint(A.w) & ENDBIT) return false;  // last triangle of the leaf
+    j++;
+  }
+}
+
+// ---------------------------------------------------------------- 4-wide nodes
+// Decoded child boxes of one 4-wide node.
+struct Boxes4
+{
+  float lo[3][4], hi[3][4];
+  uint4 ref;
+};
+
+__device__ __forceinline__ void load_node4(const Node4F32* __restrict__ n, Boxes4& B)
+{
+  const float4* p = reinterpret_cast<const float4*>(n);
+  const float4 lx = __ldg(p + 0), ly = __ldg(p + 1), lz = __ldg(p + 2);
+  const float4 hx = __ldg(p + 3), hy = __ldg(p + 4), hz = __ldg(p + 5);
+  B.ref = __ldg(reinterpret_cast<const uint4*>(p + 6));
+  B.lo[0][0] = lx.x; B.lo[0][1] = lx.y; B.lo[0][2] = lx.z; B.lo[0][3] = lx.w;
+  B.lo[1][0] = ly.x; B.lo[1][1] = ly.y; B.lo[1][2] = ly.z; B.lo[1][3] = ly.w;
+  B.lo[2][0] = lz.x; B.lo[2][1] = lz.y; B.lo[2][2] = lz.z; B.lo[2][3] = lz.w;
+  B.hi[0][0] = hx.x; B.hi[0][1] = hx.y; B.hi[0][2] = hx.z; B.hi[0][3] = hx.w;
+  B.hi[1][0] = hy.x; B.hi[1][1] = hy.y; B.hi[1][2] = hy.z; B.hi[1][3] = hy.w;
+  B.hi[2][0] = hz.x; B.hi[2][1] = hz.y; B.hi[2][2] = hz.z; B.hi[2][3] = hz.w;
+}
+
+__device__ __forceinline__ float2 h2f(uint32_t w) { return __half22float2(*reinterpret_cast<const __half2*>(&w)); }
+
+__device__ __forceinline__ void load_node4(const Node4F16* __restrict__ n, Boxes4& B)
+{
+  const uint4* p = reinterpret_cast<const uint4*>(n);
+  const uint4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2);
+  B.ref = __ldg(p + 3);
+  const uint32_t aw[4] = {a.x, a.y, a.z, a.w}, bw[4] = {b.x, b.y, b.z, b.w}, cw[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+  {
+    const float2 xy = h2f(aw[k]), zx = h2f(bw[k]), yz = h2f(cw[k]);
+    B.lo[0][k] = xy.x; B.lo[1][k] = xy.y; B.lo[2][k] = zx.x;
+    B.hi[0][k] = zx.y; B.hi[1][k] = yz.x; B.hi[2][k] = yz.y;
+  }
+}
+
+__device__ __forceinline__ void load_node4(const Node4Q8* __restrict__ n, Boxes4& B)
+{
+  const uint4* p = reinterpret_cast<const uint4*>(n);
+  const float4 f = __ldg(reinterpret_cast<const float4*>(p));
+  const uint4 q0 = __ldg(p + 1), q1 = __ldg(p + 2);
+  B.ref = __ldg(p + 3);
+  const uint32_t e = __float_as_uint(f.w);
+  const float org[3] = {f.x, f.y, f.z};
+  const float sc[3] = {__int_as_float((int)(((e & 0xFFu) - 128u + 127u) << 23)),
+                       __int_as_float((int)((((e >> 8) & 0xFFu) - 128u + 127u) << 23)),
+                       __int_as_float((int)((((e >> 16) & 0xFFu) - 128u + 127u) << 23))};
+  const uint32_t w[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+    {
+      // origin + q * 2^e: the product is exact, so one fused add rounds like the encoder's add
+      B.lo[c][k] = fmaf((float)((w[c] >> (8 * k)) & 0xFFu), sc[c], org[c]);
+      B.hi[c][k] = fmaf((float)((w[3 + c] >> (8 * k)) & 0xFFu), sc[c], org[c]);
+    }
+}
+
+template <int LAYOUT> struct Node4Type;
+template <> struct Node4Type<1> { using type = Node4F32; };
+template <> struct Node4Type<2> { using type = Node4F16; };
+template <> struct Node4Type<3> { using type = Node4Q8; };
+
+__device__ __forceinline__ void cswap(float& ka, uint32_t& va, float& kb, uint32_t& vb)
+{
+  const bool s = kb < ka;
+  const float tk = s ? kb : ka;
+  const uint32_t tv = s ? vb : va;
+  kb = s ? ka : kb;
+  vb = s ? va : vb;
+  ka = tk;
+  va = tv;
+}
+
+// Per-lane traversal state.
+struct Lane
+{
+  Ray      r;
+  Hit      h;
+  float4   po, di;    // the ray as given (world space)
+  uint32_t ray;       // ray index or kNoRay
+  uint32_t inst;      // current instance
+  uint32_t cur;       // current record / leaf reference
+  int      top;       // stack depth
+};
+
+// Advances the lane's instance cursor to the next instance with triangles,
+// starting at `from`; prepares the ray for it.  Returns false when none is left.
+__device__ __forceinline__ bool begin_instance(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t nInst,
+                                               uint32_t from)
+{
+  for (uint32_t k = from; k < nInst; k++)
+    if (inst[k].valid)
+    {
+      L.inst = k;
+      make_ray(inst[k], L.po, L.di, L.r);
+      L.cur = 0;  // record 0 = the root's two children
+      L.top = 0;
+      return true;
+    }
+  return false;
+}
+
+// One traversal step (an internal node, or a leaf followed by a pop).
+// Returns true when the lane's ray is finished.
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t nInst,
+                                     uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
+                                     uint32_t* errorWord)
+{
+  const InstanceDesc& d = inst[L.inst];
+  bool pop = false;
+  if constexpr (LAYOUT != 0)
+  {
+    // 4-wide node: test the four slots, continue with the nearest hit child,
+    // push the other hit children farthest first (HeavyRT's BVH4 order,
+    // core/BVH4CommonRT.cpp:49-246).
+    if ((L.cur & kLeafBit) == 0u)
+    {
+      using N = typename Node4Type<LAYOUT>::type;
+      Boxes4 B;
+      load_node4(reinterpret_cast<const N*>(d.nodes4) + L.cur, B);
+      if (COUNT) nPairs++;
+      float key[4];
+      uint32_t ref[4] = {B.ref.x, B.ref.y, B.ref.z, B.ref.w};
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+      {
+        float tn, tf;
+        slab(L.r, B.lo[0][k], B.lo[1][k], B.lo[2][k], B.hi[0][k], B.hi[1][k], B.hi[2][k], tn, tf);
+        const bool hit = ref[k] != kEmptyRef && tn <= tf && tf >= L.r.tNear && tn <= L.h.t;
+        key[k] = hit ? tn : INFINITY;
+        ref[k] = hit ? ref[k] : kEmptyRef;
+      }
+      cswap(key[0], ref[0], key[1], ref[1]);
+      cswap(key[2], ref[2], key[3], ref[3]);
+      cswap(key[0], ref[0], key[2], ref[2]);
+      cswap(key[1], ref[1], key[3], ref[3]);
+      cswap(key[1], ref[1], key[2], ref[2]);
+      int f = 0;
+      while (f < 4 && ref[f] == kEmptyRef) f++;
+      if (f == 4)
+        pop = true;
+      else
+      {
+        L.cur = ref[f];
+#pragma unroll
+        for (int k = 3; k >= 1; k--)
+          if (k > f && ref[k] != kEmptyRef)
+          {
+            if (L.top >= kStack4)
+            {
+              atomicOr(errorWord, kErrStack);
+              return true;
+            }
+            stack[L.top * THREADS] = ref[k];
+            L.top++;
+          }
+      }
+    }
+    else
+    {
+      if (L.cur != kEmptyRef &&
+          leaf_test<ANY, COUNT, 2u>(d.tris, L.cur & ~kLeafBit, L.r, L.h, d.instId, d.geomId, nTris))
+        return true;  // any-hit found
+      pop = true;
+    }
+  }
+  else if ((L.cur & kLeafBit) == 0u)
+  {
+    const float4* p = reinterpret_cast<const float4*>(d.recs + L.cur);
+    const float4 a = __ldg(p + 0);
+    const float4 b = __ldg(p + 1);
+    const float4 c = __ldg(p + 2);
+    const uint4 e = __ldg(reinterpret_cast<const uint4*>(p + 3));
+    if (COUNT) nPairs++;
+    float t0n, t0f, t1n, t1f;
+    slab(L.r, a.x, a.y, a.z, a.w, b.x, b.y, t0n, t0f);
+    slab(L.r, b.z, b.w, c.x, c.y, c.z, c.w, t1n, t1f);
+    const bool h0 = (t0n <= t0f) && (t0f >= L.r.tNear) && (t0n <= L.h.t);
+    const bool h1 = (t1n <= t1f) && (t1f >= L.r.tNear) && (t1n <= L.h.t);
+    pop = !h0 && !h1;
+    L.cur = h0 ? e.x : e.y;
+    if (h0 && h1)
+    {
+      const bool first0 = (t0n <= t1n);
+      L.cur = first0 ? e.x : e.y;
+      if (L.top >= kStack2)
+      {
+        atomicOr(errorWord, kErrStack);
+        return true;
+      }
+      stack[L.top * THREADS] = first0 ? e.y : e.x;
+      L.top++;
+    }
+  }
+  else
+  {
+    if (L.cur != kEmptyRef && leaf_test<ANY, COUNT>(d.tris, L.cur & ~kLeafBit, L.r, L.h, d.instId, d.geomId, nTris))
+      return true;  // any-hit found
+    pop = true;
+  }
+  if (pop)
+  {
+    L.top--;
+    if (L.top < 0) return !begin_instance(L, inst, nInst, L.inst + 1);
+    L.cur = stack[L.top * THREADS];
+  }
+  return false;
+}
+
+template <bool ANY>
+__device__ __forceinline__ void write_result(const Lane& L, void* out)
+{
+  if (ANY)
+    reinterpret_cast<uint8_t*>(out)[L.ray] = (L.h.geom != 0xFFFFFFFFu) ? 1 : 0;
+  else
+  {
+    float4* o = reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray);
+    o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(L.h.inst), __uint_as_float(L.h.geom));
+    o[1] = make_float4(L.h.u, L.h.v, 0.0f, 0.0f);
+  }
+}
+
+__device__ __forceinline__ void start_ray(Lane& L, uint32_t i, const float4* __restrict__ rays)
+{
+  L.ray = i;
+  L.po = __ldg(rays + 2 * (size_t)i + 0);
+  L.di = __ldg(rays + 2 * (size_t)i + 1);
+  L.h.t = L.di.w;
+  L.h.u = L.h.v = 0.0f;
+  L.h.prim = L.h.inst = L.h.geom = 0xFFFFFFFFu;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void flush_counters(uint64_t nPairs, uint64_t nTris, unsigned long long* counters)
+{
+  if (!COUNT) return;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    nPairs += __shfl_down_sync(0xFFFFFFFFu, nPairs, o);
+    nTris += __shfl_down_sync(0xFFFFFFFFu, nTris, o);
+  }
+  if ((threadIdx.x & 31) == 0)
+  {
+    atomicAdd(&counters[0], (unsigned long long)nPairs);
+    atomicAdd(&counters[1], (unsigned long long)nTris);
+  }
+}
+
+// Persistent warp pool.  Lanes run `steps` traversal steps between refills; a
+// warp refills when at least `refill` lanes are idle (or all are).
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict__ rays, uint32_t n,
+                                                        const InstanceDesc* __restrict__ inst, uint32_t nInst, void* out,
+                                                        unsigned long long* counters, uint32_t* errorWord,
+                                                        unsigned int* rayCounter, int steps, int refill)
+{
+  __shared__ uint32_t s_stack[StackDepth<LAYOUT>::value * THREADS];
+  uint32_t* stack = s_stack + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t ltMask = (1u << lane) - 1u;
+  uint64_t nPairs = 0, nTris = 0;
+  Lane L;
+  L.ray = kNoRay;
+  bool exhausted = false;
+  while (true)
+  {
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, L.ray == kNoRay);
+    if (exhausted && idle == 0xFFFFFFFFu) break;
+    if (!exhausted && (__popc(idle) >= refill || idle == 0xFFFFFFFFu))
+    {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(rayCounter, (unsigned int)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+      if (L.ray == kNoRay)
+      {
+        const uint32_t i = base + __popc(idle & ltMask);
+        if (i < n)
+        {
+          start_ray(L, i, rays);
+          if (!begin_instance(L, inst, nInst, 0))
+          {
+            write_result<ANY>(L, out);
+            L.ray = kNoRay;
+          }
+        }
+      }
+    }
+    if (L.ray != kNoRay)
+    {
+      for (int s = 0; s < steps; s++)
+      {
+        if (step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord))
+        {
+          write_result<ANY>(L, out);
+          L.ray = kNoRay;
+          break;
+        }
+      }
+    }
+  }
+  flush_counters<COUNT>(nPairs, nTris, counters);
+}
+
+// One thread per ray.
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict__ rays, uint32_t n,
+                                                        const InstanceDesc* __restrict__ inst, uint32_t nInst, void* out,
+                                                        unsigned long long* counters, uint32_t* errorWord)
+{
+  __shared__ uint32_t s_stack[StackDepth<LAYOUT>::value * THREADS];
+  uint32_t* stack = s_stack + threadIdx.x;
+  uint64_t nPairs = 0, nTris = 0;
+  const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
+  if (i < n)
+  {
+    Lane L;
+    start_ray(L, i, rays);
+    if (begin_instance(L, inst, nInst, 0))
+      while (!step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord)) {}
+    write_result<ANY>(L, out);
+  }
+  flush_counters<COUNT>(nPairs, nTris, counters);
+}
+
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  const uint32_t n = (uint32_t)a.n;
+  if (c.persistent && !COUNT)
+  {
+    int perSM = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_pool<LAYOUT, ANY, COUNT, THREADS>,
+                                                                  THREADS, 0);
+    if (e != cudaSuccess) return e;
+    if (perSM < 1) perSM = 1;
+    uint64_t blocks = (uint64_t)numSMs * perSM;
+    const uint64_t need = ((uint64_t)n + THREADS - 1) / THREADS;
+    if (blocks > need) blocks = need;
+    e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    k_trace_pool<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(
+        a.rays, n, a.inst, a.nInst, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes);
+  }
+  else
+  {
+    const uint64_t blocks = ((uint64_t)n + THREADS - 1) / THREADS;
+    k_trace_grid<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(a.rays, n, a.inst, a.nInst, a.hits,
+                                                                                 a.counters, a.errorWord);
+  }
+  return cudaGetLastError();
+}
+
+// Counting runs use the one-thread-per-ray grid at 128 threads: the counts do
+// not depend on the schedule.
+template <int LAYOUT>
+cudaError_t trace_layout(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  if (counting)
+    return kind == 0 ? launch<LAYOUT, false, true, 128>(a, c, numSMs, s) : launch<LAYOUT, true, true, 128>(a, c, numSMs, s);
+  switch (c.threadsPerBlock)
+  {
+    case 64:
+      return kind == 0 ? launch<LAYOUT, false, false, 64>(a, c, numSMs, s) : launch<LAYOUT, true, false, 64>(a, c, numSMs, s);
+    case 256:
+      return kind == 0 ? launch<LAYOUT, false, false, 256>(a, c, numSMs, s)
+                       : launch<LAYOUT, true, false, 256>(a, c, numSMs, s);
+    default:
+      return kind == 0 ? launch<LAYOUT, false, false, 128>(a, c, numSMs, s)
+                       : launch<LAYOUT, true, false, 128>(a, c, numSMs, s);
+  }
+}
+
+}  // namespace
+
+// Per-layout entry points, one translation unit each (trace_l*.cu).
+cudaError_t trace_l0(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+cudaError_t trace_l1(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+cudaError_t trace_l2(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+cudaError_t trace_l3(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+
+}  // namespace hrt

@@ -40,6 +40,12 @@ EXPORT_LR_COUNTS = 5
 EXPORT_PRIM_INDICES = 6
 EXPORT_SORTED_INDICES = 7
 EXPORT_MORTON_UNSORTED = 8
+EXPORT_NODES4 = 9
+
+# node layouts (include/hrt.h); names accepted as CreateSceneRT's a_layoutName
+LAYOUT_BVH2, LAYOUT_BVH4_F32, LAYOUT_BVH4_F16, LAYOUT_BVH4_Q8 = 0, 1, 2, 3
+LAYOUT_NAMES = {"": LAYOUT_BVH2, "bvh2": LAYOUT_BVH2, "bvh4": LAYOUT_BVH4_F32, "bvh4_f32": LAYOUT_BVH4_F32,
+                "bvh4_f16": LAYOUT_BVH4_F16, "bvh4_half": LAYOUT_BVH4_F16, "bvh4_q8": LAYOUT_BVH4_Q8}
 
 # CRT_Hit, core/CrossRT.h:20-27
 HIT_DTYPE = np.dtype([("t", "<f4"), ("primId", "<u4"), ("instId", "<u4"), ("geomId", "<u4"), ("coords", "<f4", (4,))])
@@ -56,7 +62,18 @@ _EXPORT_DTYPES = {
     EXPORT_LR_COUNTS: np.uint32,
     EXPORT_PRIM_INDICES: np.uint32,
     EXPORT_SORTED_INDICES: np.uint32,
+    EXPORT_NODES4: np.uint32,
 }
+
+
+class TraceConfig(C.Structure):
+    """hrt_trace_config (include/hrt.h): launch shape of the traversal kernel."""
+
+    _fields_ = [("threadsPerBlock", C.c_int), ("persistent", C.c_int), ("stepsPerRefill", C.c_int),
+                ("refillLanes", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class HrtError(RuntimeError):
@@ -109,6 +126,10 @@ def lib() -> C.CDLL:
         "hrt_geom_export": (i32, [vp, u32, i32, vp, u64, C.POINTER(u64)]),
         "hrt_host_alloc": (i32, [u64, C.POINTER(vp)]),
         "hrt_host_free": (i32, [vp]),
+        "hrt_scene_set_layout": (i32, [vp, i32]),
+        "hrt_scene_get_layout": (i32, [vp, C.POINTER(i32)]),
+        "hrt_scene_set_trace_config": (i32, [vp, i32, C.POINTER(TraceConfig)]),
+        "hrt_scene_get_trace_config": (i32, [vp, i32, C.POINTER(TraceConfig)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -179,12 +200,24 @@ def _as_rays(posAndNear, dirAndFar=None) -> np.ndarray:
 class SceneRT:
     """GPU LBVH scene behind HeavyRT's ISceneObject interface (core/CrossRT.h:64-193)."""
 
-    def __init__(self, ctx: Context | None = None, build_name: str = "cbvh_lbvh"):
+    def __init__(self, ctx: Context | None = None, build_name: str = "cbvh_lbvh", layout=LAYOUT_BVH2):
         self.ctx = ctx or default_context()
         self._h = C.c_void_p()
         self.ctx.check(lib().hrt_scene_create(self.ctx.handle, build_name.encode() if build_name else None,
                                               C.byref(self._h)), "hrt_scene_create")
         self._build_name = build_name
+        if isinstance(layout, str):
+            if layout.lower() not in LAYOUT_NAMES:
+                raise HrtError(HRT_ERR_UNSUPPORTED, f"layout '{layout}' is not provided by this engine")
+            layout = LAYOUT_NAMES[layout.lower()]
+        if layout != LAYOUT_BVH2:
+            self.ctx.check(lib().hrt_scene_set_layout(self._h, int(layout)), "set_layout")
+
+    @property
+    def layout(self) -> int:
+        v = C.c_int()
+        self.ctx.check(lib().hrt_scene_get_layout(self._h, C.byref(v)), "get_layout")
+        return v.value
 
     # ---- ISceneObject ---------------------------------------------------
     def Name(self) -> str:  # ISceneObject::Name, core/CrossRT.h:72
@@ -277,6 +310,15 @@ class SceneRT:
                        "query_counters")
         return int(c[0]), int(c[1])
 
+    def set_trace_config(self, kind: int, threadsPerBlock=128, persistent=1, stepsPerRefill=16, refillLanes=24):
+        c = TraceConfig(threadsPerBlock, persistent, stepsPerRefill, refillLanes)
+        self.ctx.check(lib().hrt_scene_set_trace_config(self._h, kind, C.byref(c)), "set_trace_config")
+
+    def trace_config(self, kind: int) -> dict:
+        c = TraceConfig()
+        self.ctx.check(lib().hrt_scene_get_trace_config(self._h, kind, C.byref(c)), "trace_config")
+        return c.as_dict()
+
     def geom_info(self, geom_id: int = 0) -> dict:
         out = (C.c_uint64 * 4)()
         ms = C.c_float()
@@ -308,7 +350,7 @@ def CreateSceneRT(a_implName: str = "GB300_LBVH", a_buildName: str = "cbvh_lbvh"
     """Factory mirroring CreateSceneRT (core/FactoryRT.cpp:29-78, core/CrossRT.h:195)."""
     if a_implName not in ("GB300_LBVH", "BVH2Common"):
         raise HrtError(HRT_ERR_UNSUPPORTED, f"implementation '{a_implName}' is not provided by this engine")
-    return SceneRT(build_name=a_buildName)
+    return SceneRT(build_name=a_buildName, layout=a_layoutName or "")
 
 
 def DeleteSceneRT(scene: SceneRT):  # core/CrossRT.h:196

@@ -95,6 +95,24 @@ int hrt_scene_create(hrt_context* ctx, const char* buildName, hrt_scene** out);
 /* Replaces DeleteSceneRT (core/CrossRT.h:196). */
 int hrt_scene_destroy(hrt_scene* scene);
 
+/* Node layout of a scene's acceleration structures, HeavyRT's a_layoutName
+ * argument of CreateSceneRT (core/CrossRT.h:195).  Chosen before the first
+ * geometry is added (HRT_ERR_STATE afterwards).
+ *   BVH2      binary LBVH, 64-byte child-pair records (default; the
+ *             reference's BVH2CommonRT decisions, bit-exact)
+ *   BVH4_F32  4-wide collapse (core/builders/cbvh.cpp:226-311), FP32 boxes, 128 B nodes
+ *   BVH4_F16  4-wide, FP16 boxes rounded outward, 64 B nodes
+ *   BVH4_Q8   4-wide, 8-bit offsets against a per-node FP32 frame with
+ *             power-of-two scales, rounded outward, 64 B nodes
+ * Quantised boxes contain their FP32 boxes, so they can only add node visits;
+ * the triangle test is the same in every layout. */
+#define HRT_LAYOUT_BVH2     0
+#define HRT_LAYOUT_BVH4_F32 1
+#define HRT_LAYOUT_BVH4_F16 2
+#define HRT_LAYOUT_BVH4_Q8  3
+int hrt_scene_set_layout(hrt_scene* scene, int layout);
+int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
+
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */
 int hrt_clear_geom(hrt_scene* scene);
 
@@ -144,6 +162,20 @@ int hrt_query_any(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out,
 int hrt_query_nearest_host(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits);
 int hrt_query_any_host(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out);
 
+/* Launch shape of the traversal kernel, per query kind (0 nearest, 1 any);
+ * results never depend on it.  No reference counterpart (the reference runs
+ * one ray per virtual call).  Defaults: 128 threads, persistent pool,
+ * 16 steps between refills, refill at 24 idle lanes. */
+typedef struct hrt_trace_config
+{
+  int threadsPerBlock; /* 64, 128 or 256                                          */
+  int persistent;      /* 1: persistent warp pool that refills idle lanes; 0: one thread per ray */
+  int stepsPerRefill;  /* traversal steps between refill checks (1..1024)        */
+  int refillLanes;     /* a warp refills when at least this many lanes are idle (1..32) */
+} hrt_trace_config;
+int hrt_scene_set_trace_config(hrt_scene* scene, int kind, const hrt_trace_config* config);
+int hrt_scene_get_trace_config(const hrt_scene* scene, int kind, hrt_trace_config* config);
+
 /* Traversal work of a batch, the quantity behind ISceneObject::GetStats
  * (core/CrossRT.h:154, core/FactoryRT.cpp:82-101): counters[0] = node pairs
  * fetched (HeavyRT counts 2 nodes, 64 bytes, per pair), counters[1] = triangle
@@ -175,6 +207,7 @@ int hrt_geom_info(const hrt_scene* scene, uint32_t geomId, uint64_t out[4], floa
 #define HRT_EXPORT_PRIM_INDICES    6 /* uint32[N] original triangle of each sorted position                */
 #define HRT_EXPORT_SORTED_INDICES  7 /* uint32[3N] index buffer in sorted order (BVH2CommonRT_host.cpp:45-64) */
 #define HRT_EXPORT_MORTON_UNSORTED 8 /* uint2[N] (code, triId) before the sort (lbvh.cpp:259-287)           */
+#define HRT_EXPORT_NODES4          9 /* the 4-wide nodes of a BVH4 layout, raw (128 or 64 bytes each)      */
 int hrt_geom_export(const hrt_scene* scene, uint32_t geomId, int what, void* dst, uint64_t capacityBytes,
                     uint64_t* sizeBytes);
 

@@ -137,6 +137,28 @@ def test_counters_match_oracle(native):
     assert gpairs == ocnt[0] and gtris <= ocnt[1]
 
 
+CONFIGS = [(64, 0, 1, 1), (128, 0, 1, 1), (256, 0, 1, 1), (128, 1, 1, 1), (128, 1, 4, 16), (256, 1, 32, 32),
+           (64, 1, 2, 8)]
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_trace_configs_give_identical_results(native, cfg):
+    """The launch shape (block size, persistent pool, refill policy) never
+    changes a result."""
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(21, 96, 96)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 96, 54),
+                           wl.rays_at_triangles(3, v, idx, 6000, jitter=0.02)])
+    o, _ = _oracle_expect(v, idx)
+    s, _ = _scene(v, idx)
+    for kind in (0, 1):
+        s.set_trace_config(kind, *cfg)
+        assert tuple(s.trace_config(kind).values()) == cfg
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), o.trace(rays).view(np.uint32))
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True))
+
+
 def test_device_queries_match_host_queries(native):
     import torch
 
