@@ -43,9 +43,26 @@ __global__ void __launch_bounds__(kThreads) k_depth(const BuildParams* __restric
   }
 }
 
+// First sorted triangle and one-past-last of the triangles under binary node s.
+__device__ __forceinline__ void node_range(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
+                                           uint32_t L, uint32_t nTris, uint32_t s, uint32_t& start, uint32_t& end)
+{
+  // leftmost / rightmost leaf under s: follow left (right) children down
+  uint32_t a = s, b = s;
+  while (a + 1u < L) a = lr[a].leftOffset;
+  while (b + 1u < L) b = lr[b].escapeIndex;
+  const uint32_t la = a - (L - 1), lb = b - (L - 1);
+  start = runStarts[la];
+  end = (lb + 1 < L) ? runStarts[lb + 1] : nTris;
+}
+
 // Role of each internal node: 1 = 4-wide node, 2 = merged leaf, 0 = absorbed.
+// mergeMode 0: merge when both children are leaves (the reference's rule);
+// mergeMode M > 0: merge when the subtree holds at most M triangles.
 __global__ void __launch_bounds__(kThreads) k_roles(const BuildParams* __restrict__ params,
-                                                    const BVHNode32* __restrict__ lr, const uint8_t* __restrict__ depth,
+                                                    const BVHNode32* __restrict__ lr,
+                                                    const uint32_t* __restrict__ runStarts, uint32_t nTris,
+                                                    const uint8_t* __restrict__ depth, int mergeMode,
                                                     uint8_t* __restrict__ role)
 {
   const uint32_t L = params->nLeaves;
@@ -54,9 +71,16 @@ __global__ void __launch_bounds__(kThreads) k_roles(const BuildParams* __restric
     uint8_t r = 0;
     if ((depth[i] & 1u) == 0u)
     {
-      const bool leafL = lr[i].leftOffset + 1u >= L;
-      const bool leafR = lr[i].escapeIndex + 1u >= L;
-      r = (i != 0 && leafL && leafR) ? 2 : 1;
+      bool merge;
+      if (mergeMode == 0)
+        merge = lr[i].leftOffset + 1u >= L && lr[i].escapeIndex + 1u >= L;
+      else
+      {
+        uint32_t st, en;
+        node_range(lr, runStarts, L, nTris, i, st, en);
+        merge = en - st <= (uint32_t)mergeMode;
+      }
+      r = (i != 0 && merge) ? 2 : 1;
     }
     role[i] = r;
   }
@@ -168,19 +192,6 @@ __global__ void __launch_bounds__(kThreads) k_scan_roles(const BuildParams* __re
   }
 }
 
-// First sorted triangle and one-past-last of the triangles under binary node s.
-__device__ __forceinline__ void node_range(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
-                                           uint32_t L, uint32_t nTris, uint32_t s, uint32_t& start, uint32_t& end)
-{
-  // leftmost / rightmost leaf under s: follow left (right) children down
-  uint32_t a = s, b = s;
-  while (a + 1u < L) a = lr[a].leftOffset;
-  while (b + 1u < L) b = lr[b].escapeIndex;
-  const uint32_t la = a - (L - 1), lb = b - (L - 1);
-  start = runStarts[la];
-  end = (lb + 1 < L) ? runStarts[lb + 1] : nTris;
-}
-
 struct Slot
 {
   float    lo[3], hi[3];
@@ -286,14 +297,19 @@ __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restric
           uint32_t st, en;
           node_range(lr, runStarts, L, nTris, s, st, en);
           slot[k].ref = kLeafBit | st;
-          // the merged leaf ends at the end of its right run: clear the 4-wide
-          // end flag (bit 1) at the end of the left run
-          const uint32_t leftLeaf = lr[s].leftOffset - (L - 1);
-          const uint32_t leftEnd = runStarts[leftLeaf + 1];
-          if (leftEnd > st && leftEnd < en)
+          // the merged leaf ends at the end of its last run: clear the 4-wide
+          // end flag (bit 1) at the ends of the runs before it
+          uint32_t a = s, b = s;
+          while (a + 1u < L) a = lr[a].leftOffset;
+          while (b + 1u < L) b = lr[b].escapeIndex;
+          for (uint32_t leaf = a - (L - 1); leaf < b - (L - 1); leaf++)
           {
-            uint32_t w = __float_as_uint(tris[leftEnd - 1].a.w);
-            tris[leftEnd - 1].a.w = __uint_as_float(w & ~2u);
+            const uint32_t runEnd = runStarts[leaf + 1];
+            if (runEnd > st && runEnd < en)
+            {
+              const uint32_t w = __float_as_uint(tris[runEnd - 1].a.w);
+              tris[runEnd - 1].a.w = __uint_as_float(w & ~2u);
+            }
           }
         }
         else
@@ -414,7 +430,7 @@ cudaError_t bvh4_plan(const Bvh4Buffers& b, int numSMs, cudaStream_t s)
   if (e != cudaSuccess) return e;
   const uint32_t g = grid_for(N, numSMs);
   k_depth<<<g, kThreads, 0, s>>>(b.params, b.parent, depth);
-  k_roles<<<g, kThreads, 0, s>>>(b.params, b.lr, depth, role);
+  k_roles<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, N, depth, b.mergeMode, role);
   k_scan_roles<<<(uint32_t)(nTiles ? nTiles : 1), kThreads, 0, s>>>(b.params, role, index, tiles + 4, tiles, total,
                                                                       &b.params->error);
   return cudaMemcpyAsync(b.hostNodeCount, total, 4, cudaMemcpyDeviceToHost, s);

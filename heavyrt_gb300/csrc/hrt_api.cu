@@ -69,6 +69,7 @@ struct hrt_scene
   std::vector<Instance> insts;
   bool                  committed = false;
   int                   layout = HRT_LAYOUT_BVH2;
+  int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
   InstanceDesc*         dInst = nullptr;
   uint32_t              nInstDev = 0;
   uint32_t*             dError = nullptr;
@@ -288,6 +289,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
     b4.parent = parent;
     b4.tris = g.tris;
     b4.scratch = scratch4;
+    b4.mergeMode = s->bvh4Merge;
     b4.hostNodeCount = &count4;
     HRT_CUDA(ctx, bvh4_plan(b4, ctx->numSMs, st));
     HRT_CUDA(ctx, cudaStreamSynchronize(st));
@@ -431,10 +433,11 @@ int hrt_scene_create(hrt_context* ctx, const char* buildName, hrt_scene** out)
   cudaSetDevice(ctx->device);
   hrt_scene* s = new hrt_scene();
   s->ctx = ctx;
-  if (cudaMalloc((void**)&s->dError, sizeof(uint32_t)) != cudaSuccess ||
+  // error word + the state of the first ray that ran out of its step budget
+  if (cudaMalloc((void**)&s->dError, 8 * sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc((void**)&s->dCounters, 2 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc((void**)&s->dRayCounters, kCounterSlots * sizeof(unsigned int)) != cudaSuccess ||
-      cudaMemset(s->dError, 0, sizeof(uint32_t)) != cudaSuccess)
+      cudaMemset(s->dError, 0, 8 * sizeof(uint32_t)) != cudaSuccess)
   {
     if (s->dError) cudaFree(s->dError);
     if (s->dCounters) cudaFree(s->dCounters);
@@ -617,7 +620,25 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
   if (st != HRT_OK) return st;
   const size_t outBytes = kind == 0 ? sizeof(hrt_hit) * n : n;
   HRT_CUDA(ctx, cudaMemcpyAsync(out, s->stageOut, outBytes, cudaMemcpyDeviceToHost, cs));
+  uint32_t ew[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  HRT_CUDA(ctx, cudaMemcpyAsync(ew, s->dError, sizeof(ew), cudaMemcpyDeviceToHost, cs));
   HRT_CUDA(ctx, cudaStreamSynchronize(cs));
+  const uint32_t err = ew[0];
+  if (err)
+  {
+    cudaMemsetAsync(s->dError, 0, sizeof(ew), cs);
+    cudaStreamSynchronize(cs);
+    if (err & kErrStepBudget)
+    {
+      char msg[200];
+      std::snprintf(msg, sizeof(msg),
+                    "a ray exceeded the traversal step budget (ray %u, ref 0x%08x, stack depth %d)", ew[2], ew[3],
+                    (int)ew[4]);
+      return fail(ctx, HRT_ERR_DEVICE_CHECK, msg);
+    }
+    if (err & kErrStack) return fail(ctx, HRT_ERR_DEVICE_CHECK, "traversal stack bound exceeded");
+    return fail(ctx, HRT_ERR_DEVICE_CHECK, "device-side check failed during a query");
+  }
   return HRT_OK;
 }
 
@@ -755,6 +776,20 @@ int hrt_scene_set_layout(hrt_scene* s, int layout)
   if (!s->geoms.empty()) return fail(s->ctx, HRT_ERR_STATE, "the layout is chosen before the first geometry is added");
   s->layout = layout;
   return HRT_OK;
+}
+
+int hrt_scene_set_option(hrt_scene* s, int option, int value)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(s->mu);
+  switch (option)
+  {
+    case HRT_OPTION_BVH4_MERGE:
+      if (value < 0 || value > 64) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "BVH4 merge value out of range");
+      s->bvh4Merge = value;
+      return HRT_OK;
+    default: return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown option");
+  }
 }
 
 int hrt_scene_get_layout(const hrt_scene* s, int* layout)

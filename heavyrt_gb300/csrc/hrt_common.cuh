@@ -19,6 +19,7 @@ constexpr uint32_t kErrLeafCount   = 1u << 1;  // more than 127 triangles share 
 constexpr uint32_t kErrWaitTimeout = 1u << 2;  // a decoupled look-back wait gave up
 constexpr uint32_t kErrStack       = 1u << 3;  // traversal stack bound exceeded
 constexpr uint32_t kErrLayout      = 1u << 4;  // inconsistent tree (refit did not reach the root)
+constexpr uint32_t kErrStepBudget  = 1u << 5;  // a ray exceeded its traversal step budget (ended as a miss)
 
 // HeavyRT's BVHNode (core/builders/cbvh.h:20-26): 32 bytes, the layout of the
 // LR tree the builder exports for parity checks.

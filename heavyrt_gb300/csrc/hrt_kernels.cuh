@@ -60,6 +60,7 @@ struct Bvh4Buffers
   const uint32_t*  runStarts;       // L
   const uint32_t*  parent;          // 2L-1
   TriRec*          tris;            // N; bit 1 of a.w marks 4-wide leaf ends
+  int              mergeMode;       // 0: merge two leaf children (reference rule); M > 0: merge subtrees of <= M triangles
   void*            scratch;         // bvh4_scratch_bytes(nTris)
   uint32_t*        hostNodeCount;   // host word receiving the node count (0 when L == 1)
 };

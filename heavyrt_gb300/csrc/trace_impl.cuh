@@ -247,7 +247,28 @@ struct Lane
   uint32_t inst;      // current instance
   uint32_t cur;       // current record / leaf reference
   int      top;       // stack depth
+  uint32_t budget;    // steps left for this ray
 };
+
+// Upper bound on the steps of one ray: far above any real traversal (a ray
+// visits each node at most once per instance); reaching it means a broken
+// tree, and the ray ends as a miss with kErrStepBudget instead of looping.
+constexpr uint32_t kStepBudget = 1u << 24;
+
+// The first lane to run out of budget records its state after the error word:
+// [1] = 1 (taken), [2] ray, [3] current ref, [4] stack depth.
+__device__ __forceinline__ bool out_of_budget(Lane& L, uint32_t* errorWord)
+{
+  if (L.budget-- != 0u) return false;
+  atomicOr(errorWord, kErrStepBudget);
+  if (atomicCAS(errorWord + 1, 0u, 1u) == 0u)
+  {
+    errorWord[2] = L.ray;
+    errorWord[3] = L.cur;
+    errorWord[4] = (uint32_t)L.top;
+  }
+  return true;
+}
 
 // Advances the lane's instance cursor to the next instance with triangles,
 // starting at `from`; prepares the ray for it.  Returns false when none is left.
@@ -266,73 +287,63 @@ __device__ __forceinline__ bool begin_instance(Lane& L, const InstanceDesc* __re
   return false;
 }
 
-// One traversal step (an internal node, or a leaf followed by a pop).
-// Returns true when the lane's ray is finished.
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
-__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t nInst,
-                                     uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
-                                     uint32_t* errorWord)
+template <int LAYOUT> struct EndBit
 {
-  const InstanceDesc& d = inst[L.inst];
-  bool pop = false;
+  static constexpr uint32_t value = LAYOUT == 0 ? 1u : 2u;  // flag bit that ends a leaf of this layout
+};
+
+// Visits the internal node L.cur: tests its children, continues with the
+// nearest hit child (child 0 on equal entry distance) and pushes the others,
+// farthest first.  Returns 1 when no child is hit (the caller pops), 0
+// otherwise, -1 when the stack bound would be exceeded (reported).
+template <int LAYOUT, bool COUNT, int THREADS>
+__device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32_t* __restrict__ stack,
+                                          uint64_t& nPairs, uint32_t* errorWord)
+{
   if constexpr (LAYOUT != 0)
   {
-    // 4-wide node: test the four slots, continue with the nearest hit child,
-    // push the other hit children farthest first (HeavyRT's BVH4 order,
-    // core/BVH4CommonRT.cpp:49-246).
-    if ((L.cur & kLeafBit) == 0u)
-    {
-      using N = typename Node4Type<LAYOUT>::type;
-      Boxes4 B;
-      load_node4(reinterpret_cast<const N*>(d.nodes4) + L.cur, B);
-      if (COUNT) nPairs++;
-      float key[4];
-      uint32_t ref[4] = {B.ref.x, B.ref.y, B.ref.z, B.ref.w};
+    // 4-wide node: HeavyRT's BVH4 order (core/BVH4CommonRT.cpp:49-246)
+    using N = typename Node4Type<LAYOUT>::type;
+    Boxes4 B;
+    load_node4(reinterpret_cast<const N*>(d.nodes4) + L.cur, B);
+    if (COUNT) nPairs++;
+    float key[4];
+    uint32_t ref[4] = {B.ref.x, B.ref.y, B.ref.z, B.ref.w};
 #pragma unroll
-      for (int k = 0; k < 4; k++)
-      {
-        float tn, tf;
-        slab(L.r, B.lo[0][k], B.lo[1][k], B.lo[2][k], B.hi[0][k], B.hi[1][k], B.hi[2][k], tn, tf);
-        const bool hit = ref[k] != kEmptyRef && tn <= tf && tf >= L.r.tNear && tn <= L.h.t;
-        key[k] = hit ? tn : INFINITY;
-        ref[k] = hit ? ref[k] : kEmptyRef;
-      }
-      cswap(key[0], ref[0], key[1], ref[1]);
-      cswap(key[2], ref[2], key[3], ref[3]);
-      cswap(key[0], ref[0], key[2], ref[2]);
-      cswap(key[1], ref[1], key[3], ref[3]);
-      cswap(key[1], ref[1], key[2], ref[2]);
-      int f = 0;
-      while (f < 4 && ref[f] == kEmptyRef) f++;
-      if (f == 4)
-        pop = true;
-      else
-      {
-        L.cur = ref[f];
-#pragma unroll
-        for (int k = 3; k >= 1; k--)
-          if (k > f && ref[k] != kEmptyRef)
-          {
-            if (L.top >= kStack4)
-            {
-              atomicOr(errorWord, kErrStack);
-              return true;
-            }
-            stack[L.top * THREADS] = ref[k];
-            L.top++;
-          }
-      }
-    }
-    else
+    for (int k = 0; k < 4; k++)
     {
-      if (L.cur != kEmptyRef &&
-          leaf_test<ANY, COUNT, 2u>(d.tris, L.cur & ~kLeafBit, L.r, L.h, d.instId, d.geomId, nTris))
-        return true;  // any-hit found
-      pop = true;
+      float tn, tf;
+      slab(L.r, B.lo[0][k], B.lo[1][k], B.lo[2][k], B.hi[0][k], B.hi[1][k], B.hi[2][k], tn, tf);
+      const bool hit = ref[k] != kEmptyRef && tn <= tf && tf >= L.r.tNear && tn <= L.h.t;
+      key[k] = hit ? tn : INFINITY;
+      ref[k] = hit ? ref[k] : kEmptyRef;
     }
+    cswap(key[0], ref[0], key[1], ref[1]);
+    cswap(key[2], ref[2], key[3], ref[3]);
+    cswap(key[0], ref[0], key[2], ref[2]);
+    cswap(key[1], ref[1], key[3], ref[3]);
+    cswap(key[1], ref[1], key[2], ref[2]);
+    int f = 0;
+    while (f < 4 && ref[f] == kEmptyRef) f++;
+    if (f == 4) return 1;
+    L.cur = ref[f];
+#pragma unroll
+    for (int k = 3; k >= 1; k--)
+      if (k > f && ref[k] != kEmptyRef)
+      {
+        if (L.top >= kStack4)
+        {
+          atomicOr(errorWord, kErrStack);
+          return -1;
+        }
+        stack[L.top * THREADS] = ref[k];
+        L.top++;
+      }
+    return 0;
   }
-  else if ((L.cur & kLeafBit) == 0u)
+  else
   {
+    // child pair: BVH2TraverseC32's decisions (core/BVH2CommonRT.cpp:88-113)
     const float4* p = reinterpret_cast<const float4*>(d.recs + L.cur);
     const float4 a = __ldg(p + 0);
     const float4 b = __ldg(p + 1);
@@ -344,7 +355,7 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
     slab(L.r, b.z, b.w, c.x, c.y, c.z, c.w, t1n, t1f);
     const bool h0 = (t0n <= t0f) && (t0f >= L.r.tNear) && (t0n <= L.h.t);
     const bool h1 = (t1n <= t1f) && (t1f >= L.r.tNear) && (t1n <= L.h.t);
-    pop = !h0 && !h1;
+    if (!h0 && !h1) return 1;
     L.cur = h0 ? e.x : e.y;
     if (h0 && h1)
     {
@@ -353,15 +364,34 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
       if (L.top >= kStack2)
       {
         atomicOr(errorWord, kErrStack);
-        return true;
+        return -1;
       }
       stack[L.top * THREADS] = first0 ? e.y : e.x;
       L.top++;
     }
+    return 0;
+  }
+}
+
+// One traversal step (an internal node, or a leaf followed by a pop).
+// Returns true when the lane's ray is finished.
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t nInst,
+                                     uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
+                                     uint32_t* errorWord)
+{
+  const InstanceDesc& d = inst[L.inst];
+  bool pop;
+  if ((L.cur & kLeafBit) == 0u)
+  {
+    const int r = visit_node<LAYOUT, COUNT, THREADS>(L, d, stack, nPairs, errorWord);
+    if (r < 0) return true;
+    pop = (r == 1);
   }
   else
   {
-    if (L.cur != kEmptyRef && leaf_test<ANY, COUNT>(d.tris, L.cur & ~kLeafBit, L.r, L.h, d.instId, d.geomId, nTris))
+    if (L.cur != kEmptyRef &&
+        leaf_test<ANY, COUNT, EndBit<LAYOUT>::value>(d.tris, L.cur & ~kLeafBit, L.r, L.h, d.instId, d.geomId, nTris))
       return true;  // any-hit found
     pop = true;
   }
@@ -395,6 +425,7 @@ __device__ __forceinline__ void start_ray(Lane& L, uint32_t i, const float4* __r
   L.h.t = L.di.w;
   L.h.u = L.h.v = 0.0f;
   L.h.prim = L.h.inst = L.h.geom = 0xFFFFFFFFu;
+  L.budget = kStepBudget;
 }
 
 template <bool COUNT>
@@ -458,7 +489,8 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
     {
       for (int s = 0; s < steps; s++)
       {
-        if (step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord))
+        if (out_of_budget(L, errorWord) ||
+            step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord))
         {
           write_result<ANY>(L, out);
           L.ray = kNoRay;
@@ -485,7 +517,8 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
     Lane L;
     start_ray(L, i, rays);
     if (begin_instance(L, inst, nInst, 0))
-      while (!step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord)) {}
+      while (!out_of_budget(L, errorWord) &&
+             !step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord)) {}
     write_result<ANY>(L, out);
   }
   flush_counters<COUNT>(nPairs, nTris, counters);

@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
         "hrt_host_alloc": (i32, [u64, C.POINTER(vp)]),
         "hrt_host_free": (i32, [vp]),
         "hrt_scene_set_layout": (i32, [vp, i32]),
+        "hrt_scene_set_option": (i32, [vp, i32, i32]),
         "hrt_scene_get_layout": (i32, [vp, C.POINTER(i32)]),
         "hrt_scene_set_trace_config": (i32, [vp, i32, C.POINTER(TraceConfig)]),
         "hrt_scene_get_trace_config": (i32, [vp, i32, C.POINTER(TraceConfig)]),
@@ -212,6 +213,10 @@ class SceneRT:
             layout = LAYOUT_NAMES[layout.lower()]
         if layout != LAYOUT_BVH2:
             self.ctx.check(lib().hrt_scene_set_layout(self._h, int(layout)), "set_layout")
+
+    def set_bvh4_merge(self, value: int):
+        """0: the reference's leaf merge rule; M: merge subtrees of <= M triangles."""
+        self.ctx.check(lib().hrt_scene_set_option(self._h, 1, int(value)), "set_option")
 
     @property
     def layout(self) -> int:

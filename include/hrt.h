@@ -113,6 +113,15 @@ int hrt_scene_destroy(hrt_scene* scene);
 int hrt_scene_set_layout(hrt_scene* scene, int layout);
 int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
 
+/* Build options (applied to geometry added afterwards).  No reference
+ * counterpart beyond the collapse rule itself.
+ *   HRT_OPTION_BVH4_MERGE  0: a node whose two children are leaves becomes
+ *                          one leaf (BVH2ToBVH4, core/builders/cbvh.cpp:242-255);
+ *                          M in 1..64: a subtree of at most M triangles becomes
+ *                          one leaf (1 never merges). */
+#define HRT_OPTION_BVH4_MERGE 1
+int hrt_scene_set_option(hrt_scene* scene, int option, int value);
+
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */
 int hrt_clear_geom(hrt_scene* scene);
 

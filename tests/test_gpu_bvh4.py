@@ -11,10 +11,12 @@ MISS = 0xFFFFFFFF
 LAYOUTS = [1, 2, 3]  # BVH4_F32, BVH4_F16, BVH4_Q8
 
 
-def _scene(v, idx, layout):
+def _scene(v, idx, layout, merge=0):
     from heavyrt_gb300 import SceneRT
 
     s = SceneRT(layout=layout)
+    if merge:
+        s.set_bvh4_merge(merge)
     gid = s.AddGeom_Triangles3f(v, v.shape[0], idx, idx.size, vByteStride=16)
     s.AddInstance(gid)
     s.CommitScene()
@@ -48,15 +50,17 @@ def _cases():
     return out
 
 
-@pytest.mark.parametrize("layout", LAYOUTS)
-def test_bvh4_layouts_match_oracle(native, layout):
+@pytest.mark.parametrize("layout,merge", [(1, 0), (2, 0), (3, 0), (1, 1), (2, 4), (3, 8)])
+def test_bvh4_layouts_match_oracle(native, layout, merge):
     from heavyrt_gb300 import engine as E
     from oracle import oracle as orc
 
     for name, v, idx, rays in _cases():
         o = orc.OracleBVH(v, idx)
-        s, gid = _scene(v, idx, layout)
-        np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True), err_msg=name)
+        s, gid = _scene(v, idx, layout, merge)
+        for persistent in (0, 1):
+            s.set_trace_config(1, persistent=persistent)
+            np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True), err_msg=name)
         _check_nearest(s.RayQuery_NearestHit(rays), o.trace(rays), o.sorted_indices(), v)
         # the 4-wide tree shares the binary tree's sorted order
         np.testing.assert_array_equal(s.export(gid, E.EXPORT_PRIM_INDICES), o.prim_indices())

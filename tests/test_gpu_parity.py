@@ -138,7 +138,7 @@ def test_counters_match_oracle(native):
 
 
 CONFIGS = [(64, 0, 1, 1), (128, 0, 1, 1), (256, 0, 1, 1), (128, 1, 1, 1), (128, 1, 4, 16), (256, 1, 32, 32),
-           (64, 1, 2, 8)]
+           (64, 1, 2, 8), (128, 1, 16, 24)]
 
 
 @pytest.mark.parametrize("cfg", CONFIGS)
