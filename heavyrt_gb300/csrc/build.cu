@@ -3,6 +3,7 @@
 // records.  Every stage reproduces the integer and float results of HeavyRT's
 // LBVHBuilder (core/builders/lbvh.cpp) bit for bit; float arithmetic is written
 // with explicit round-to-nearest intrinsics so that no multiply-add is fused.
+#include "build_common.cuh"
 #include "hrt_kernels.cuh"
 
 namespace hrt
@@ -66,30 +67,10 @@ __global__ void k_box_final(const float4* __restrict__ partial, uint32_t nPartia
     mn[0] = lm_min(mn[0], a.x); mn[1] = lm_min(mn[1], a.y); mn[2] = lm_min(mn[2], a.z); mn[3] = lm_min(mn[3], a.w);
     mx[0] = lm_max(mx[0], c.x); mx[1] = lm_max(mx[1], c.y); mx[2] = lm_max(mx[2], c.z); mx[3] = lm_max(mx[3], c.w);
   }
-  for (int c = 0; c < 4; c++)
-  {
-    params->bmin[c] = mn[c];
-    params->bmax[c] = mx[c];
-    const float lo = __fsub_rn(mn[c], 1e-4f);
-    const float hi = __fadd_rn(mx[c], 1e-4f);
-    const float ext = __fsub_rn(hi, lo);
-    float inv = __fdiv_rn(1.0f, ext);
-    if (c < 3 && fabsf(ext) < 1e-20f) inv = 0.0f;
-    params->scale[c] = __fmul_rn(1024.0f, inv);
-  }
+  bc::zindex_scale(mn, mx, params);
 }
 
 // ---------------------------------------------------------------- Morton codes
-// SpreadBits / ZIndex3D, core/builders/lbvh.cpp:25-39.
-__device__ __forceinline__ uint32_t spread_bits(int x, int offset)
-{
-  x = (x | (x << 10)) & 0x000F801F;
-  x = (x | (x << 4)) & 0x00E181C3;
-  x = (x | (x << 2)) & 0x03248649;
-  x = (x | (x << 2)) & 0x09249249;
-  return (uint32_t)x << offset;
-}
-
 // kernel1D_EvalMortonCodesFromTriangles, core/builders/lbvh.cpp:259-287: box
 // centre (or the centroid 0.33333333*(v1+v2+v3) when fewer than 256
 // triangles), quantised against the scene box with truncation toward zero.
@@ -106,24 +87,7 @@ __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ 
     atomicOr(errorWord, kErrIndexRange);
     ia = ib = ic = 0;
   }
-  const float4 a = v[ia], b = v[ib], c = v[ic];
-  const float pa[3] = {a.x, a.y, a.z}, pb[3] = {b.x, b.y, b.z}, pc[3] = {c.x, c.y, c.z};
-  int q[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-  {
-    float center;
-    if (nTris < 256)
-      center = __fmul_rn(0.33333333f, __fadd_rn(__fadd_rn(pa[k], pb[k]), pc[k]));
-    else
-    {
-      const float mn = lm_min(pa[k], lm_min(pb[k], pc[k]));
-      const float mx = lm_max(pa[k], lm_max(pb[k], pc[k]));
-      center = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
-    }
-    q[k] = __float2int_rz(__fmul_rn(params->scale[k], __fsub_rn(center, params->bmin[k])));
-  }
-  keys[i] = spread_bits(q[0], 0) | spread_bits(q[1], 1) | spread_bits(q[2], 2);
+  keys[i] = bc::morton_code(v[ia], v[ib], v[ic], nTris, params->bmin, params->scale);
   vals[i] = i;
 }
 
@@ -132,23 +96,14 @@ __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ 
 // (core/builders/lbvh.cpp:289-319,762-767) as one single-pass scan with
 // decoupled look-back: flag = code differs from its predecessor; flagged
 // positions are appended to (compressed, runStarts) in order.
-constexpr int      kScanItems   = 16;
-constexpr uint32_t kScanTile    = kThreads * kScanItems;
-constexpr uint32_t kFlagAgg     = 1u << 30;
-constexpr uint32_t kFlagPrefix  = 2u << 30;
-constexpr uint32_t kValueMask   = (1u << 30) - 1u;
-constexpr uint32_t kSpinLimit   = 1u << 22;
-
-__device__ __forceinline__ void store_relaxed(uint32_t* p, uint32_t v)
-{
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ uint32_t load_relaxed(const uint32_t* p)
-{
-  uint32_t v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
+using bc::kScanItems;
+constexpr uint32_t kScanTile = kThreads * kScanItems;
+using bc::kFlagAgg;
+using bc::kFlagPrefix;
+using bc::kValueMask;
+using bc::kSpinLimit;
+using bc::load_relaxed;
+using bc::store_relaxed;
 
 __global__ void __launch_bounds__(kThreads) k_compact_runs(const uint32_t* __restrict__ keys, uint32_t n,
                                                            uint32_t* __restrict__ compressed,
@@ -156,94 +111,8 @@ __global__ void __launch_bounds__(kThreads) k_compact_runs(const uint32_t* __res
                                                            uint32_t* tileCounter, BuildParams* params,
                                                            uint32_t* errorWord)
 {
-  __shared__ uint32_t s_tile, s_prefix;
-  __shared__ uint32_t s_warp[kThreads / 32 + 1];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_tile = atomicAdd(tileCounter, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  const uint32_t base = tile * kScanTile + tid * kScanItems;
-
-  uint32_t key[kScanItems];
-  uint32_t flags = 0, cnt = 0;
-  uint32_t prev = (base > 0 && base - 1 < n) ? keys[base - 1] : 0u;
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++)
-  {
-    const uint32_t i = base + k;
-    key[k] = (i < n) ? keys[i] : 0u;
-    const bool f = (i < n) && (i == 0 || key[k] != prev);
-    prev = key[k];
-    flags |= (f ? 1u : 0u) << k;
-    cnt += f ? 1u : 0u;
-  }
-  // block exclusive scan of cnt
-  uint32_t incl = cnt;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1)
-  {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (tid == 0)
-  {
-    uint32_t run = 0;
-    for (int w = 0; w < kThreads / 32; w++)
-    {
-      const uint32_t t = s_warp[w];
-      s_warp[w] = run;
-      run += t;
-    }
-    s_warp[kThreads / 32] = run;
-    // publish and look back (one value per tile)
-    uint32_t* my = tileStatus + tile;
-    uint32_t excl = 0;
-    if (tile == 0)
-      store_relaxed(my, kFlagPrefix | run);
-    else
-    {
-      store_relaxed(my, kFlagAgg | run);
-      int64_t t = (int64_t)tile - 1;
-      uint32_t spins = 0;
-      while (t >= 0)
-      {
-        const uint32_t s = load_relaxed(tileStatus + t);
-        const uint32_t flag = s & ~kValueMask;
-        if (flag == 0u)
-        {
-          if (++spins > kSpinLimit)
-          {
-            atomicOr(errorWord, kErrWaitTimeout);
-            break;
-          }
-          if (spins > 64) __nanosleep(32);
-          continue;
-        }
-        excl += s & kValueMask;
-        if (flag == kFlagPrefix) break;
-        t--;
-      }
-      store_relaxed(my, kFlagPrefix | (excl + run));
-    }
-    s_prefix = excl;
-    const uint32_t tiles = (n + kScanTile - 1) / kScanTile;
-    if (tile == tiles - 1) params->nLeaves = (excl + run <= n) ? excl + run : n;
-  }
-  __syncthreads();
-  uint32_t pos = s_prefix + s_warp[warp] + incl - cnt;
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++)
-    if (flags & (1u << k))
-    {
-      if (pos < n)  // always true unless a look-back wait gave up (reported through errorWord)
-      {
-        compressed[pos] = key[k];
-        runStarts[pos] = base + k;
-      }
-      pos++;
-    }
+  bc::compact_runs_tile<kThreads>(keys, n, nullptr, 0u, compressed, runStarts, tileStatus, tileCounter,
+                                  &params->nLeaves, errorWord);
 }
 
 // ---------------------------------------------------------------- leaves
@@ -311,13 +180,6 @@ __global__ void __launch_bounds__(kThreads) k_leaves(const float4* __restrict__ 
 // delta() and kernel1D_Karras12, core/builders/lbvh.cpp:386-441.  The codes
 // are unique after compaction, so delta(i,j) is the count of leading zeros of
 // their XOR (32 for equal codes, -1 out of range, as the reference defines).
-__device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ c, int L, int i, int j)
-{
-  if (j < 0 || j >= L) return -1;
-  const uint32_t x = c[i] ^ c[j];
-  return x == 0u ? 32 : __clz(x);
-}
-
 __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict__ codes,
                                                      const BuildParams* __restrict__ params, BVHNode32* __restrict__ lr,
                                                      uint32_t* __restrict__ parent)
@@ -325,22 +187,8 @@ __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict_
   const int L = (int)params->nLeaves;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < L - 1; i += gridDim.x * kThreads)
   {
-    const int dl = karras_delta(codes, L, i, i + 1) - karras_delta(codes, L, i, i - 1);
-    const int d = (dl > 0) - (dl < 0);
-    const int dmin = karras_delta(codes, L, i, i - d);
-    int lmax = 2;
-    while (karras_delta(codes, L, i, i + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t > 0; t >>= 1)
-      if (karras_delta(codes, L, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = karras_delta(codes, L, i, j);
-    int s = 0;
-    for (int t = (l + 1) >> 1; t > 0; t = (t == 1 ? 0 : (t + 1) >> 1))
-      if (karras_delta(codes, L, i, i + (s + t) * d) > dnode) s += t;
-    const int gamma = i + s * d + (d < 0 ? d : 0);
-    const uint32_t left = ((i < j ? i : j) == gamma) ? (uint32_t)(L - 1 + gamma) : (uint32_t)gamma;
-    const uint32_t right = ((i > j ? i : j) == gamma + 1) ? (uint32_t)(L - 1 + gamma + 1) : (uint32_t)(gamma + 1);
+    uint32_t left, right;
+    bc::karras_node(codes, L, i, left, right);
     lr[i].leftOffset = left;
     lr[i].escapeIndex = right;
     parent[left] = (uint32_t)i;
@@ -354,12 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict_
 // and the second child to arrive at a node computes it, so every node is
 // computed once from its finished children: box = (min, max) of the children
 // in (left, right) order, count = children's counts + 2.
-__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v)
-{
-  uint32_t old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
+using bc::atomic_add_acq_rel;
 
 __global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode32* lr,
                                                     uint32_t* lrCount, const uint32_t* __restrict__ parent,

@@ -50,6 +50,7 @@ struct Geom
   float        box[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   void*        nodes4 = nullptr;  // 4-wide nodes of the scene's layout
   uint32_t     nNodes4 = 0;
+  bool         shared = false;    // arrays point into a batch allocation (hrt_add_geoms_triangles3f_batched)
 };
 
 struct Instance
@@ -67,6 +68,7 @@ struct hrt_scene
   hrt_context*          ctx = nullptr;
   std::vector<Geom>     geoms;
   std::vector<Instance> insts;
+  std::vector<void*>    batchAllocs;  // device allocations shared by batch-built geometries
   bool                  committed = false;
   int                   layout = HRT_LAYOUT_BVH2;
   int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
@@ -114,10 +116,13 @@ int cuda_fail(hrt_context* ctx, cudaError_t e, const char* what)
 
 void free_geom(Geom& g)
 {
-  void* ptrs[] = {g.verts, g.keys, g.vals, g.keysUnsorted, g.compressed, g.runStarts, g.lr,
-                  g.lrCount, g.recs, g.tris, g.sortedIdx, g.params, g.nodes4};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
+  if (!g.shared)
+  {
+    void* ptrs[] = {g.verts, g.keys, g.vals, g.keysUnsorted, g.compressed, g.runStarts, g.lr,
+                    g.lrCount, g.recs, g.tris, g.sortedIdx, g.params, g.nodes4};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+  }
   g = Geom();
 }
 
@@ -329,6 +334,245 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   return HRT_OK;
 }
 
+// Device allocation owned by a batch: recorded in `owned` (freed together).
+template <typename T> cudaError_t balloc(T** p, size_t count, std::vector<void*>& owned)
+{
+  const cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+  if (e == cudaSuccess) owned.push_back(*p);
+  return e;
+}
+
+inline size_t align_up(size_t b, size_t a) { return (b + a - 1) / a * a; }
+
+// Builds G geometries with one segmented LBVH build (build_batch.cu) and, for
+// a 4-wide layout, collapses each.  On success appends G geometries whose
+// arrays point into allocations recorded in `owned`.
+int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOff, const uint32_t* idx,
+                const uint64_t* iOff, uint64_t stride, std::vector<Geom>& out, std::vector<void*>& owned)
+{
+  hrt_context* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  const uint64_t V = vOff[G], N = iOff[G] / 3;
+  std::vector<uint32_t> hv(G + 1), ht(G + 1);
+  for (uint32_t i = 0; i <= G; i++)
+  {
+    hv[i] = (uint32_t)vOff[i];
+    ht[i] = (uint32_t)(iOff[i] / 3);
+  }
+  // inputs
+  float4* verts = nullptr;
+  uint32_t *dVOff = nullptr, *dTOff = nullptr, *dIdx = nullptr;
+  HRT_CUDA(ctx, balloc(&verts, V, owned));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&dVOff, sizeof(uint32_t) * (G + 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&dTOff, sizeof(uint32_t) * (G + 1), st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(dVOff, hv.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(dTOff, ht.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, st));
+  if (V)
+  {
+    uint8_t* raw = nullptr;
+    if (stride == 16)
+      HRT_CUDA(ctx, cudaMemcpyAsync(verts, vpos, 16 * V, cudaMemcpyHostToDevice, st));
+    else
+    {
+      HRT_CUDA(ctx, cudaMallocAsync((void**)&raw, stride * V, st));
+      HRT_CUDA(ctx, cudaMemcpyAsync(raw, vpos, stride * V, cudaMemcpyHostToDevice, st));
+    }
+    const uint8_t* src = raw ? raw : reinterpret_cast<const uint8_t*>(verts);
+    uint64_t blocks = (V + 255) / 256;
+    if (blocks > 65535) blocks = 65535;
+    k_pack_verts<<<(uint32_t)blocks, 256, 0, st>>>(src, V, stride, verts);
+    HRT_CUDA(ctx, cudaGetLastError());
+    if (raw) HRT_CUDA(ctx, cudaFreeAsync(raw, st));
+  }
+  BatchBuffers b{};
+  b.verts = verts;
+  b.vertOffsets = dVOff;
+  b.triOffsets = dTOff;
+  b.G = G;
+  b.nTris = (uint32_t)N;
+  uint32_t *keysAlt = nullptr, *valsAlt = nullptr, *parent = nullptr, *visit = nullptr;
+  void* scratch = nullptr;
+  HRT_CUDA(ctx, balloc(&b.keys, N, owned));
+  HRT_CUDA(ctx, balloc(&b.vals, N, owned));
+  HRT_CUDA(ctx, balloc(&b.keysUnsorted, N, owned));
+  HRT_CUDA(ctx, balloc(&b.compressed, N, owned));
+  HRT_CUDA(ctx, balloc(&b.runStarts, N, owned));
+  HRT_CUDA(ctx, balloc(&b.lr, 2 * N, owned));
+  HRT_CUDA(ctx, balloc(&b.lrCount, 2 * N, owned));
+  HRT_CUDA(ctx, balloc(&b.recs, N, owned));
+  HRT_CUDA(ctx, balloc(&b.tris, N, owned));
+  HRT_CUDA(ctx, balloc(&b.sortedIdx, 3 * N, owned));
+  HRT_CUDA(ctx, balloc(&b.params, G, owned));
+  // offsets (4 x (G+1)), counts (4) and the error word in one array
+  uint32_t* offs = nullptr;
+  HRT_CUDA(ctx, balloc(&offs, 4 * ((size_t)G + 1) + 8, owned));
+  b.leafOffsets = offs;
+  b.intOffsets = offs + (G + 1);
+  b.nodeOffsets = offs + 2 * (G + 1);
+  b.recOffsets = offs + 3 * (G + 1);
+  b.counts = offs + 4 * (G + 1);
+  b.errorWord = b.counts + 4;
+  HRT_CUDA(ctx, cudaMemsetAsync(offs, 0, sizeof(uint32_t) * (4 * ((size_t)G + 1) + 8), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&dIdx, sizeof(uint32_t) * 3 * (N ? N : 1), st));
+  if (N) HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * 3 * N, cudaMemcpyHostToDevice, st));
+  b.idx = dIdx;
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&keysAlt, sizeof(uint32_t) * (N ? N : 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&valsAlt, sizeof(uint32_t) * (N ? N : 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * 2 * (N ? N : 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * (N ? N : 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync(&scratch, build_batch_scratch_bytes((uint32_t)N, G), st));
+  b.keysAlt = keysAlt;
+  b.valsAlt = valsAlt;
+  b.parent = parent;
+  b.visit = visit;
+  b.scratch = scratch;
+  if (N == 0) HRT_CUDA(ctx, cudaMemsetAsync(b.params, 0, sizeof(BuildParams) * G, st));
+
+  cudaEvent_t e0, e1;
+  HRT_CUDA(ctx, cudaEventCreate(&e0));
+  HRT_CUDA(ctx, cudaEventCreate(&e1));
+  HRT_CUDA(ctx, cudaEventRecord(e0, st));
+  cudaError_t be = build_lbvh_batch(b, ctx->numSMs, st);
+  if (be != cudaSuccess) return cuda_fail(ctx, be, "build_lbvh_batch");
+  std::vector<BuildParams> hp(G);
+  std::vector<uint32_t> ho(4 * ((size_t)G + 1) + 8);
+  HRT_CUDA(ctx, cudaMemcpyAsync(ho.data(), offs, sizeof(uint32_t) * ho.size(), cudaMemcpyDeviceToHost, st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(hp.data(), b.params, sizeof(BuildParams) * G, cudaMemcpyDeviceToHost, st));
+  HRT_CUDA(ctx, cudaStreamSynchronize(st));
+  const uint32_t* hLeaf = ho.data();
+  const uint32_t* hNode = ho.data() + 2 * (G + 1);
+  const uint32_t* hRec = ho.data() + 3 * (G + 1);
+  uint32_t err = ho[4 * ((size_t)G + 1) + 4];
+
+  // 4-wide collapse of every geometry with triangles: plan all, one
+  // synchronisation for the node counts, then emit into one node array
+  std::vector<uint32_t> count4(G, 0);
+  std::vector<size_t> node4Off(G, 0);
+  void* nodes4 = nullptr;
+  size_t nodeBytes = 0;
+  void* scratch4 = nullptr;
+  std::vector<Bvh4Buffers> b4(G);
+  if (s->layout != HRT_LAYOUT_BVH2 && N > 0 && err == 0)
+  {
+    nodeBytes = (s->layout == HRT_LAYOUT_BVH4_F32) ? sizeof(Node4F32) : sizeof(Node4F16);
+    std::vector<size_t> scrOff(G + 1, 0);
+    for (uint32_t i = 0; i < G; i++)
+      scrOff[i + 1] = scrOff[i] + (ht[i + 1] > ht[i] ? align_up(bvh4_scratch_bytes(ht[i + 1] - ht[i]), 256) : 0);
+    HRT_CUDA(ctx, cudaMallocAsync(&scratch4, scrOff[G] ? scrOff[G] : 256, st));
+    uint32_t* hostCounts = nullptr;
+    HRT_CUDA(ctx, cudaMallocHost((void**)&hostCounts, sizeof(uint32_t) * G));
+    for (uint32_t i = 0; i < G; i++)
+    {
+      hostCounts[i] = 0;
+      const uint32_t Ni = ht[i + 1] - ht[i];
+      if (Ni == 0) continue;
+      Bvh4Buffers& q = b4[i];
+      q.nTris = Ni;
+      q.params = b.params + i;
+      q.lr = b.lr + hNode[i];
+      q.runStarts = b.runStarts + hLeaf[i];
+      q.parent = parent + hNode[i];
+      q.tris = b.tris + ht[i];
+      q.mergeMode = s->bvh4Merge;
+      q.scratch = (char*)scratch4 + scrOff[i];
+      q.hostNodeCount = hostCounts + i;
+      cudaError_t pe = bvh4_plan(q, ctx->numSMs, st);
+      if (pe != cudaSuccess)
+      {
+        cudaFreeHost(hostCounts);
+        return cuda_fail(ctx, pe, "bvh4_plan");
+      }
+    }
+    cudaError_t se = cudaStreamSynchronize(st);
+    size_t total = 0;
+    for (uint32_t i = 0; i < G; i++)
+    {
+      count4[i] = (ht[i + 1] > ht[i]) ? (hostCounts[i] ? hostCounts[i] : 1u) : 0u;
+      node4Off[i] = total;
+      total += count4[i];
+    }
+    cudaFreeHost(hostCounts);
+    if (se != cudaSuccess) return cuda_fail(ctx, se, "bvh4_plan sync");
+    HRT_CUDA(ctx, balloc((char**)&nodes4, nodeBytes * (total ? total : 1), owned));
+    for (uint32_t i = 0; i < G; i++)
+      if (count4[i])
+        HRT_CUDA(ctx, bvh4_emit(b4[i], s->layout - 1, (char*)nodes4 + nodeBytes * node4Off[i], count4[i],
+                                ctx->numSMs, st));
+  }
+  HRT_CUDA(ctx, cudaEventRecord(e1, st));
+  if (nodes4) HRT_CUDA(ctx, cudaMemcpyAsync(hp.data(), b.params, sizeof(BuildParams) * G, cudaMemcpyDeviceToHost, st));
+  HRT_CUDA(ctx, cudaFreeAsync(dIdx, st));
+  HRT_CUDA(ctx, cudaFreeAsync(keysAlt, st));
+  HRT_CUDA(ctx, cudaFreeAsync(valsAlt, st));
+  HRT_CUDA(ctx, cudaFreeAsync(parent, st));
+  HRT_CUDA(ctx, cudaFreeAsync(visit, st));
+  HRT_CUDA(ctx, cudaFreeAsync(scratch, st));
+  HRT_CUDA(ctx, cudaFreeAsync(dVOff, st));
+  HRT_CUDA(ctx, cudaFreeAsync(dTOff, st));
+  if (scratch4) HRT_CUDA(ctx, cudaFreeAsync(scratch4, st));
+  HRT_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (uint32_t i = 0; i < G; i++) err |= hp[i].error;
+  if (err & kErrIndexRange) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "triangle index >= vertex count of its geometry");
+  if (err & kErrLeafCount)
+    return fail(ctx, HRT_ERR_CAPACITY, "more than 127 triangles share one Morton code (leaf count field overflows)");
+  if (err & kErrWaitTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "device look-back wait timed out during the build");
+  if (err & kErrLayout) return fail(ctx, HRT_ERR_DEVICE_CHECK, "inconsistent tree or node encoding");
+
+  out.resize(G);
+  for (uint32_t i = 0; i < G; i++)
+  {
+    Geom& g = out[i];
+    const uint32_t Ni = ht[i + 1] - ht[i];
+    const uint32_t Li = hLeaf[i + 1] - hLeaf[i];
+    g.shared = true;
+    g.nTris = Ni;
+    g.nVerts = hv[i + 1] - hv[i];
+    g.nLeaves = Li;
+    g.verts = verts + hv[i];
+    g.keys = b.keys + ht[i];
+    g.vals = b.vals + ht[i];
+    g.keysUnsorted = b.keysUnsorted + ht[i];
+    g.compressed = b.compressed + hLeaf[i];
+    g.runStarts = b.runStarts + hLeaf[i];
+    g.lr = b.lr + hNode[i];
+    g.lrCount = b.lrCount + hNode[i];
+    g.recs = b.recs + hRec[i];
+    g.tris = b.tris + ht[i];
+    g.sortedIdx = b.sortedIdx + 3 * (size_t)ht[i];
+    g.params = b.params + i;
+    g.host = hp[i];
+    g.buildMs = ms;  // the whole batch's build time
+    if (nodes4 && count4[i])
+    {
+      g.nodes4 = (char*)nodes4 + nodeBytes * node4Off[i];
+      g.nNodes4 = count4[i];
+    }
+    const uint64_t recsI = Li > 1 ? Li - 1 : (Li ? 1 : 0);
+    g.bytes = 16ull * g.nVerts + (uint64_t)Ni * (4 * 5 + sizeof(TriRec) + 12) + (Li ? (2ull * Li - 1) * 36 : 0) +
+              recsI * sizeof(PairRec) + (uint64_t)g.nNodes4 * nodeBytes + sizeof(BuildParams);
+    if (Ni == 0)
+      for (int c = 0; c < 4; c++)
+      {
+        g.box[c] = INFINITY;
+        g.box[4 + c] = -INFINITY;
+      }
+    else
+    {
+      if (Li == 0 || Li > Ni) return fail(ctx, HRT_ERR_DEVICE_CHECK, "leaf count out of range");
+      for (int c = 0; c < 4; c++)
+      {
+        g.box[c] = hp[i].bmin[c];
+        g.box[4 + c] = hp[i].bmax[c];
+      }
+    }
+  }
+  return HRT_OK;
+}
+
 bool lbvh_builder_name(const char* name)
 {
   if (!name || !*name) return true;
@@ -349,11 +593,25 @@ int ensure_stage(hrt_scene* s, uint64_t n)
   return HRT_OK;
 }
 
-int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out, int counting, cudaStream_t st)
+// Segments of a segmented query (all null/0 for a plain query) and, when not
+// null, the work counter the launch uses instead of a slot of the scene's ring.
+struct QuerySegments
+{
+  const uint32_t* rayOffsets = nullptr;
+  const uint32_t* segInst = nullptr;
+  uint32_t        nSeg = 0;
+  unsigned int*   counter = nullptr;
+};
+
+int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out, int counting, cudaStream_t st,
+                 const QuerySegments& q = QuerySegments())
 {
   if (!s->committed) return fail(s->ctx, HRT_ERR_STATE, "query before hrt_commit_scene");
   if (n == 0) return HRT_OK;
   if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
+  if (n > 0xFFFFFFFFull) return fail(s->ctx, HRT_ERR_CAPACITY, "more than 2^32-1 rays in one query");
+  if (q.rayOffsets && (!q.segInst || q.nSeg == 0))
+    return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "segmented query without segments");
   TraceArgs a;
   a.rays = reinterpret_cast<const float4*>(rays);
   a.n = n;
@@ -362,7 +620,10 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
   a.hits = out;
   a.counters = s->dCounters;
   a.errorWord = s->dError;
-  a.rayCounter = s->dRayCounters + (s->counterSlot.fetch_add(1) % kCounterSlots);
+  a.rayCounter = q.counter ? q.counter : s->dRayCounters + (s->counterSlot.fetch_add(1) % kCounterSlots);
+  a.rayOffsets = q.rayOffsets;
+  a.segInst = q.segInst;
+  a.nSeg = q.nSeg;
   cudaError_t e = trace(a, kind, counting, s->layout, s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
@@ -456,6 +717,8 @@ int hrt_clear_geom(hrt_scene* s)
   cudaSetDevice(s->ctx->device);
   cudaStreamSynchronize(s->ctx->stream);
   for (Geom& gm : s->geoms) free_geom(gm);
+  for (void* p : s->batchAllocs) cudaFree(p);
+  s->batchAllocs.clear();
   s->geoms.clear();
   s->insts.clear();
   s->committed = false;
@@ -501,6 +764,51 @@ int hrt_add_geom_triangles3f(hrt_scene* s, const float* vpos, uint64_t nVert, co
   s->geoms.push_back(g);
   s->committed = false;
   if (geomId) *geomId = (uint32_t)(s->geoms.size() - 1);
+  return HRT_OK;
+}
+
+int hrt_add_geoms_triangles3f_batched(hrt_scene* s, uint32_t count, const float* vpos, const uint64_t* vertOffsets,
+                                      const uint32_t* idx, const uint64_t* idxOffsets, int quality,
+                                      uint64_t vByteStride, uint32_t* firstGeomId)
+{
+  (void)quality;
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  hrt_context* ctx = s->ctx;
+  if (count == 0) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "empty batch");
+  if (!vertOffsets || !idxOffsets) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "null offset array");
+  if (vByteStride == 0) vByteStride = 12;
+  if (vByteStride < 12 || vByteStride % 4 != 0)
+    return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "vByteStride must be >= 12 and a multiple of 4");
+  if (vertOffsets[0] != 0 || idxOffsets[0] != 0) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "offsets must start at 0");
+  for (uint32_t i = 0; i < count; i++)
+  {
+    if (vertOffsets[i + 1] < vertOffsets[i] || idxOffsets[i + 1] < idxOffsets[i])
+      return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "offsets must be ascending");
+    if ((idxOffsets[i + 1] - idxOffsets[i]) % 3 != 0)
+      return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "a geometry's index count is not a multiple of 3");
+    if ((idxOffsets[i + 1] - idxOffsets[i]) / 3 > HRT_MAX_TRIS_PER_GEOM)
+      return fail(ctx, HRT_ERR_CAPACITY, "more than 2^24-1 triangles in one geometry");
+  }
+  const uint64_t V = vertOffsets[count], nIdx = idxOffsets[count];
+  if ((V && !vpos) || (nIdx && !idx)) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "null vertex or index pointer");
+  if (nIdx / 3 > HRT_MAX_TRIS_PER_BATCH) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^30-1 triangles in one batch");
+  if (V > 0xFFFFFFFFull) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^32-1 vertices in one batch");
+  std::lock_guard<std::mutex> lk(s->mu);
+  cudaSetDevice(ctx->device);
+  std::vector<Geom> built;
+  std::vector<void*> owned;
+  const int st = build_batch(s, count, vpos, vertOffsets, idx, idxOffsets, vByteStride, built, owned);
+  if (st != HRT_OK)
+  {
+    cudaStreamSynchronize(ctx->stream);
+    for (void* p : owned) cudaFree(p);
+    return st;
+  }
+  const uint32_t first = (uint32_t)s->geoms.size();
+  for (Geom& g : built) s->geoms.push_back(g);
+  for (void* p : owned) s->batchAllocs.push_back(p);
+  s->committed = false;
+  if (firstGeomId) *firstGeomId = first;
   return HRT_OK;
 }
 
@@ -821,6 +1129,177 @@ int hrt_scene_get_trace_config(const hrt_scene* s, int kind, hrt_trace_config* c
   c->persistent = s->cfg[kind].persistent;
   c->stepsPerRefill = s->cfg[kind].stepsPerRefill;
   c->refillLanes = s->cfg[kind].refillLanes;
+  return HRT_OK;
+}
+
+int hrt_query_multi(hrt_scene* s, const hrt_query_desc* q, void* stream)
+{
+  if (!s || !q || (q->kind != 0 && q->kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
+  QuerySegments sg;
+  sg.rayOffsets = q->rayOffsets;
+  sg.segInst = q->segInst;
+  sg.nSeg = q->nSeg;
+  return launch_query(s, q->kind, q->rays, q->n, q->out, 0, (cudaStream_t)stream, sg);
+}
+
+}  // extern "C"
+
+struct hrt_graph
+{
+  hrt_scene*      scene = nullptr;
+  cudaGraph_t     graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned int*   counters = nullptr;  // one work counter per captured query
+};
+
+extern "C" {
+
+int hrt_graph_create(hrt_scene* s, const hrt_query_desc* queries, uint32_t count, hrt_graph** out)
+{
+  if (!s || !out || (count && !queries)) return HRT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  hrt_context* ctx = s->ctx;
+  if (count == 0) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "a graph needs at least one query");
+  for (uint32_t i = 0; i < count; i++)
+    if (queries[i].kind != 0 && queries[i].kind != 1) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "unknown query kind");
+  if (!s->committed) return fail(ctx, HRT_ERR_STATE, "graph capture before hrt_commit_scene");
+  cudaSetDevice(ctx->device);
+  hrt_graph* g = new hrt_graph();
+  g->scene = s;
+  cudaStream_t cs = nullptr;
+  auto cleanup = [&](int status) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->counters) cudaFree(g->counters);
+    if (cs) cudaStreamDestroy(cs);
+    delete g;
+    return status;
+  };
+  cudaError_t e = cudaMalloc((void**)&g->counters, sizeof(unsigned int) * count);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "graph counters"));
+  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "capture stream"));
+  // the relaxed mode lets the launcher query occupancy while capturing
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaStreamBeginCapture"));
+  int st = HRT_OK;
+  for (uint32_t i = 0; i < count && st == HRT_OK; i++)
+  {
+    QuerySegments sg;
+    sg.rayOffsets = queries[i].rayOffsets;
+    sg.segInst = queries[i].segInst;
+    sg.nSeg = queries[i].nSeg;
+    sg.counter = g->counters + i;
+    st = launch_query(s, queries[i].kind, queries[i].rays, queries[i].n, queries[i].out, 0, cs, sg);
+  }
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(cs, &graph);
+  g->graph = graph;
+  if (st != HRT_OK) return cleanup(st);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaStreamEndCapture"));
+  e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaGraphInstantiate"));
+  cudaStreamDestroy(cs);
+  *out = g;
+  return HRT_OK;
+}
+
+int hrt_graph_launch(hrt_graph* g, void* stream)
+{
+  if (!g) return HRT_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(g->scene->ctx, e, "cudaGraphLaunch");
+  return HRT_OK;
+}
+
+int hrt_graph_destroy(hrt_graph* g)
+{
+  if (!g) return HRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(g->scene->ctx->device);
+  cudaDeviceSynchronize();
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->counters) cudaFree(g->counters);
+  delete g;
+  return HRT_OK;
+}
+
+int hrt_scene_autotune(hrt_scene* s, const hrt_query_desc* q, int repeats, hrt_trace_config* best, float* bestMs)
+{
+  if (!s || !q || (q->kind != 0 && q->kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
+  hrt_context* ctx = s->ctx;
+  if (repeats < 1 || repeats > 1000) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "repeats out of range");
+  cudaSetDevice(ctx->device);
+  std::vector<TraceConfig> grid;
+  for (int tpb : {64, 128, 256})
+  {
+    TraceConfig c;
+    c.threadsPerBlock = tpb;
+    c.persistent = 0;
+    grid.push_back(c);
+    for (int steps : {4, 8, 16, 32, 64})
+      for (int lanes : {8, 16, 24, 28, 32})
+      {
+        c.persistent = 1;
+        c.stepsPerRefill = steps;
+        c.refillLanes = lanes;
+        grid.push_back(c);
+      }
+  }
+  const TraceConfig saved = s->cfg[q->kind];
+  cudaStream_t cs = ctx->stream;
+  cudaEvent_t e0, e1;
+  HRT_CUDA(ctx, cudaEventCreate(&e0));
+  HRT_CUDA(ctx, cudaEventCreate(&e1));
+  QuerySegments sg;
+  sg.rayOffsets = q->rayOffsets;
+  sg.segInst = q->segInst;
+  sg.nSeg = q->nSeg;
+  float bestT = INFINITY;
+  TraceConfig bestC = saved;
+  int st = HRT_OK;
+  for (const TraceConfig& c : grid)
+  {
+    s->cfg[q->kind] = c;
+    st = launch_query(s, q->kind, q->rays, q->n, q->out, 0, cs, sg);  // warm-up
+    if (st != HRT_OK) break;
+    cudaEventRecord(e0, cs);
+    for (int r = 0; r < repeats && st == HRT_OK; r++) st = launch_query(s, q->kind, q->rays, q->n, q->out, 0, cs, sg);
+    cudaEventRecord(e1, cs);
+    if (st != HRT_OK) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess)
+    {
+      st = cuda_fail(ctx, cudaGetLastError(), "autotune timing");
+      break;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)repeats;
+    if (ms < bestT)
+    {
+      bestT = ms;
+      bestC = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->cfg[q->kind] = (st == HRT_OK) ? bestC : saved;
+  if (st != HRT_OK) return st;
+  uint32_t err = 0;
+  HRT_CUDA(ctx, cudaMemcpy(&err, s->dError, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err)
+  {
+    cudaMemset(s->dError, 0, 8 * sizeof(uint32_t));
+    return fail(ctx, HRT_ERR_DEVICE_CHECK, "device-side check failed during autotuning");
+  }
+  if (best)
+  {
+    best->threadsPerBlock = bestC.threadsPerBlock;
+    best->persistent = bestC.persistent;
+    best->stepsPerRefill = bestC.stepsPerRefill;
+    best->refillLanes = bestC.refillLanes;
+  }
+  if (bestMs) *bestMs = bestT;
   return HRT_OK;
 }
 

@@ -18,6 +18,13 @@ constexpr uint32_t kTileSize = 4096;  // pairs per onesweep tile
 size_t radix_sort_scratch_bytes(uint32_t n);
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, uint32_t* valsAlt, uint32_t n,
                              void* scratch, uint32_t* errorWord, int numSMs, cudaStream_t stream);
+// Stable sort by (segment, key) where the segment of a pair is the segment of
+// its value in segOffsets[0..segCount] (device, ascending, offsets[0] = 0):
+// each segment ends up sorted by key in place of its input range.
+size_t radix_sort_segmented_scratch_bytes(uint32_t n, uint32_t segCount);
+cudaError_t radix_sort_pairs_segmented(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, uint32_t* valsAlt,
+                                       uint32_t n, const uint32_t* segOffsets, uint32_t segCount, void* scratch,
+                                       uint32_t* errorWord, int numSMs, cudaStream_t stream);
 
 // ---------------------------------------------------------------- build.cu
 struct BuildBuffers
@@ -49,6 +56,49 @@ size_t build_scratch_bytes(uint32_t nTris);
 // Runs the whole LBVH build asynchronously on `stream`.  Errors found on the
 // device are ORed into params->error.
 cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t stream);
+
+// ---------------------------------------------------------------- build_batch.cu
+// G geometries built together.  Geometry s owns vertices
+// [vertOffsets[s], vertOffsets[s+1]) and triangles [triOffsets[s],
+// triOffsets[s+1]) of the concatenated inputs (indices local to its vertices).
+// Its results sit at its own offsets: triangle arrays at triOffsets[s], runs at
+// leafOffsets[s], LR nodes / parents at nodeOffsets[s], refit counters at
+// intOffsets[s], records at recOffsets[s]; all offsets (G+1 entries) and the
+// totals in counts ([0] runs, [1] internal nodes, [2] LR nodes, [3] records)
+// are computed on the device.
+struct BatchBuffers
+{
+  const float4*   verts;        // total vertices, w = 1
+  const uint32_t* idx;          // 3 * nTris, local to each geometry
+  const uint32_t* vertOffsets;  // G+1 (device)
+  const uint32_t* triOffsets;   // G+1 (device)
+  uint32_t        G;
+  uint32_t        nTris;        // triOffsets[G]
+  uint32_t*  keys;              // nTris
+  uint32_t*  vals;              // nTris: global triangle ids in sorted order
+  uint32_t*  keysAlt;           // nTris
+  uint32_t*  valsAlt;           // nTris
+  uint32_t*  keysUnsorted;      // nTris
+  uint32_t*  compressed;        // nTris
+  uint32_t*  runStarts;         // nTris: global positions
+  BVHNode32* lr;                // 2*nTris
+  uint32_t*  lrCount;           // 2*nTris
+  uint32_t*  parent;            // 2*nTris
+  uint32_t*  visit;             // nTris
+  PairRec*   recs;              // nTris
+  TriRec*    tris;              // nTris; e1.w = triangle id local to the geometry
+  uint32_t*  sortedIdx;         // 3*nTris, local vertex ids
+  BuildParams* params;          // G: box, scale, nLeaves per geometry
+  uint32_t*  leafOffsets;       // G+1
+  uint32_t*  intOffsets;        // G+1
+  uint32_t*  nodeOffsets;       // G+1
+  uint32_t*  recOffsets;        // G+1
+  uint32_t*  counts;            // 4
+  uint32_t*  errorWord;         // device word shared by the batch
+  void*      scratch;           // build_batch_scratch_bytes(nTris, G)
+};
+size_t build_batch_scratch_bytes(uint32_t nTris, uint32_t G);
+cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t stream);
 
 // ---------------------------------------------------------------- bvh4.cu
 // Collapse of a finished LBVH (LR tree, parents, run starts) into 4-wide nodes.
@@ -97,6 +147,11 @@ struct TraceArgs
   unsigned long long* counters;    // optional [2]: node pairs, triangle tests
   uint32_t*           errorWord;   // device
   unsigned int*       rayCounter;  // device, work counter of the persistent pool
+  // segmented query (optional): rays [rayOffsets[k], rayOffsets[k+1]) are
+  // traced against instance segInst[k] only; device arrays of nSeg+1 / nSeg
+  const uint32_t*     rayOffsets = nullptr;
+  const uint32_t*     segInst = nullptr;
+  uint32_t            nSeg = 0;
 };
 
 // Launch shape of the traversal (tuned per workload).

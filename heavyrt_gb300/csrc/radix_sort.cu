@@ -13,6 +13,12 @@
 // Tiles are numbered in the order blocks start (atomic ticket), so every tile
 // a block waits on belongs to a block that is already resident; each wait is
 // still bounded and reports kErrWaitTimeout instead of spinning forever.
+//
+// The segmented variant sorts many geometries' pairs in one go: after the four
+// code passes, one more stable pass per byte of the segment index (the digit
+// of an element is looked up from its triangle id) makes the order
+// segment-major while keeping each segment's code order and ties.
+#include "build_common.cuh"
 #include "hrt_kernels.cuh"
 
 namespace hrt
@@ -42,6 +48,29 @@ __device__ __forceinline__ uint32_t load_relaxed(const uint32_t* p)
   uint32_t v;
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+
+// Digit of an element for one pass: a byte of the key, or - for the segment
+// passes of the segmented sort - a byte of the index of the segment that holds
+// the element's value (ascending offsets[0..segCount]; value = global
+// triangle index).
+__device__ __forceinline__ uint32_t pass_digit(uint32_t key, uint32_t val, uint32_t shift,
+                                               const uint32_t* __restrict__ segOffsets, uint32_t segCount)
+{
+  if (segOffsets == nullptr) return (key >> shift) & 0xFFu;
+  return (bc::find_segment(segOffsets, segCount, val) >> shift) & 0xFFu;
+}
+
+// Histogram of one byte of the segment index over all elements: each segment
+// adds its element count to the bin of its byte.
+__global__ void k_segment_histogram(const uint32_t* __restrict__ segOffsets, uint32_t segCount, uint32_t shift,
+                                    uint32_t* __restrict__ hist)
+{
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < segCount; s += gridDim.x * blockDim.x)
+  {
+    const uint32_t c = segOffsets[s + 1] - segOffsets[s];
+    if (c) atomicAdd(&hist[(s >> shift) & 0xFFu], c);
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) k_histogram(const uint32_t* __restrict__ keys, uint32_t n,
@@ -95,10 +124,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
   return r;
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_histograms(uint32_t* __restrict__ hist)
+__global__ void __launch_bounds__(kThreads) k_scan_histograms(uint32_t* __restrict__ hist, int nHist)
 {
   __shared__ uint32_t warpSums[kWarps + 1];
-  for (int p = 0; p < kPasses; p++)
+  for (int p = 0; p < nHist; p++)
   {
     uint32_t total;
     const uint32_t v = hist[p * kRadix + threadIdx.x];
@@ -111,7 +140,8 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
                                                        const uint32_t* __restrict__ valsIn,
                                                        uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
                                                        uint32_t n, uint32_t shift, const uint32_t* __restrict__ digitBase,
-                                                       uint32_t* tileStatus, uint32_t* tileCounter, uint32_t* errorWord)
+                                                       uint32_t* tileStatus, uint32_t* tileCounter, uint32_t* errorWord,
+                                                       const uint32_t* __restrict__ segOffsets, uint32_t segCount)
 {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_warpHist[kWarps][kRadix];  // counts, then per-warp exclusive offsets
@@ -145,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   for (int k = 0; k < kItems; k++)
   {
     const bool valid = (warpBase + k * 32 + lane) < n;
-    const uint32_t digit = (key[k] >> shift) & 0xFF;
+    const uint32_t digit = valid ? pass_digit(key[k], val[k], shift, segOffsets, segCount) : 0xFFu;
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? digit : (0x100u + lane));
     const uint32_t before = s_warpHist[warp][digit];
     rank[k] = before + __popc(peers & ltMask);
@@ -203,7 +233,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   {
     if ((warpBase + k * 32 + lane) < n)
     {
-      const uint32_t digit = (key[k] >> shift) & 0xFF;
+      const uint32_t digit = pass_digit(key[k], val[k], shift, segOffsets, segCount);
       const uint32_t pos = s_digitStart[digit] + s_warpHist[warp][digit] + rank[k];
       s_keys[pos] = key[k];
       s_vals[pos] = val[k];
@@ -215,7 +245,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   for (uint32_t i = tid; i < count; i += kThreads)
   {
     const uint32_t k = s_keys[i];
-    const uint32_t dst = s_dst[(k >> shift) & 0xFF] + i;
+    const uint32_t dst = s_dst[pass_digit(k, s_vals[i], shift, segOffsets, segCount)] + i;
     if (dst < n)  // always true unless a look-back wait gave up (reported through errorWord)
     {
       keysOut[dst] = k;
@@ -246,7 +276,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, 
   const uint32_t maxHb = (uint32_t)numSMs * 4u;
   if (hb > maxHb) hb = maxHb;
   k_histogram<<<hb, kThreads, 0, stream>>>(keys, n, hist);
-  k_scan_histograms<<<1, kThreads, 0, stream>>>(hist);
+  k_scan_histograms<<<1, kThreads, 0, stream>>>(hist, kPasses);
   uint32_t* srcK = keys;
   uint32_t* srcV = vals;
   uint32_t* dstK = keysAlt;
@@ -254,11 +284,72 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, 
   for (int p = 0; p < kPasses; p++)
   {
     k_onesweep<<<tiles, kThreads, 0, stream>>>(srcK, srcV, dstK, dstV, n, 8u * p, hist + p * kRadix,
-                                               status + (size_t)p * tiles * kRadix, counters + p, errorWord);
+                                               status + (size_t)p * tiles * kRadix, counters + p, errorWord, nullptr, 0u);
     uint32_t* t = srcK; srcK = dstK; dstK = t;
     t = srcV; srcV = dstV; dstV = t;
   }
   return cudaGetLastError();  // four passes: the result is back in keys/vals
+}
+
+// Number of segment-index bytes the segmented sort passes over.
+static int segment_passes(uint32_t segCount)
+{
+  int p = 1;
+  while (p < 4 && (segCount - 1u) >> (8 * p)) p++;
+  return p;
+}
+
+size_t radix_sort_segmented_scratch_bytes(uint32_t n, uint32_t segCount)
+{
+  const size_t tiles = (n + kTile - 1) / kTile;
+  const size_t passes = kPasses + segment_passes(segCount);
+  return sizeof(uint32_t) * (passes * kRadix + passes + 4 + passes * tiles * kRadix);
+}
+
+cudaError_t radix_sort_pairs_segmented(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, uint32_t* valsAlt,
+                                       uint32_t n, const uint32_t* segOffsets, uint32_t segCount, void* scratch,
+                                       uint32_t* errorWord, int numSMs, cudaStream_t stream)
+{
+  if (n <= 1) return cudaSuccess;
+  const int segPasses = segment_passes(segCount);
+  const int passes = kPasses + segPasses;
+  const uint32_t tiles = (n + kTile - 1) / kTile;
+  uint32_t* hist = (uint32_t*)scratch;
+  uint32_t* counters = hist + passes * kRadix;
+  uint32_t* status = counters + passes + 4;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, radix_sort_segmented_scratch_bytes(n, segCount), stream);
+  if (e != cudaSuccess) return e;
+  uint32_t hb = (n + kThreads - 1) / kThreads;
+  const uint32_t maxHb = (uint32_t)numSMs * 4u;
+  if (hb > maxHb) hb = maxHb;
+  k_histogram<<<hb, kThreads, 0, stream>>>(keys, n, hist);
+  for (int q = 0; q < segPasses; q++)
+    k_segment_histogram<<<(segCount + 255) / 256, 256, 0, stream>>>(segOffsets, segCount, 8u * q,
+                                                                     hist + (kPasses + q) * kRadix);
+  k_scan_histograms<<<1, kThreads, 0, stream>>>(hist, passes);
+  uint32_t* srcK = keys;
+  uint32_t* srcV = vals;
+  uint32_t* dstK = keysAlt;
+  uint32_t* dstV = valsAlt;
+  // code bytes first (least significant), then the segment index bytes: a
+  // stable LSD sort by (segment, code) keeps the input order among ties
+  for (int p = 0; p < passes; p++)
+  {
+    const bool seg = p >= kPasses;
+    k_onesweep<<<tiles, kThreads, 0, stream>>>(srcK, srcV, dstK, dstV, n, seg ? 8u * (p - kPasses) : 8u * p,
+                                               hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p,
+                                               errorWord, seg ? segOffsets : nullptr, segCount);
+    uint32_t* t = srcK; srcK = dstK; dstK = t;
+    t = srcV; srcV = dstV; dstV = t;
+  }
+  if (srcK != keys)
+  {
+    e = cudaMemcpyAsync(keys, srcK, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(vals, srcV, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace hrt

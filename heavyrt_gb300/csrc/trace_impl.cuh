@@ -245,6 +245,7 @@ struct Lane
   float4   po, di;    // the ray as given (world space)
   uint32_t ray;       // ray index or kNoRay
   uint32_t inst;      // current instance
+  uint32_t instEnd;   // one past the last instance this ray is traced against
   uint32_t cur;       // current record / leaf reference
   int      top;       // stack depth
   uint32_t budget;    // steps left for this ray
@@ -271,11 +272,11 @@ __device__ __forceinline__ bool out_of_budget(Lane& L, uint32_t* errorWord)
 }
 
 // Advances the lane's instance cursor to the next instance with triangles,
-// starting at `from`; prepares the ray for it.  Returns false when none is left.
-__device__ __forceinline__ bool begin_instance(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t nInst,
-                                               uint32_t from)
+// starting at `from` and ending before L.instEnd; prepares the ray for it.
+// Returns false when none is left.
+__device__ __forceinline__ bool begin_instance(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t from)
 {
-  for (uint32_t k = from; k < nInst; k++)
+  for (uint32_t k = from; k < L.instEnd; k++)
     if (inst[k].valid)
     {
       L.inst = k;
@@ -376,8 +377,7 @@ __device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32
 // One traversal step (an internal node, or a leaf followed by a pop).
 // Returns true when the lane's ray is finished.
 template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
-__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t nInst,
-                                     uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
+__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
                                      uint32_t* errorWord)
 {
   const InstanceDesc& d = inst[L.inst];
@@ -398,7 +398,7 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
   if (pop)
   {
     L.top--;
-    if (L.top < 0) return !begin_instance(L, inst, nInst, L.inst + 1);
+    if (L.top < 0) return !begin_instance(L, inst, L.inst + 1);
     L.cur = stack[L.top * THREADS];
   }
   return false;
@@ -415,6 +415,37 @@ __device__ __forceinline__ void write_result(const Lane& L, void* out)
     o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(L.h.inst), __uint_as_float(L.h.geom));
     o[1] = make_float4(L.h.u, L.h.v, 0.0f, 0.0f);
   }
+}
+
+// Instances a ray is traced against: all of them, or - for a segmented query -
+// the one instance of the ray's segment (rayOffsets[0..nSeg] ascending, ray i
+// in segment k when rayOffsets[k] <= i < rayOffsets[k+1]); an instance id out
+// of range leaves the ray a miss.
+struct Segments
+{
+  const uint32_t* rayOffsets;  // nullptr: no segments
+  const uint32_t* segInst;
+  uint32_t        nSeg;
+  uint32_t        nInst;
+};
+
+__device__ __forceinline__ uint32_t first_instance(Lane& L, uint32_t i, const Segments& sg)
+{
+  if (sg.rayOffsets == nullptr)
+  {
+    L.instEnd = sg.nInst;
+    return 0;
+  }
+  uint32_t lo = 0, hi = sg.nSeg;
+  while (hi - lo > 1)
+  {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(sg.rayOffsets + mid) <= i) lo = mid;
+    else hi = mid;
+  }
+  const uint32_t k = __ldg(sg.segInst + lo);
+  L.instEnd = k < sg.nInst ? k + 1 : 0;
+  return k;
 }
 
 __device__ __forceinline__ void start_ray(Lane& L, uint32_t i, const float4* __restrict__ rays)
@@ -449,7 +480,7 @@ __device__ __forceinline__ void flush_counters(uint64_t nPairs, uint64_t nTris, 
 // warp refills when at least `refill` lanes are idle (or all are).
 template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict__ rays, uint32_t n,
-                                                        const InstanceDesc* __restrict__ inst, uint32_t nInst, void* out,
+                                                        const InstanceDesc* __restrict__ inst, Segments sg, void* out,
                                                         unsigned long long* counters, uint32_t* errorWord,
                                                         unsigned int* rayCounter, int steps, int refill)
 {
@@ -477,7 +508,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
         if (i < n)
         {
           start_ray(L, i, rays);
-          if (!begin_instance(L, inst, nInst, 0))
+          if (!begin_instance(L, inst, first_instance(L, i, sg)))
           {
             write_result<ANY>(L, out);
             L.ray = kNoRay;
@@ -490,7 +521,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
       for (int s = 0; s < steps; s++)
       {
         if (out_of_budget(L, errorWord) ||
-            step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord))
+            step<LAYOUT, ANY, COUNT, THREADS>(L, inst, stack, nPairs, nTris, errorWord))
         {
           write_result<ANY>(L, out);
           L.ray = kNoRay;
@@ -505,7 +536,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
 // One thread per ray.
 template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict__ rays, uint32_t n,
-                                                        const InstanceDesc* __restrict__ inst, uint32_t nInst, void* out,
+                                                        const InstanceDesc* __restrict__ inst, Segments sg, void* out,
                                                         unsigned long long* counters, uint32_t* errorWord)
 {
   __shared__ uint32_t s_stack[StackDepth<LAYOUT>::value * THREADS];
@@ -516,9 +547,9 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
   {
     Lane L;
     start_ray(L, i, rays);
-    if (begin_instance(L, inst, nInst, 0))
+    if (begin_instance(L, inst, first_instance(L, i, sg)))
       while (!out_of_budget(L, errorWord) &&
-             !step<LAYOUT, ANY, COUNT, THREADS>(L, inst, nInst, stack, nPairs, nTris, errorWord)) {}
+             !step<LAYOUT, ANY, COUNT, THREADS>(L, inst, stack, nPairs, nTris, errorWord)) {}
     write_result<ANY>(L, out);
   }
   flush_counters<COUNT>(nPairs, nTris, counters);
@@ -528,6 +559,7 @@ template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
 cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   const uint32_t n = (uint32_t)a.n;
+  const Segments sg{a.rayOffsets, a.segInst, a.nSeg, a.nInst};
   if (c.persistent && !COUNT)
   {
     int perSM = 0;
@@ -541,12 +573,12 @@ cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStr
     e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
     k_trace_pool<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(
-        a.rays, n, a.inst, a.nInst, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes);
+        a.rays, n, a.inst, sg, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes);
   }
   else
   {
     const uint64_t blocks = ((uint64_t)n + THREADS - 1) / THREADS;
-    k_trace_grid<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(a.rays, n, a.inst, a.nInst, a.hits,
+    k_trace_grid<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(a.rays, n, a.inst, sg, a.hits,
                                                                                  a.counters, a.errorWord);
   }
   return cudaGetLastError();

@@ -76,6 +76,19 @@ class TraceConfig(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class QueryDesc(C.Structure):
+    """hrt_query_desc (include/hrt.h): one traversal launch, optionally segmented."""
+
+    _fields_ = [("kind", C.c_int), ("rays", C.c_void_p), ("n", C.c_uint64), ("rayOffsets", C.c_void_p),
+                ("segInst", C.c_void_p), ("nSeg", C.c_uint32), ("out", C.c_void_p)]
+
+
+def query_desc(kind: int, rays_ptr: int, n: int, out_ptr: int, ray_offsets_ptr: int = 0, seg_inst_ptr: int = 0,
+               n_seg: int = 0) -> QueryDesc:
+    return QueryDesc(int(kind), C.c_void_p(rays_ptr), int(n), C.c_void_p(ray_offsets_ptr or None),
+                     C.c_void_p(seg_inst_ptr or None), int(n_seg), C.c_void_p(out_ptr))
+
+
 class HrtError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"hrt status {status}: {message}")
@@ -131,6 +144,12 @@ def lib() -> C.CDLL:
         "hrt_scene_get_layout": (i32, [vp, C.POINTER(i32)]),
         "hrt_scene_set_trace_config": (i32, [vp, i32, C.POINTER(TraceConfig)]),
         "hrt_scene_get_trace_config": (i32, [vp, i32, C.POINTER(TraceConfig)]),
+        "hrt_add_geoms_triangles3f_batched": (i32, [vp, u32, vp, vp, vp, vp, i32, u64, C.POINTER(u32)]),
+        "hrt_query_multi": (i32, [vp, C.POINTER(QueryDesc), vp]),
+        "hrt_graph_create": (i32, [vp, C.POINTER(QueryDesc), u32, C.POINTER(vp)]),
+        "hrt_graph_launch": (i32, [vp, vp]),
+        "hrt_graph_destroy": (i32, [vp]),
+        "hrt_scene_autotune": (i32, [vp, C.POINTER(QueryDesc), i32, C.POINTER(TraceConfig), C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -304,6 +323,50 @@ class SceneRT:
         return out
 
     # ---- engine extensions ----------------------------------------------
+    def add_geoms_batched(self, verts_list, idx_list, a_qualityLevel=BUILD_HIGH) -> list:
+        """Builds many geometries with one segmented build; returns their ids.
+
+        verts_list[i]: float32 [V_i, 3] or [V_i, 4] (xyz used); idx_list[i]: uint32 indices local to
+        verts_list[i]."""
+        if len(verts_list) != len(idx_list) or not verts_list:
+            raise ValueError("verts_list and idx_list must be non-empty and of equal length")
+        vs = []
+        for v in verts_list:
+            a = np.asarray(v, dtype=np.float32)
+            a = a.reshape(len(a), -1) if a.size else np.zeros((0, 3), np.float32)
+            p4 = np.ones((len(a), 4), np.float32)
+            p4[:, :3] = a[:, :3]
+            vs.append(p4)
+        v = np.ascontiguousarray(np.concatenate(vs, axis=0))
+        ids = [np.asarray(i, dtype=np.uint32).reshape(-1) for i in idx_list]
+        idx = np.ascontiguousarray(np.concatenate(ids))
+        voff = np.zeros(len(vs) + 1, dtype=np.uint64)
+        voff[1:] = np.cumsum([len(x) for x in vs])
+        ioff = np.zeros(len(ids) + 1, dtype=np.uint64)
+        ioff[1:] = np.cumsum([len(x) for x in ids])
+        first = C.c_uint32()
+        self.ctx.check(lib().hrt_add_geoms_triangles3f_batched(self._h, len(vs), _ptr(v), _ptr(voff), _ptr(idx),
+                                                               _ptr(ioff), int(a_qualityLevel), 16, C.byref(first)),
+                       "add_geoms_batched")
+        return list(range(first.value, first.value + len(vs)))
+
+    def query_multi(self, desc: QueryDesc, stream: int = 0):
+        """Asynchronous (optionally segmented) query on device arrays (hrt_query_multi)."""
+        self.ctx.check(lib().hrt_query_multi(self._h, C.byref(desc), C.c_void_p(stream)), "query_multi")
+
+    def autotune(self, desc: QueryDesc, repeats: int = 3):
+        """Sweeps the launch grid for desc's kind, keeps the fastest; returns (config dict, ms)."""
+        best = TraceConfig()
+        ms = C.c_float()
+        self.ctx.check(lib().hrt_scene_autotune(self._h, C.byref(desc), int(repeats), C.byref(best), C.byref(ms)),
+                       "autotune")
+        return best.as_dict(), ms.value
+
+    def capture(self, descs) -> "QueryGraph":
+        """Records the launches of `descs` (QueryDesc list) into a CUDA graph (hrt_graph_create)."""
+        return QueryGraph(self, descs)
+
+
     def query_device(self, kind: int, rays_ptr: int, n: int, out_ptr: int, stream: int = 0):
         """Asynchronous query on device arrays (kind 0 nearest -> CRT_Hit[n], 1 any -> uint8[n])."""
         f = lib().hrt_query_nearest if kind == 0 else lib().hrt_query_any
@@ -342,6 +405,31 @@ class SceneRT:
     def close(self):
         if self._h:
             lib().hrt_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class QueryGraph:
+    """A captured sequence of queries (hrt_graph); launch() replays it on a stream."""
+
+    def __init__(self, scene: SceneRT, descs):
+        self.scene = scene
+        arr = (QueryDesc * len(descs))(*descs)
+        self._descs = arr
+        self._h = C.c_void_p()
+        scene.ctx.check(lib().hrt_graph_create(scene._h, arr, len(descs), C.byref(self._h)), "hrt_graph_create")
+
+    def launch(self, stream: int = 0):
+        self.scene.ctx.check(lib().hrt_graph_launch(self._h, C.c_void_p(stream)), "hrt_graph_launch")
+
+    def close(self):
+        if self._h:
+            lib().hrt_graph_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

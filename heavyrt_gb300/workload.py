@@ -25,6 +25,7 @@ _lib = None
 SEED_SOUP = 0x5EED0001
 SEED_HEIGHTFIELD = 0x5EED0002
 SEED_AO = 0x5EED0003
+SEED_BATCH = 0x5EED0004
 
 
 def lib() -> C.CDLL:
@@ -149,6 +150,44 @@ def config1(nx: int = 1024, width: int = 1920, height: int = 1080) -> Workload:
                     {"tris": 2 * nx * nx, "width": width, "height": height, "seed": SEED_HEIGHTFIELD,
                      "ao_per_hit": 16, "ao_length": 0.1 * diag, "ao_offset": 1e-4, "ao_seed": SEED_AO,
                      "heightfield_params": hp.tolist()})
+
+
+def log_uniform_counts(seed: int, stream: int, n: int, lo: int, hi: int) -> np.ndarray:
+    """n integers log-uniform in [lo, hi]: floor(lo * (hi/lo)^u), u = (pcg32 >> 8) * 2^-24."""
+    u = (pcg32(seed, stream, n) >> 8).astype(np.float64) * 2.0 ** -24
+    c = np.floor(lo * np.exp(u * np.log(hi / lo))).astype(np.int64)
+    return np.clip(c, lo, hi)
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    verts: list              # per scene: float32 [3N, 4]
+    idx: list                # per scene: uint32 [3N]
+    rays: np.ndarray         # all scenes' rays, scene after scene: float32 [R, 8]
+    ray_offsets: np.ndarray  # uint32 [S+1]: scene s owns rays ray_offsets[s] .. ray_offsets[s+1]-1
+    params: dict = field(default_factory=dict)
+
+
+def config3(n_scenes: int = 256, tri_lo: int = 1024, tri_hi: int = 262144, ray_lo: int = 4096, ray_hi: int = 65536,
+            seed: int = SEED_BATCH) -> BatchWorkload:
+    """Many independent soups (generator of config0) with log-uniform triangle
+    and ray counts; each scene's rays start uniformly on the sphere of radius 3
+    and aim at uniform points of [-1,1]^3."""
+    tris = log_uniform_counts(seed, 1, n_scenes, tri_lo, tri_hi)
+    nrays = log_uniform_counts(seed, 2, n_scenes, ray_lo, ray_hi)
+    verts, idx, rays = [], [], []
+    for i in range(n_scenes):
+        v, ix = soup(seed + 16 + i, int(tris[i]), -1.0, 1.0, 0.02)
+        verts.append(v)
+        idx.append(ix)
+        rays.append(sphere_rays(seed + 65536 + i, int(nrays[i]), 3.0))
+    offs = np.zeros(n_scenes + 1, dtype=np.uint32)
+    offs[1:] = np.cumsum(nrays)
+    return BatchWorkload(f"soups{n_scenes}_tris{tri_lo}-{tri_hi}_rays{ray_lo}-{ray_hi}", verts, idx,
+                         np.ascontiguousarray(np.concatenate(rays)), offs,
+                         {"scenes": n_scenes, "tris": int(tris.sum()), "rays": int(nrays.sum()), "seed": seed,
+                          "tri_counts": tris.tolist(), "ray_counts": nrays.tolist()})
 
 
 def scene_file(path, verts: np.ndarray, idx: np.ndarray):

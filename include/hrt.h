@@ -191,6 +191,67 @@ int hrt_scene_get_trace_config(const hrt_scene* scene, int kind, hrt_trace_confi
  * tests.  kind: 0 nearest, 1 any.  Device rays; synchronous. */
 int hrt_query_counters(hrt_scene* scene, int kind, const float* rays, uint64_t n, uint64_t counters[2], void* stream);
 
+/* ---------------------------------------------------------------- batches of scenes
+ * Many small scenes served together: their geometries are built by one
+ * segmented LBVH build and their rays traced by one kernel launch.  No
+ * single reference call corresponds; each geometry and each hit is exactly
+ * what one AddGeom_Triangles3f (core/BVH2CommonRT_host.cpp:66-98) and one
+ * RayQuery_NearestHit / RayQuery_AnyHit per scene would give. */
+
+/* AddGeom_Triangles3f for `count` geometries at once.  Host arrays:
+ * geometry i has vertices vertOffsets[i] .. vertOffsets[i+1]-1 of vpos
+ * (vByteStride bytes each, 0 means 12) and indices idxOffsets[i] ..
+ * idxOffsets[i+1]-1 of idx (a multiple of 3 each), its indices counting from
+ * its own first vertex.  Both offset arrays have count+1 entries starting at
+ * 0.  The geometries get ids *firstGeomId .. *firstGeomId+count-1; their
+ * device memory is shared and freed by hrt_clear_geom / hrt_scene_destroy.
+ * Limits: each geometry HRT_MAX_TRIS_PER_GEOM, the batch
+ * HRT_MAX_TRIS_PER_BATCH triangles and 2^32-1 vertices. */
+#define HRT_MAX_TRIS_PER_BATCH ((1u << 30) - 1u)
+int hrt_add_geoms_triangles3f_batched(hrt_scene* scene, uint32_t count, const float* vpos, const uint64_t* vertOffsets,
+                                      const uint32_t* idx, const uint64_t* idxOffsets, int quality,
+                                      uint64_t vByteStride, uint32_t* firstGeomId);
+
+/* One traversal launch.  rays/out as for hrt_query_nearest / hrt_query_any.
+ * With rayOffsets == NULL every ray is traced against the whole scene; else
+ * rays rayOffsets[k] .. rayOffsets[k+1]-1 are traced against instance
+ * segInst[k] only (as a scene holding just that instance would trace them;
+ * the hit's instId is segInst[k]).  rayOffsets (nSeg+1 entries, ascending, 0
+ * first, n last) and segInst (nSeg entries) are device arrays; a ray whose
+ * instance id is out of range is a miss. */
+typedef struct hrt_query_desc
+{
+  int             kind;        /* 0 nearest (out: hrt_hit[n]), 1 any (out: uint8_t[n]) */
+  const float*    rays;        /* device, 8 floats per ray                             */
+  uint64_t        n;
+  const uint32_t* rayOffsets;  /* device or NULL                                       */
+  const uint32_t* segInst;     /* device                                               */
+  uint32_t        nSeg;
+  void*           out;         /* device                                               */
+} hrt_query_desc;
+int hrt_query_multi(hrt_scene* scene, const hrt_query_desc* query, void* stream);
+
+/* Captured query sequences: the launches of `count` queries (in order) are
+ * recorded once into a CUDA graph and replayed by hrt_graph_launch with one
+ * call.  The descriptors' device buffers must stay valid while the graph
+ * exists; their contents may change between launches.  A graph keeps its own
+ * work counters, so different graphs may run concurrently; one graph runs
+ * one launch at a time.  The scene must not be rebuilt or recommitted while
+ * one of its graphs exists. */
+typedef struct hrt_graph hrt_graph;
+int hrt_graph_create(hrt_scene* scene, const hrt_query_desc* queries, uint32_t count, hrt_graph** graph);
+int hrt_graph_launch(hrt_graph* graph, void* stream);
+int hrt_graph_destroy(hrt_graph* graph);
+
+/* Launch-shape autotuner: times `query` (repeats timed runs after one
+ * warm-up) under every trace configuration of a fixed grid (64/128/256
+ * threads; one ray per thread, or the persistent pool with 4..64 steps per
+ * refill and 8..32 idle lanes to refill), sets the fastest as the scene's
+ * configuration for query->kind, and returns it with its mean time in ms.
+ * Synchronous; overwrites query->out (with identical results). */
+int hrt_scene_autotune(hrt_scene* scene, const hrt_query_desc* query, int repeats, hrt_trace_config* best,
+                       float* bestMs);
+
 /* ---------------------------------------------------------------- scene info */
 
 /* ISceneObject::GetGeomNum / GetInstNum / GetGeomBoxes (core/CrossRT.h:163-165). */
