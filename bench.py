@@ -58,6 +58,10 @@ def parse():
                    help="node layout of the scene (binary FP32, 4-wide FP32/FP16/8-bit)")
     p.add_argument("--ncu", action="store_true",
                    help="profiling run: setup, warm-up and timed steps only (no extra builds, counters, e2e, CPU)")
+    p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched measurement")
+    p.add_argument("--only-batched", action="store_true",
+                   help="run only the 256-scene batched measurement (prints its JSON object)")
+    p.add_argument("--batch-scenes", type=int, default=256)
     return p.parse_args()
 
 
@@ -238,6 +242,141 @@ def run_reference(args):
     return 0
 
 
+# ---------------------------------------------------------------- batched scenes
+
+def run_batched(ctx, args, tune: bool = True) -> dict:
+    """256 independent soups (log-uniform 1k..256k triangles) with log-uniform
+    4k..64k rays each: one segmented build + one graph-captured launch per
+    query kind over all scenes ("batched"), against one build and two
+    launches per scene ("plain": BVH2 FP32, default launch shape)."""
+    import torch
+
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import autotune as AT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    w = wl.config3(args.batch_scenes)
+    G = len(w.verts)
+    n = int(w.ray_offsets[-1])
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_rays = torch.from_numpy(w.rays).cuda()
+    d_offs = torch.from_numpy(w.ray_offsets.view(np.int32)).cuda()
+    seg_inst = AT.seg_inst_identity(G)
+    d_seg = torch.from_numpy(seg_inst.view(np.int32)).cuda()
+    d_hits = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+    d_any = torch.empty(n, dtype=torch.uint8, device="cuda")
+
+    # structure + launch shape
+    if tune and not args.ncu:
+        tr = AT.tune_batch(ctx, w.verts, w.idx, d_rays.data_ptr(), n, d_offs.data_ptr(), d_seg.data_ptr(), G,
+                           d_hits.data_ptr(), d_any.data_ptr())
+        layout, merge = tr.layout, tr.merge
+    else:
+        tr, layout, merge = None, "bvh4_f16", 1
+
+    # batched build: repeated for timing (GPU time of the whole batch)
+    b_ms, b_wall = [], []
+    for _ in range(1 if args.ncu else 3):
+        t0 = time.perf_counter()
+        scene, ids = AT.build_batch(ctx, w.verts, w.idx, layout, merge)
+        b_wall.append(time.perf_counter() - t0)
+        b_ms.append(scene.geom_info(ids[0])["build_ms"])
+        if _ < (0 if args.ncu else 2):
+            scene.close()
+    if tr is not None:
+        AT.apply(scene, tr)
+    descs = [E.query_desc(0, d_rays.data_ptr(), n, d_hits.data_ptr(), d_offs.data_ptr(), d_seg.data_ptr(), G),
+             E.query_desc(1, d_rays.data_ptr(), n, d_any.data_ptr(), d_offs.data_ptr(), d_seg.data_ptr(), G)]
+    graph = scene.capture(descs)
+    steps = max(3, args.steps // 10)
+    for _ in range(3):
+        graph.launch(sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        graph.launch(sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / steps
+    if args.ncu:
+        graph.close()
+        return {"ncu_run": True, "batched_ms": batched_ms}
+    hits_b = d_hits.cpu().numpy().view(np.uint32)
+    any_b = d_any.cpu().numpy()
+
+    # plain: one scene per soup, one build and two launches per scene
+    plain, p_ms = [], []
+    t0 = time.perf_counter()
+    for i in range(G):
+        s = SceneRT(ctx)
+        g = s.AddGeom_Triangles3f(w.verts[i], len(w.verts[i]), w.idx[i], w.idx[i].size, vByteStride=16)
+        s.AddInstance(g)
+        s.CommitScene()
+        p_ms.append(s.geom_info(g)["build_ms"])
+        plain.append(s)
+    p_wall = time.perf_counter() - t0
+    p_hits = torch.empty_like(d_hits)
+    p_any = torch.empty_like(d_any)
+    offs = w.ray_offsets.astype(np.int64)
+
+    def plain_step(evs=None):
+        for i, s in enumerate(plain):
+            a, b = int(offs[i]), int(offs[i + 1])
+            if evs is not None:
+                evs[i][0].record(stream)
+            s.query_device(0, d_rays.data_ptr() + 32 * a, b - a, p_hits.data_ptr() + 32 * a, sh)
+            s.query_device(1, d_rays.data_ptr() + 32 * a, b - a, p_any.data_ptr() + a, sh)
+            if evs is not None:
+                evs[i][1].record(stream)
+
+    for _ in range(2):
+        plain_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        plain_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / steps
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(G)]
+    plain_step(evs)
+    torch.cuda.synchronize()
+    plain_kernel_ms = sum(a.elapsed_time(b) for a, b in evs)
+    # the batched results are the per-scene results, up to the instance id (scene index)
+    ph = p_hits.cpu().numpy().view(np.uint32).copy()
+    hit = ph[:, 1] != 0xFFFFFFFF
+    owner = np.repeat(np.arange(G, dtype=np.uint32), np.diff(offs))
+    ph[hit, 2] = owner[hit]
+    ph[hit, 3] = owner[hit]
+    same = bool(np.array_equal(ph, hits_b) and np.array_equal(p_any.cpu().numpy(), any_b))
+    graph.close()
+    scene.close()
+    for s in plain:
+        s.close()
+    rays2 = 2 * n  # each ray is traced twice: nearest and any
+    out = {
+        "workload": w.name, "scenes": G, "tris": w.params["tris"], "rays": n,
+        "structure": {"layout": layout, "bvh4_merge": merge},
+        "launch": tr.configs if tr is not None else None,
+        "tuning_table_ms": tr.table if tr is not None else None,
+        "batched_mrays_s": round(rays2 / batched_ms / 1e3, 2), "batched_ms": round(batched_ms, 4),
+        "plain_mrays_s": round(rays2 / plain_ms / 1e3, 2), "plain_ms": round(plain_ms, 4),
+        "plain_kernel_sum_ms": round(plain_kernel_ms, 4),
+        "speedup": round(plain_ms / batched_ms, 2),
+        "build_batched_gpu_ms": round(statistics.median(b_ms), 3),
+        "build_batched_wall_ms": round(1e3 * statistics.median(b_wall), 1),
+        "build_plain_gpu_ms_sum": round(sum(p_ms), 3), "build_plain_wall_ms": round(1e3 * p_wall, 1),
+        "results_equal_plain": same,
+        "note": "batched = segmented build + one CUDA graph of two segmented launches (nearest, any) over all "
+                "scenes, structure and launch shape autotuned; plain = BVH2 FP32 scene per soup, two launches "
+                "per scene on one stream (ms includes launch gaps; kernel_sum excludes them)",
+    }
+    return out
+
+
 # ---------------------------------------------------------------- GPU engine
 
 def run_engine(args):
@@ -252,8 +391,12 @@ def run_engine(args):
     from heavyrt_gb300 import Context, PinnedBuffer, SceneRT
     from heavyrt_gb300 import engine as E
 
-    w = make_frame(args)
     ctx = Context(local)
+    if args.only_batched:
+        if rank == 0:
+            print(json.dumps({"batched": run_batched(ctx, args)}), flush=True)
+        return 0
+    w = make_frame(args)
     scene = SceneRT(ctx, layout=args.layout)
     gid = scene.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
     scene.AddInstance(gid)
@@ -395,6 +538,9 @@ def run_engine(args):
         "clocks": clk,
     }
 
+    if not args.no_batched:
+        line["batched"] = run_batched(ctx, args)
+        line["gpu_launches_batched_per_step"] = 2
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as orc
 
