@@ -62,6 +62,11 @@ def parse():
     p.add_argument("--only-batched", action="store_true",
                    help="run only the 256-scene batched measurement (prints its JSON object)")
     p.add_argument("--batch-scenes", type=int, default=256)
+    p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
+    p.add_argument("--only-served", action="store_true",
+                   help="run only the served-stream measurement (prints its JSON object)")
+    p.add_argument("--served-seconds", type=float, default=4.0, help="length of the request arrival trace")
+    p.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrival rate, requests/s")
     return p.parse_args()
 
 
@@ -377,6 +382,191 @@ def run_batched(ctx, args, tune: bool = True) -> dict:
     return out
 
 
+# ---------------------------------------------------------------- served stream
+
+def served_workload(args):
+    """64 resident scenes, the arrival trace, ray pools and upload scenes."""
+    from heavyrt_gb300 import workload as wl
+
+    seed = 0x5EED0005
+    n_tris = wl.log_uniform_counts(seed, 1, 64, 10000, 2000000)
+    scenes = []
+    for i, n in enumerate(n_tris):
+        if i % 2 == 0:
+            scenes.append(wl.soup(seed + 100 + i, int(n), -1.0, 1.0, 0.02))
+        else:
+            side = max(2, int(round((int(n) / 2) ** 0.5)))
+            v, idx, _ = wl.heightfield(seed + 100 + i, side, side)
+            scenes.append((v, idx))
+    up_tris = wl.log_uniform_counts(seed, 2, 6, 100000, 1000000)
+    uploads = [wl.soup(seed + 300 + i, int(n), -1.0, 1.0, 0.02) for i, n in enumerate(up_tris)]
+    rng = np.random.default_rng(seed)
+    count = int(args.served_rate * args.served_seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.served_rate, count))
+    sizes = wl.log_uniform_counts(seed, 3, count, 1000, 1000000)
+    target = rng.integers(0, len(scenes), count)
+    kinds = rng.integers(0, 2, count)
+    upload = rng.random(count) < 0.05
+    pools = [wl.sphere_rays(seed + 400 + k, 1000000, 3.0) for k in range(4)]
+    return {"scenes": scenes, "uploads": uploads, "arrivals": arrivals, "sizes": sizes, "target": target,
+            "kinds": kinds, "upload": upload, "pools": pools,
+            "tris": [int(len(x[1]) // 3) for x in scenes]}
+
+
+def _latency_stats(lat_s, rays, span_s):
+    lat = np.sort(np.asarray(lat_s)) * 1e3
+    return {"p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "max_ms": round(float(lat[-1]), 3), "mrays_s": round(rays / span_s / 1e6, 2),
+            "requests": int(len(lat))}
+
+
+def run_served(ctx, args) -> dict:
+    """Served stream: 64 resident scenes (soups and heightfields, log-uniform
+    10k..2M triangles), Poisson arrivals, each request log-uniform 1k..1M rays
+    against a uniformly chosen scene, half nearest / half any; 5% of requests
+    upload a new 100k..1M-triangle scene (built on arrival, evictable) and
+    query it.  "served": the engine's server (continuous batching over
+    resident scenes, 150 GB budget); "plain": the same arrivals handled one at
+    a time in arrival order through the host-pointer query of one BVH2 scene
+    per geometry.  Latency = completion - scheduled arrival."""
+    import queue as Q
+
+    from heavyrt_gb300 import PinnedBuffer, SceneRT
+    from heavyrt_gb300 import engine as E
+
+    W = served_workload(args)
+    arrivals, sizes, target, kinds, upload = W["arrivals"], W["sizes"], W["target"], W["kinds"], W["upload"]
+    count = len(arrivals)
+    pools = []
+    for p in W["pools"]:
+        b = PinnedBuffer(p.nbytes)
+        b.array(np.float32).reshape(-1, 8)[:] = p
+        pools.append(b)
+    ring = 64
+    outs = [PinnedBuffer(32 * 1000000) for _ in range(ring)]
+    result = {"workload": f"served: 64 resident scenes ({sum(W['tris'])} tris), Poisson {args.served_rate:.0f} req/s "
+                          f"for {args.served_seconds:.1f} s, 1k..1M rays per request, 5% uploads",
+              "requests": count, "rays": int(sizes.sum()), "uploads": int(upload.sum())}
+
+    # ---- served
+    srv = E.Server(ctx, memory_budget=150 * 10**9, layout="bvh4_f16", bvh4_merge=1)
+    t0 = time.perf_counter()
+    ids = [srv.add_scene(v, idx, evictable=False) for v, idx in W["scenes"]]
+    for i in ids:
+        assert srv.scene_state(i, timeout=600) == E.SCENE_READY
+    setup_s = time.perf_counter() - t0
+    lat = np.zeros(count)
+    tickets = Q.Queue()
+    busy = [False] * ring  # output buffer in use by a request in flight
+    done_lock = threading.Condition()
+    up_q = Q.Queue()
+    infos = [None] * count
+
+    def waiter():
+        while True:
+            item = tickets.get()
+            if item is None:
+                return
+            j, t, lag = item
+            st, info = srv.wait(t)
+            if st != 0:
+                raise RuntimeError(f"served request {j} failed: {st}")
+            lat[j] = (info["tDone"] - info["tSubmit"]) + lag
+            infos[j] = info
+            with done_lock:
+                busy[j % ring] = False
+                done_lock.notify_all()
+
+    def submit(j, sid, start):
+        with done_lock:
+            while busy[j % ring]:
+                done_lock.wait()
+            busy[j % ring] = True
+        n = int(sizes[j])
+        t = srv.submit(sid, int(kinds[j]), pools[j % 4].ptr, n, outs[j % ring].ptr)
+        tickets.put((j, t, time.perf_counter() - start - arrivals[j]))
+
+    def uploader(start):
+        while True:
+            j = up_q.get()
+            if j is None:
+                return
+            v, idx = W["uploads"][j % len(W["uploads"])]
+            sid = srv.add_scene(v, idx, evictable=True)
+            submit(j, sid, start)
+
+    wt = threading.Thread(target=waiter)
+    wt.start()
+    start = time.perf_counter()
+    ut = threading.Thread(target=uploader, args=(start,))
+    ut.start()
+    for j in range(count):
+        d = start + arrivals[j] - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        if upload[j]:
+            up_q.put(j)
+        else:
+            submit(j, ids[int(target[j])], start)
+    up_q.put(None)
+    ut.join()
+    tickets.put(None)
+    wt.join()
+    span = time.perf_counter() - start
+    st = srv.stats()
+    srv.close()
+    served = _latency_stats(lat, float(sizes.sum()), span)
+    bsz = [i["batchRequests"] for i in infos]
+    served.update({"batches": int(st["batches"]), "mean_requests_per_batch": round(float(np.mean(bsz)), 2),
+                   "max_requests_per_batch": int(max(bsz)), "builds": int(st["builds"]),
+                   "evictions": int(st["evictions"]), "peak_resident_gb": round(st["peakResidentBytes"] / 1e9, 2),
+                   "upload_p50_ms": round(float(np.percentile(lat[upload] * 1e3, 50)), 3) if upload.any() else None,
+                   "setup_s": round(setup_s, 2), "layout": "bvh4_f16 (merge 1)"})
+
+    # ---- plain: one request at a time, in arrival order
+    plain_scenes = []
+    for v, idx in W["scenes"]:
+        sc = SceneRT(ctx)
+        g = sc.AddGeom_Triangles3f(v, len(v), idx, idx.size, vByteStride=16)
+        sc.AddInstance(g)
+        sc.CommitScene()
+        plain_scenes.append(sc)
+    L = E.lib()
+    import ctypes as C
+
+    lat_p = np.zeros(count)
+    start = time.perf_counter()
+    for j in range(count):
+        d = start + arrivals[j] - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        n = int(sizes[j])
+        if upload[j]:
+            v, idx = W["uploads"][j % len(W["uploads"])]
+            sc = SceneRT(ctx)
+            g = sc.AddGeom_Triangles3f(v, len(v), idx, idx.size, vByteStride=16)
+            sc.AddInstance(g)
+            sc.CommitScene()
+        else:
+            sc = plain_scenes[int(target[j])]
+        f = L.hrt_query_nearest_host if kinds[j] == 0 else L.hrt_query_any_host
+        ctx.check(f(sc._h, C.c_void_p(pools[j % 4].ptr), n, C.c_void_p(outs[0].ptr)), "plain query")
+        if upload[j]:
+            sc.close()
+        lat_p[j] = time.perf_counter() - start - arrivals[j]
+    span_p = time.perf_counter() - start
+    for sc in plain_scenes:
+        sc.close()
+    for b in pools + outs:
+        b.free()
+    result["served"] = served
+    result["plain"] = _latency_stats(lat_p, float(sizes.sum()), span_p)
+    result["plain"]["layout"] = "bvh2"
+    result["note"] = ("Mrays/s = rays of all requests / (last completion - first arrival): at an offered load below "
+                      "capacity it equals the offered rate; the latencies show the difference")
+    return result
+
+
 # ---------------------------------------------------------------- GPU engine
 
 def run_engine(args):
@@ -395,6 +585,10 @@ def run_engine(args):
     if args.only_batched:
         if rank == 0:
             print(json.dumps({"batched": run_batched(ctx, args)}), flush=True)
+        return 0
+    if args.only_served:
+        if rank == 0:
+            print(json.dumps({"served": run_served(ctx, args)}), flush=True)
         return 0
     w = make_frame(args)
     scene = SceneRT(ctx, layout=args.layout)
@@ -541,6 +735,8 @@ def run_engine(args):
     if not args.no_batched:
         line["batched"] = run_batched(ctx, args)
         line["gpu_launches_batched_per_step"] = 2
+    if not args.no_served:
+        line["served"] = run_served(ctx, args)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as orc
 

@@ -10,85 +10,16 @@
 #include <string>
 #include <vector>
 
-#include "hrt_kernels.cuh"
-#include "../../include/hrt.h"
+#include "hrt_internal.cuh"
 
 using namespace hrt;
+using namespace hrt::api;
 
-static constexpr uint32_t kCounterSlots = 256;
 
-struct hrt_context
+
+namespace hrt
 {
-  int          device = 0;
-  int          numSMs = 0;
-  cudaStream_t stream = nullptr;
-  std::string  lastError;
-  std::mutex   mu;
-};
-
-namespace
-{
-
-struct Geom
-{
-  uint32_t     nTris = 0, nVerts = 0, nLeaves = 0;
-  float4*      verts = nullptr;
-  uint32_t*    keys = nullptr;          // sorted Morton codes
-  uint32_t*    vals = nullptr;          // sorted triangle ids (= prim indices)
-  uint32_t*    keysUnsorted = nullptr;
-  uint32_t*    compressed = nullptr;
-  uint32_t*    runStarts = nullptr;
-  BVHNode32*   lr = nullptr;
-  uint32_t*    lrCount = nullptr;
-  PairRec*     recs = nullptr;
-  TriRec*      tris = nullptr;
-  uint32_t*    sortedIdx = nullptr;
-  BuildParams* params = nullptr;
-  BuildParams  host{};
-  float        buildMs = 0.0f;
-  uint64_t     bytes = 0;
-  float        box[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  void*        nodes4 = nullptr;  // 4-wide nodes of the scene's layout
-  uint32_t     nNodes4 = 0;
-  bool         shared = false;    // arrays point into a batch allocation (hrt_add_geoms_triangles3f_batched)
-};
-
-struct Instance
-{
-  uint32_t geomId = 0;
-  float    m[16];     // column-major
-  float    inv[12];   // rows 0..2 of the inverse, row-major
-  bool     identity = true;
-};
-
-}  // namespace
-
-struct hrt_scene
-{
-  hrt_context*          ctx = nullptr;
-  std::vector<Geom>     geoms;
-  std::vector<Instance> insts;
-  std::vector<void*>    batchAllocs;  // device allocations shared by batch-built geometries
-  bool                  committed = false;
-  int                   layout = HRT_LAYOUT_BVH2;
-  int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
-  InstanceDesc*         dInst = nullptr;
-  uint32_t              nInstDev = 0;
-  uint32_t*             dError = nullptr;
-  unsigned long long*   dCounters = nullptr;
-  // work counters of the persistent traversal pool: one slot per launch, taken
-  // round-robin, so up to kCounterSlots queries on one scene may be in flight
-  unsigned int*         dRayCounters = nullptr;
-  std::atomic<uint32_t> counterSlot{0};
-  TraceConfig           cfg[2];  // [0] nearest, [1] any
-  // staging for the host-pointer queries
-  void*                 stageRays = nullptr;
-  void*                 stageOut = nullptr;
-  uint64_t              stageCap = 0;
-  std::mutex            mu;
-};
-
-namespace
+namespace api
 {
 
 int fail(hrt_context* ctx, int status, const std::string& msg)
@@ -573,6 +504,19 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   return HRT_OK;
 }
 
+void make_instance_desc(const Geom& g, uint32_t geomId, uint32_t instId, const float* inv12, InstanceDesc& d)
+{
+  static const float id12[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  d.recs = g.recs;
+  d.nodes4 = g.nodes4;
+  d.tris = g.tris;
+  d.geomId = geomId;
+  d.instId = instId;
+  d.identity = inv12 ? 0u : 1u;
+  d.valid = g.nTris > 0 ? 1u : 0u;
+  std::memcpy(d.inv, inv12 ? inv12 : id12, sizeof(d.inv));
+}
+
 bool lbvh_builder_name(const char* name)
 {
   if (!name || !*name) return true;
@@ -629,7 +573,8 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
   return HRT_OK;
 }
 
-}  // namespace
+}  // namespace api
+}  // namespace hrt
 
 extern "C" {
 
@@ -878,15 +823,7 @@ int hrt_commit_scene(hrt_scene* s, int quality)
   for (size_t i = 0; i < s->insts.size(); i++)
   {
     const Instance& in = s->insts[i];
-    const Geom& gm = s->geoms[in.geomId];
-    d[i].recs = gm.recs;
-    d[i].nodes4 = gm.nodes4;
-    d[i].tris = gm.tris;
-    d[i].geomId = in.geomId;
-    d[i].instId = (uint32_t)i;
-    d[i].identity = in.identity ? 1u : 0u;
-    d[i].valid = gm.nTris > 0 ? 1u : 0u;
-    std::memcpy(d[i].inv, in.inv, sizeof(in.inv));
+    make_instance_desc(s->geoms[in.geomId], in.geomId, (uint32_t)i, in.identity ? nullptr : in.inv, d[i]);
   }
   if (s->dInst) cudaFree(s->dInst);
   s->dInst = nullptr;

@@ -89,6 +89,38 @@ def query_desc(kind: int, rays_ptr: int, n: int, out_ptr: int, ray_offsets_ptr: 
                      C.c_void_p(seg_inst_ptr or None), int(n_seg), C.c_void_p(out_ptr))
 
 
+class ServerConfig(C.Structure):
+    """hrt_server_config (include/hrt.h)."""
+
+    _fields_ = [("memoryBudget", C.c_uint64), ("slotRays", C.c_uint64), ("slots", C.c_uint32),
+                ("maxScenes", C.c_uint32), ("maxBatchRequests", C.c_uint32), ("layout", C.c_int),
+                ("bvh4Merge", C.c_int)]
+
+
+class RequestInfo(C.Structure):
+    """hrt_request_info (include/hrt.h)."""
+
+    _fields_ = [("status", C.c_int), ("batch", C.c_uint32), ("batchRequests", C.c_uint32), ("batchRays", C.c_uint64),
+                ("tSubmit", C.c_double), ("tStart", C.c_double), ("tDone", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    """hrt_server_stats (include/hrt.h)."""
+
+    _fields_ = [("requests", C.c_uint64), ("rays", C.c_uint64), ("batches", C.c_uint64), ("builds", C.c_uint64),
+                ("evictions", C.c_uint64), ("failed", C.c_uint64), ("residentBytes", C.c_uint64),
+                ("peakResidentBytes", C.c_uint64), ("scenesResident", C.c_uint32), ("queued", C.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+SCENE_BUILDING, SCENE_READY, SCENE_FAILED, SCENE_EVICTED = 0, 1, 2, 3
+
+
 class HrtError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"hrt status {status}: {message}")
@@ -150,6 +182,15 @@ def lib() -> C.CDLL:
         "hrt_graph_launch": (i32, [vp, vp]),
         "hrt_graph_destroy": (i32, [vp]),
         "hrt_scene_autotune": (i32, [vp, C.POINTER(QueryDesc), i32, C.POINTER(TraceConfig), C.POINTER(C.c_float)]),
+        "hrt_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+        "hrt_server_destroy": (i32, [vp]),
+        "hrt_server_add_scene": (i32, [vp, vp, u64, vp, u64, u64, i32, C.POINTER(u32)]),
+        "hrt_server_scene_state": (i32, [vp, u32, C.c_double, C.POINTER(i32)]),
+        "hrt_server_remove_scene": (i32, [vp, u32]),
+        "hrt_server_submit": (i32, [vp, u32, i32, vp, u64, vp, C.POINTER(u64)]),
+        "hrt_server_wait": (i32, [vp, u64, C.c_double, C.POINTER(RequestInfo)]),
+        "hrt_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
+        "hrt_server_scene_bytes": (i32, [vp, u64, u64, C.POINTER(u64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -430,6 +471,76 @@ class QueryGraph:
     def close(self):
         if self._h:
             lib().hrt_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop over resident scenes (hrt_server_*): builds on arrival,
+    memory-budget admission, continuous batching of ray requests."""
+
+    def __init__(self, ctx: Context | None = None, memory_budget: int = 0, slot_rays: int = 0, slots: int = 0,
+                 max_scenes: int = 0, max_batch_requests: int = 0, layout=LAYOUT_BVH2, bvh4_merge: int = 0):
+        self.ctx = ctx or default_context()
+        if isinstance(layout, str):
+            layout = LAYOUT_NAMES[layout.lower()]
+        cfg = ServerConfig(memory_budget, slot_rays, slots, max_scenes, max_batch_requests, int(layout),
+                           int(bvh4_merge))
+        self._h = C.c_void_p()
+        self.ctx.check(lib().hrt_server_create(self.ctx.handle, C.byref(cfg), C.byref(self._h)), "hrt_server_create")
+
+    def add_scene(self, verts: np.ndarray, idx: np.ndarray, evictable: bool = True) -> int:
+        """Queues a scene build; returns its id at once.  verts: float32 [V, 3] or [V, 4]."""
+        v = np.ascontiguousarray(verts, dtype=np.float32)
+        v = v.reshape(v.shape[0], -1) if v.size else v.reshape(0, 3)
+        i = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1)
+        sid = C.c_uint32()
+        self.ctx.check(lib().hrt_server_add_scene(self._h, _ptr(v), v.shape[0], _ptr(i), i.size, 4 * v.shape[1],
+                                                  int(bool(evictable)), C.byref(sid)), "hrt_server_add_scene")
+        return sid.value
+
+    def scene_state(self, scene_id: int, timeout: float = 0.0) -> int:
+        st = C.c_int()
+        self.ctx.check(lib().hrt_server_scene_state(self._h, scene_id, float(timeout), C.byref(st)), "scene_state")
+        return st.value
+
+    def remove_scene(self, scene_id: int):
+        self.ctx.check(lib().hrt_server_remove_scene(self._h, scene_id), "hrt_server_remove_scene")
+
+    def submit(self, scene_id: int, kind: int, rays_ptr: int, n: int, out_ptr: int) -> int:
+        """Queues a request on host buffers (pointers as ints); returns its ticket."""
+        t = C.c_uint64()
+        self.ctx.check(lib().hrt_server_submit(self._h, scene_id, kind, C.c_void_p(rays_ptr), n, C.c_void_p(out_ptr),
+                                               C.byref(t)), "hrt_server_submit")
+        return t.value
+
+    def submit_array(self, scene_id: int, kind: int, rays: np.ndarray, out: np.ndarray) -> int:
+        return self.submit(scene_id, kind, rays.ctypes.data, rays.shape[0], out.ctypes.data)
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """(status, info dict) of a request; status HRT_ERR_TIMEOUT keeps the ticket valid."""
+        info = RequestInfo()
+        st = lib().hrt_server_wait(self._h, ticket, float(timeout), C.byref(info))
+        return st, info.as_dict()
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self.ctx.check(lib().hrt_server_get_stats(self._h, C.byref(s)), "hrt_server_get_stats")
+        return s.as_dict()
+
+    def scene_bytes(self, n_verts: int, n_tris: int) -> int:
+        b = C.c_uint64()
+        self.ctx.check(lib().hrt_server_scene_bytes(self._h, n_verts, n_tris, C.byref(b)), "hrt_server_scene_bytes")
+        return b.value
+
+    def close(self):
+        if self._h:
+            lib().hrt_server_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

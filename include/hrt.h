@@ -252,6 +252,87 @@ int hrt_graph_destroy(hrt_graph* graph);
 int hrt_scene_autotune(hrt_scene* scene, const hrt_query_desc* query, int repeats, hrt_trace_config* best,
                        float* bestMs);
 
+/* ---------------------------------------------------------------- serving
+ * A request loop over scenes kept resident in device memory.  No reference
+ * counterpart (HeavyRT's renderers call ISceneObject per ray on one scene).
+ *
+ * Scenes are built on arrival by the server's builder thread and admitted
+ * against a device-memory budget: when a new scene does not fit, idle
+ * evictable scenes are evicted, least recently used first.  Ray requests
+ * (host arrays) are queued; whenever one of the server's batch slots is free,
+ * a dispatcher packs every queued request whose scene is ready (in arrival
+ * order, up to the slot's capacity) into one batch and traces it with one
+ * segmented launch per query kind on the slot's own stream.  Requests that
+ * arrive while batches are on the GPU join the next free slot, and the
+ * copies and traversals of successive batches overlap.  A request's results
+ * do not depend on the requests it was batched with.
+ *
+ * Host ray / result buffers must stay valid until the request is waited for;
+ * page-locked buffers (hrt_host_alloc) copy at full link speed.  Every ticket
+ * must be waited for exactly once.  Scene ids of evicted or removed scenes
+ * are never valid again. */
+typedef struct hrt_server hrt_server;
+
+typedef struct hrt_server_config
+{
+  uint64_t memoryBudget;     /* device bytes for scenes + batch slots; 0 = 150e9          */
+  uint64_t slotRays;         /* rays per batch slot = largest request; 0 = 8,388,608       */
+  uint32_t slots;            /* batches in flight, 1..16; 0 = 3                            */
+  uint32_t maxScenes;        /* resident scene capacity, <= 65536; 0 = 4096                */
+  uint32_t maxBatchRequests; /* requests per batch; 0 = 1024                               */
+  int      layout;           /* HRT_LAYOUT_* of every scene                                */
+  int      bvh4Merge;        /* HRT_OPTION_BVH4_MERGE value for 4-wide layouts             */
+} hrt_server_config;
+
+/* Result of one request; times in seconds since the server was created. */
+typedef struct hrt_request_info
+{
+  int      status;         /* HRT_OK, or why the request failed                    */
+  uint32_t batch;          /* sequence number of the batch that traced it          */
+  uint32_t batchRequests;  /* requests in that batch                               */
+  uint64_t batchRays;      /* rays in that batch                                   */
+  double   tSubmit, tStart, tDone;
+} hrt_request_info;
+
+typedef struct hrt_server_stats
+{
+  uint64_t requests, rays, batches, builds, evictions, failed;
+  uint64_t residentBytes, peakResidentBytes;  /* held against the budget        */
+  uint32_t scenesResident, queued;
+} hrt_server_stats;
+
+#define HRT_SCENE_BUILDING 0
+#define HRT_SCENE_READY    1
+#define HRT_SCENE_FAILED   2
+#define HRT_SCENE_EVICTED  3  /* evicted, removed or never existed */
+
+int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_server** server);
+/* Finishes queued builds and requests, then frees everything. */
+int hrt_server_destroy(hrt_server* server);
+/* Queues the build of a scene of one triangle geometry under the identity
+ * (arguments as hrt_add_geom_triangles3f; the arrays are copied before the call
+ * returns).  Requests may be submitted at once; they run when the build is
+ * done.  evictable = 0 keeps the scene until it is removed.
+ * HRT_ERR_OUT_OF_MEMORY when it cannot fit the budget even after evictions. */
+int hrt_server_add_scene(hrt_server* server, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
+                         uint64_t vByteStride, int evictable, uint32_t* sceneId);
+/* HRT_SCENE_* state; waits up to timeoutSeconds (< 0: no limit) while building. */
+int hrt_server_scene_state(hrt_server* server, uint32_t sceneId, double timeoutSeconds, int* state);
+/* Frees a ready scene with no requests queued or in flight (HRT_ERR_STATE otherwise). */
+int hrt_server_remove_scene(hrt_server* server, uint32_t sceneId);
+/* Queues a request: n rays (host, 8 floats each) against one scene; kind 0
+ * writes hrt_hit[n] to out, kind 1 uint8_t[n]. */
+int hrt_server_submit(hrt_server* server, uint32_t sceneId, int kind, const float* rays, uint64_t n, void* out,
+                      uint64_t* ticket);
+/* Waits for a request (timeoutSeconds < 0: no limit; HRT_ERR_TIMEOUT leaves the
+ * ticket valid); returns the request's status and fills info. */
+int hrt_server_wait(hrt_server* server, uint64_t ticket, double timeoutSeconds, hrt_request_info* info);
+int hrt_server_get_stats(hrt_server* server, hrt_server_stats* stats);
+/* Bytes a scene of nVert vertices and nTris triangles reserves against the
+ * budget while it is built (its arrays plus the build's transient arrays);
+ * once built it holds its actual, smaller size. */
+int hrt_server_scene_bytes(const hrt_server* server, uint64_t nVert, uint64_t nTris, uint64_t* bytes);
+
 /* ---------------------------------------------------------------- scene info */
 
 /* ISceneObject::GetGeomNum / GetInstNum / GetGeomBoxes (core/CrossRT.h:163-165). */
