@@ -54,14 +54,21 @@ def parse():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--layout", default="bvh2", choices=["bvh2", "bvh4", "bvh4_f16", "bvh4_q8"],
-                   help="node layout of the scene (binary FP32, 4-wide FP32/FP16/8-bit)")
+    p.add_argument("--layout", default="bvh4_f16", choices=["bvh2", "bvh4", "bvh4_f16", "bvh4_q8"],
+                   help="node layout of the headline scene (binary FP32, 4-wide FP32/FP16/8-bit)")
+    p.add_argument("--merge", type=int, default=1, help="BVH4 leaf merge bound of the headline scene")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain BVH2 FP32 comparison")
     p.add_argument("--ncu", action="store_true",
                    help="profiling run: setup, warm-up and timed steps only (no extra builds, counters, e2e, CPU)")
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched measurement")
     p.add_argument("--only-batched", action="store_true",
                    help="run only the 256-scene batched measurement (prints its JSON object)")
     p.add_argument("--batch-scenes", type=int, default=256)
+    p.add_argument("--no-precision", action="store_true", help="skip the quantised-node precision measurement")
+    p.add_argument("--only-precision", action="store_true",
+                   help="run only the quantised-node precision measurement (prints its JSON object)")
+    p.add_argument("--soup-tris", type=int, default=8388608, help="soup size of the precision measurement")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     p.add_argument("--only-served", action="store_true",
                    help="run only the served-stream measurement (prints its JSON object)")
@@ -382,6 +389,145 @@ def run_batched(ctx, args, tune: bool = True) -> dict:
     return out
 
 
+# ---------------------------------------------------------------- quantised nodes
+
+def t_error_fp64(rays, hits, verts_all, sorted_idx_all, prim_base):
+    """Relative error of the FP32 hit distance against the same ray-triangle
+    intersection evaluated in FP64 (host), over the rays that hit."""
+    h = hits.view(np.uint32).reshape(-1, 8)
+    hit = h[:, 1] != 0xFFFFFFFF
+    r = rays[hit].astype(np.float64)
+    prim = h[hit, 1].astype(np.int64) + prim_base[h[hit, 3].astype(np.int64)]
+    tri = sorted_idx_all.reshape(-1, 3)[prim].astype(np.int64)
+    v = verts_all[:, :3].astype(np.float64)
+    a, b, c = v[tri[:, 0]], v[tri[:, 1]], v[tri[:, 2]]
+    o, d = r[:, 0:3], r[:, 4:7]
+    e1, e2 = b - a, c - a
+    pv = np.cross(d, e2)
+    det = np.einsum("ij,ij->i", e1, pv)
+    sv = o - a
+    qv = np.cross(sv, e1)
+    t64 = np.einsum("ij,ij->i", e2, qv) / det
+    bu = np.einsum("ij,ij->i", sv, pv) / det
+    bv = np.einsum("ij,ij->i", d, qv) / det
+    t32 = h[hit, 0].view(np.float32).astype(np.float64)
+    rel = np.abs(t32 - t64) / np.abs(t64)
+    outside = int(np.count_nonzero((bu < -1e-6) | (bv < -1e-6) | (bu + bv > 1 + 1e-6)))
+    return {"rays_checked": int(hit.sum()), "max_rel": float(rel.max()), "p99_rel": float(np.percentile(rel, 99)),
+            "mean_rel": float(rel.mean()), "outside_fp64_triangle": outside}
+
+
+def run_precision(ctx, args) -> dict:
+    """Heightfield (1024 x 1024 quads) plus an 8,388,608-triangle soup
+    (offsets +-0.005) as two instances; 1920 x 1080 eye rays and 16 AO rays per
+    primary hit.  Every layout traces the same rays; nearest hits of the
+    quantised layouts are compared with the FP32-node build (BVH4 FP32, same
+    tree) and the binary FP32 tree, any-hit flags with both, and the hit
+    distance with an FP64 evaluation on 1M sampled eye rays."""
+    import torch
+
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    w = wl.config1(args.nx, args.width, args.height)
+    sv, sidx = wl.soup(0x5EED0006, args.soup_tris, -1.0, 1.0, 0.005)
+    geoms = [(w.verts, w.idx), (sv, sidx)]
+    n_h = len(w.idx) // 3
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    layouts = [("bvh2", None), ("bvh4", 1), ("bvh4_f16", 1), ("bvh4_q8", 1)]
+    res = {"workload": f"heightfield{args.nx}x{args.nx} + soup{args.soup_tris} (2 instances), eye {args.width}x"
+                       f"{args.height} + 16 AO per hit", "tris": int(n_h + len(sidx) // 3)}
+    d_eye = torch.from_numpy(w.eye_rays).cuda()
+    n_eye = len(w.eye_rays)
+    ref_hits = ref_any = ao = d_ao = None
+    out = {}
+    for layout, merge in layouts:
+        sc = SceneRT(ctx, layout=layout)
+        if merge is not None:
+            sc.set_bvh4_merge(merge)
+        gids = [sc.AddGeom_Triangles3f(v, len(v), i, i.size, vByteStride=16) for v, i in geoms]
+        for g in gids:
+            sc.AddInstance(g)
+        sc.CommitScene()
+        build_ms = sum(sc.geom_info(g)["build_ms"] for g in gids)
+        d_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
+        sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+        torch.cuda.synchronize()
+        hits = d_hits.cpu().numpy().view(np.uint32)
+        if ao is None:
+            # AO rays from the binary FP32 tree's primary hits (same input for every layout)
+            si = [sc.export(g, E.EXPORT_SORTED_INDICES) for g in gids]
+            verts_all = np.concatenate([geoms[0][0], geoms[1][0]])
+            si_all = np.concatenate([si[0], si[1] + len(geoms[0][0])]).astype(np.uint32)
+            prim_base = np.array([0, n_h], dtype=np.int64)
+            hh = hits.copy()
+            m = hh[:, 1] != 0xFFFFFFFF
+            hh[m, 1] = hh[m, 1] + prim_base[hh[m, 3]].astype(np.uint32)
+            p = w.params
+            ao, _ = wl.ao_rays(p["ao_seed"], w.eye_rays, hh.view(np.float32), verts_all, si_all, p["ao_per_hit"],
+                               p["ao_length"], p["ao_offset"])
+            d_ao = torch.from_numpy(ao).cuda()
+            rng = np.random.default_rng(7)
+            sample = np.sort(rng.choice(n_eye, size=min(1000000, n_eye), replace=False))
+            res["t_error_vs_fp64"] = t_error_fp64(w.eye_rays[sample], hits[sample], verts_all, si_all, prim_base)
+        n_ao = len(ao)
+        d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
+        for k in range(3):
+            sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+            sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+        torch.cuda.synchronize()
+        steps = 10
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        t_eye = t_ao = 0.0
+        for _ in range(steps):
+            e[0].record(stream)
+            sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+            e[1].record(stream)
+            sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            t_eye += e[0].elapsed_time(e[1])
+            t_ao += e[1].elapsed_time(e[2])
+        t_eye /= steps
+        t_ao /= steps
+        anyf = d_any.cpu().numpy()
+        pairs_eye, _ = sc.query_counters(0, d_eye.data_ptr(), n_eye, sh)
+        pairs_ao, _ = sc.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+        entry = {"eye_ms": round(t_eye, 4), "ao_ms": round(t_ao, 4),
+                 "mrays_s": round((n_eye + n_ao) / (t_eye + t_ao) / 1e3, 2), "build_ms": round(build_ms, 3),
+                 "node_fetches_per_eye_ray": round(pairs_eye / n_eye, 3),
+                 "node_fetches_per_ao_ray": round(pairs_ao / n_ao, 3),
+                 "bvh_bytes": int(sum(sc.geom_info(g)["bytes"] for g in gids))}
+        if ref_hits is None:
+            ref_hits, ref_any = hits, anyf
+        else:
+            diff = np.any(hits != ref_hits, axis=1)
+            same_t = hits[:, 0] == ref_hits[:, 0]
+            entry["nearest_mismatch_vs_bvh2"] = int(np.count_nonzero(diff & ~same_t))
+            entry["nearest_equal_t_other_triangle_vs_bvh2"] = int(np.count_nonzero(diff & same_t))
+            entry["anyhit_mismatch_vs_bvh2"] = int(np.count_nonzero(anyf != ref_any))
+            if layout != "bvh4":
+                f32 = out["bvh4"]["_hits"]
+                d32 = np.any(hits != f32, axis=1)
+                entry["nearest_mismatch_vs_fp32_nodes"] = int(np.count_nonzero(d32 & (hits[:, 0] != f32[:, 0])))
+                entry["nearest_equal_t_other_triangle_vs_fp32_nodes"] = int(
+                    np.count_nonzero(d32 & (hits[:, 0] == f32[:, 0])))
+        entry["_hits"] = hits
+        out[layout] = entry
+        sc.close()
+        del d_hits, d_any
+    for k in out:
+        out[k].pop("_hits")
+    res["eye_rays"] = n_eye
+    res["ao_rays"] = int(len(ao))
+    res["layouts"] = out
+    res["note"] = ("mismatch = different hit distance (must be 0); equal_t_other_triangle = a tie between triangles "
+                   "at the same t, resolved by visit order")
+    return res
+
+
 # ---------------------------------------------------------------- served stream
 
 def served_workload(args):
@@ -590,17 +736,26 @@ def run_engine(args):
         if rank == 0:
             print(json.dumps({"served": run_served(ctx, args)}), flush=True)
         return 0
+    if args.only_precision:
+        if rank == 0:
+            print(json.dumps({"precision": run_precision(ctx, args)}), flush=True)
+        return 0
     w = make_frame(args)
-    scene = SceneRT(ctx, layout=args.layout)
-    gid = scene.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
-    scene.AddInstance(gid)
-    scene.CommitScene()
+    def make_scene(layout):
+        sc = SceneRT(ctx, layout=layout)
+        if layout != "bvh2":
+            sc.set_bvh4_merge(args.merge)
+        g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+        sc.AddInstance(g)
+        sc.CommitScene()
+        return sc, g
+
+    scene, gid = make_scene(args.layout)
     info = scene.geom_info(gid)
     # build time: a few more builds of the same geometry
     build_ms = [info["build_ms"]]
     for _ in range(0 if args.ncu else 3):
-        s2 = SceneRT(ctx, layout=args.layout)
-        g2 = s2.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+        s2, g2 = make_scene(args.layout)
         build_ms.append(s2.geom_info(g2)["build_ms"])
         s2.close()
 
@@ -624,6 +779,12 @@ def run_engine(args):
     node_bytes = LAYOUT_NODE_BYTES[args.layout]
     eye_bytes = node_bytes * eye_pairs + TRI_BYTES * eye_tris + RAY_BYTES * n_eye + 32 * n_eye
     ao_bytes = node_bytes * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
+
+    tuned = None
+    if not args.no_autotune and not args.ncu:
+        tuned = {}
+        for kind, (dr, n, do) in enumerate(((d_eye, n_eye, d_hits), (d_ao, n_ao, d_any))):
+            tuned[kind], _ = scene.autotune(E.query_desc(kind, dr.data_ptr(), n, do.data_ptr()), 3)
 
     def step(ev=None):
         if ev:
@@ -697,6 +858,36 @@ def run_engine(args):
     for b in (pin_eye, pin_ao, pin_hits, pin_any):
         b.free()
 
+    # plain: the binary FP32 tree (the reference's decisions) with the default launch shape
+    plain = None
+    if not args.no_plain:
+        ps, _ = make_scene("bvh2")
+        p_hits = torch.empty_like(d_hits)
+        p_any = torch.empty_like(d_any)
+        for _ in range(3):
+            ps.query_device(0, d_eye.data_ptr(), n_eye, p_hits.data_ptr(), sh)
+            ps.query_device(1, d_ao.data_ptr(), n_ao, p_any.data_ptr(), sh)
+        torch.cuda.synchronize()
+        pe = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        for k in range(args.steps):
+            pe[k][0].record(stream)
+            ps.query_device(0, d_eye.data_ptr(), n_eye, p_hits.data_ptr(), sh)
+            pe[k][1].record(stream)
+            ps.query_device(1, d_ao.data_ptr(), n_ao, p_any.data_ptr(), sh)
+            pe[k][2].record(stream)
+        torch.cuda.synchronize()
+        pe_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in pe)
+        pa_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in pe)
+        hp = p_hits.cpu().numpy().view(np.uint32)
+        hq = d_hits.cpu().numpy().view(np.uint32)
+        diff = np.any(hp != hq, axis=1)
+        plain = {"layout": LAYOUT_DESC["bvh2"], "eye_ms": round(pe_ms, 4), "ao_ms": round(pa_ms, 4),
+                 "mrays_s": round((n_eye + n_ao) / (pe_ms + pa_ms) / 1e3, 2),
+                 "nearest_mismatch": int(np.count_nonzero(diff & (hp[:, 0] != hq[:, 0]))),
+                 "nearest_equal_t_other_triangle": int(np.count_nonzero(diff & (hp[:, 0] == hq[:, 0]))),
+                 "anyhit_mismatch": int(np.count_nonzero(p_any.cpu().numpy() != d_any.cpu().numpy()))}
+        ps.close()
+
     # roofline of the dominant kernel
     eye_avg, ao_avg = statistics.mean(eye_ms), statistics.mean(ao_ms)
     if ao_avg >= eye_avg:
@@ -731,12 +922,19 @@ def run_engine(args):
                              "node fetches mostly hit L1/L2, so frac can exceed 1 (see traffic)"},
         "clocks": clk,
     }
+    line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
+    line["config"]["launch"] = tuned if tuned is not None else "default"
+    if plain is not None:
+        line["plain"] = plain
+        line["speedup_vs_plain"] = round(line["value"] / plain["mrays_s"], 3)
 
     if not args.no_batched:
         line["batched"] = run_batched(ctx, args)
         line["gpu_launches_batched_per_step"] = 2
     if not args.no_served:
         line["served"] = run_served(ctx, args)
+    if not args.no_precision:
+        line["precision"] = run_precision(ctx, args)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as orc
 
