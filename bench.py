@@ -58,6 +58,9 @@ def parse():
                    help="node layout of the headline scene (binary FP32, 4-wide FP32/FP16/8-bit)")
     p.add_argument("--merge", type=int, default=1, help="BVH4 leaf merge bound of the headline scene")
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    p.add_argument("--launch-nearest", default=None,
+                   help="launch shape of the nearest-hit kernel, 'threads,persistent,steps,lanes' (skips its tuning)")
+    p.add_argument("--launch-any", default=None, help="launch shape of the any-hit kernel (as --launch-nearest)")
     p.add_argument("--no-plain", action="store_true", help="skip the plain BVH2 FP32 comparison")
     p.add_argument("--ncu", action="store_true",
                    help="profiling run: setup, warm-up and timed steps only (no extra builds, counters, e2e, CPU)")
@@ -781,10 +784,15 @@ def run_engine(args):
     ao_bytes = node_bytes * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
 
     tuned = None
-    if not args.no_autotune and not args.ncu:
+    fixed = {0: args.launch_nearest, 1: args.launch_any}
+    if any(fixed.values()) or (not args.no_autotune and not args.ncu):
         tuned = {}
         for kind, (dr, n, do) in enumerate(((d_eye, n_eye, d_hits), (d_ao, n_ao, d_any))):
-            tuned[kind], _ = scene.autotune(E.query_desc(kind, dr.data_ptr(), n, do.data_ptr()), 3)
+            if fixed[kind]:
+                scene.set_trace_config(kind, *[int(x) for x in fixed[kind].split(",")])
+                tuned[kind] = scene.trace_config(kind)
+            elif not args.no_autotune and not args.ncu:
+                tuned[kind], _ = scene.autotune(E.query_desc(kind, dr.data_ptr(), n, do.data_ptr()), 3)
 
     def step(ev=None):
         if ev:
