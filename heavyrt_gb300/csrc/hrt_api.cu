@@ -2,6 +2,7 @@
 // instances and batched queries.  Host-side bookkeeping mirrors
 // BVH2CommonRT's (core/BVH2CommonRT.h:70-87, core/BVH2CommonRT_host.cpp); every
 // array it keeps lives in device memory.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -517,6 +518,79 @@ void make_instance_desc(const Geom& g, uint32_t geomId, uint32_t instId, const f
   std::memcpy(d.inv, inv12 ? inv12 : id12, sizeof(d.inv));
 }
 
+// World-space box of an instance: the geometry's box corners under the
+// instance matrix, evaluated in double, rounded outward to float and widened
+// by a relative margin that covers the rounding of the rays' transform into
+// the instance.
+void instance_world_box(const Geom& g, const float* m, float* mn, float* mx)
+{
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int corner = 0; corner < 8; corner++)
+  {
+    const double p[3] = {g.box[(corner & 1) ? 4 : 0], g.box[(corner & 2) ? 5 : 1], g.box[(corner & 4) ? 6 : 2]};
+    for (int r = 0; r < 3; r++)
+    {
+      const double v = (double)m[r] * p[0] + (double)m[4 + r] * p[1] + (double)m[8 + r] * p[2] + (double)m[12 + r];
+      lo[r] = std::min(lo[r], v);
+      hi[r] = std::max(hi[r], v);
+    }
+  }
+  for (int r = 0; r < 3; r++)
+  {
+    const double margin = 1e-5 * (hi[r] - lo[r]) + 1e-6 * std::max(std::fabs(lo[r]), std::fabs(hi[r])) + 1e-30;
+    mn[r] = std::nextafter((float)(lo[r] - margin), -INFINITY);
+    mx[r] = std::nextafter((float)(hi[r] + margin), INFINITY);
+  }
+}
+
+// Instance tree of the scene's instances with triangles: one pseudo-triangle
+// per instance (min corner, max corner, max corner) whose box is the
+// instance's world box, built by the geometry LBVH build in the binary
+// layout.  Triangle record e1.w (the pseudo-triangle's index) is rewritten to
+// the instance id.  Leaves may hold more than 127 instances (coincident
+// instances share a Morton code): the traversal ends a leaf at its flagged
+// record, so only the exported LR leaf count would overflow.
+int build_tlas(hrt_scene* s)
+{
+  std::vector<uint32_t> ids;
+  for (size_t i = 0; i < s->insts.size(); i++)
+    if (s->geoms[s->insts[i].geomId].nTris > 0) ids.push_back((uint32_t)i);
+  const size_t n = ids.size();
+  if (n == 0) return HRT_OK;  // nothing to hit
+  std::vector<float> v(12 * n);
+  std::vector<uint32_t> idx(3 * n);
+  for (size_t j = 0; j < n; j++)
+  {
+    const Instance& in = s->insts[ids[j]];
+    float mn[3], mx[3];
+    instance_world_box(s->geoms[in.geomId], in.m, mn, mx);
+    for (int r = 0; r < 3; r++)
+    {
+      v[12 * j + r] = mn[r];
+      v[12 * j + 4 + r] = mx[r];
+      v[12 * j + 8 + r] = mx[r];
+    }
+    v[12 * j + 3] = v[12 * j + 7] = v[12 * j + 11] = 1.0f;
+    for (int c = 0; c < 3; c++) idx[3 * j + c] = (uint32_t)(3 * j + c);
+  }
+  int st = build_geometry(s, s->tlas, v.data(), 3 * n, idx.data(), 3 * n, 16, HRT_LAYOUT_BVH2);
+  if (st == HRT_ERR_CAPACITY && (s->tlas.host.error & ~kErrLeafCount) == 0 && s->tlas.nLeaves > 0 &&
+      s->tlas.nLeaves <= n)
+    st = HRT_OK;
+  if (st != HRT_OK) return st;
+  std::vector<TriRec> tr(n);
+  HRT_CUDA(s->ctx, cudaMemcpy(tr.data(), s->tlas.tris, sizeof(TriRec) * n, cudaMemcpyDeviceToHost));
+  for (TriRec& r : tr)
+  {
+    uint32_t k;
+    std::memcpy(&k, &r.e1.w, 4);
+    if (k >= n) return fail(s->ctx, HRT_ERR_DEVICE_CHECK, "instance tree record out of range");
+    std::memcpy(&r.e1.w, &ids[k], 4);
+  }
+  HRT_CUDA(s->ctx, cudaMemcpy(s->tlas.tris, tr.data(), sizeof(TriRec) * n, cudaMemcpyHostToDevice));
+  return HRT_OK;
+}
+
 bool lbvh_builder_name(const char* name)
 {
   if (!name || !*name) return true;
@@ -568,6 +642,11 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
   a.rayOffsets = q.rayOffsets;
   a.segInst = q.segInst;
   a.nSeg = q.nSeg;
+  if (s->tlas.nTris > 0)
+  {
+    a.tlasRecs = s->tlas.recs;
+    a.tlasTris = s->tlas.tris;
+  }
   cudaError_t e = trace(a, kind, counting, s->layout, s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
@@ -662,6 +741,7 @@ int hrt_clear_geom(hrt_scene* s)
   cudaSetDevice(s->ctx->device);
   cudaStreamSynchronize(s->ctx->stream);
   for (Geom& gm : s->geoms) free_geom(gm);
+  free_geom(s->tlas);
   for (void* p : s->batchAllocs) cudaFree(p);
   s->batchAllocs.clear();
   s->geoms.clear();
@@ -767,6 +847,9 @@ int hrt_clear_scene(hrt_scene* s)
 {
   if (!s) return HRT_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> g(s->mu);
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
+  free_geom(s->tlas);
   s->insts.clear();
   s->committed = false;
   return HRT_OK;
@@ -824,6 +907,17 @@ int hrt_commit_scene(hrt_scene* s, int quality)
   {
     const Instance& in = s->insts[i];
     make_instance_desc(s->geoms[in.geomId], in.geomId, (uint32_t)i, in.identity ? nullptr : in.inv, d[i]);
+  }
+  free_geom(s->tlas);
+  if (s->useTlas && s->insts.size() >= 2)
+  {
+    const int st = build_tlas(s);
+    if (st != HRT_OK)
+    {
+      cudaStreamSynchronize(ctx->stream);
+      free_geom(s->tlas);
+      return st;
+    }
   }
   if (s->dInst) cudaFree(s->dInst);
   s->dInst = nullptr;
@@ -1032,6 +1126,11 @@ int hrt_scene_set_option(hrt_scene* s, int option, int value)
     case HRT_OPTION_BVH4_MERGE:
       if (value < 0 || value > 64) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "BVH4 merge value out of range");
       s->bvh4Merge = value;
+      return HRT_OK;
+    case HRT_OPTION_TLAS:
+      if (value != 0 && value != 1) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "TLAS option is 0 or 1");
+      s->useTlas = value;
+      s->committed = false;
       return HRT_OK;
     default: return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown option");
   }

@@ -75,6 +75,8 @@ struct hrt_scene
   bool                  committed = false;
   int                   layout = HRT_LAYOUT_BVH2;
   int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
+  int                   useTlas = 1;    // HRT_OPTION_TLAS
+  Geom                  tlas;           // instance tree of the committed scene (nTris = 0: none)
   InstanceDesc*         dInst = nullptr;
   uint32_t              nInstDev = 0;
   uint32_t*             dError = nullptr;

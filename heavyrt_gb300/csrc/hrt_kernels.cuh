@@ -152,6 +152,10 @@ struct TraceArgs
   const uint32_t*     rayOffsets = nullptr;
   const uint32_t*     segInst = nullptr;
   uint32_t            nSeg = 0;
+  // instance tree (optional): binary LBVH over the instances' world boxes;
+  // its triangle records' e1.w hold instance ids
+  const PairRec*      tlasRecs = nullptr;
+  const TriRec*       tlasTris = nullptr;
 };
 
 // Launch shape of the traversal (tuned per workload).

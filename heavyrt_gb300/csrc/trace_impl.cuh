@@ -44,9 +44,23 @@ constexpr int      kStack2 = 32;
 constexpr int      kStack4 = 48;
 constexpr uint32_t kNoRay = 0xFFFFFFFFu;
 
-template <int LAYOUT> struct StackDepth
+// With a TLAS the instance tree's entries sit below the geometry's on the
+// same stack (at most kStack2 of them: the TLAS is a binary LBVH).
+template <int LAYOUT, bool TLAS = false> struct StackDepth
 {
-  static constexpr int value = LAYOUT == 0 ? kStack2 : kStack4;
+  static constexpr int value = (LAYOUT == 0 ? kStack2 : kStack4) + (TLAS ? kStack2 : 0);
+};
+
+constexpr uint32_t kTlasMode = 0xFFFFFFFEu;  // Lane::inst while the lane walks the instance tree
+
+// Instance tree (TLAS): a binary LBVH over the instances' world-space boxes,
+// built like a geometry's tree from one pseudo-triangle per instance; a leaf
+// is a run of sorted records whose e1.w holds the instance id.
+struct Tlas
+{
+  const PairRec* recs;  // nullptr: no TLAS, instances are taken in order
+  const TriRec*  tris;
+  uint32_t       nInst;
 };
 
 struct Ray
@@ -248,6 +262,8 @@ struct Lane
   uint32_t instEnd;   // one past the last instance this ray is traced against
   uint32_t cur;       // current record / leaf reference
   int      top;       // stack depth
+  int      base;      // stack depth at which the current instance's traversal began
+  uint32_t tnext;     // next record of the current TLAS leaf run, or kNoRay
   uint32_t budget;    // steps left for this ray
 };
 
@@ -283,6 +299,7 @@ __device__ __forceinline__ bool begin_instance(Lane& L, const InstanceDesc* __re
       make_ray(inst[k], L.po, L.di, L.r);
       L.cur = 0;  // record 0 = the root's two children
       L.top = 0;
+      L.base = 0;
       return true;
     }
   return false;
@@ -297,7 +314,41 @@ template <int LAYOUT> struct EndBit
 // nearest hit child (child 0 on equal entry distance) and pushes the others,
 // farthest first.  Returns 1 when no child is hit (the caller pops), 0
 // otherwise, -1 when the stack bound would be exceeded (reported).
-template <int LAYOUT, bool COUNT, int THREADS>
+// One child pair of a binary tree: BVH2TraverseC32's decisions
+// (core/BVH2CommonRT.cpp:88-113).
+template <bool COUNT, int THREADS, int DEPTH>
+__device__ __forceinline__ int visit_pair(Lane& L, const PairRec* __restrict__ recs, uint32_t* __restrict__ stack,
+                                          uint64_t& nPairs, uint32_t* errorWord)
+{
+  const float4* p = reinterpret_cast<const float4*>(recs + L.cur);
+  const float4 a = __ldg(p + 0);
+  const float4 b = __ldg(p + 1);
+  const float4 c = __ldg(p + 2);
+  const uint4 e = __ldg(reinterpret_cast<const uint4*>(p + 3));
+  if (COUNT) nPairs++;
+  float t0n, t0f, t1n, t1f;
+  slab(L.r, a.x, a.y, a.z, a.w, b.x, b.y, t0n, t0f);
+  slab(L.r, b.z, b.w, c.x, c.y, c.z, c.w, t1n, t1f);
+  const bool h0 = (t0n <= t0f) && (t0f >= L.r.tNear) && (t0n <= L.h.t);
+  const bool h1 = (t1n <= t1f) && (t1f >= L.r.tNear) && (t1n <= L.h.t);
+  if (!h0 && !h1) return 1;
+  L.cur = h0 ? e.x : e.y;
+  if (h0 && h1)
+  {
+    const bool first0 = (t0n <= t1n);
+    L.cur = first0 ? e.x : e.y;
+    if (L.top >= DEPTH)
+    {
+      atomicOr(errorWord, kErrStack);
+      return -1;
+    }
+    stack[L.top * THREADS] = first0 ? e.y : e.x;
+    L.top++;
+  }
+  return 0;
+}
+
+template <int LAYOUT, bool COUNT, int THREADS, int DEPTH>
 __device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32_t* __restrict__ stack,
                                           uint64_t& nPairs, uint32_t* errorWord)
 {
@@ -332,7 +383,7 @@ __device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32
     for (int k = 3; k >= 1; k--)
       if (k > f && ref[k] != kEmptyRef)
       {
-        if (L.top >= kStack4)
+        if (L.top >= DEPTH)
         {
           atomicOr(errorWord, kErrStack);
           return -1;
@@ -343,48 +394,92 @@ __device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32
     return 0;
   }
   else
-  {
-    // child pair: BVH2TraverseC32's decisions (core/BVH2CommonRT.cpp:88-113)
-    const float4* p = reinterpret_cast<const float4*>(d.recs + L.cur);
-    const float4 a = __ldg(p + 0);
-    const float4 b = __ldg(p + 1);
-    const float4 c = __ldg(p + 2);
-    const uint4 e = __ldg(reinterpret_cast<const uint4*>(p + 3));
-    if (COUNT) nPairs++;
-    float t0n, t0f, t1n, t1f;
-    slab(L.r, a.x, a.y, a.z, a.w, b.x, b.y, t0n, t0f);
-    slab(L.r, b.z, b.w, c.x, c.y, c.z, c.w, t1n, t1f);
-    const bool h0 = (t0n <= t0f) && (t0f >= L.r.tNear) && (t0n <= L.h.t);
-    const bool h1 = (t1n <= t1f) && (t1f >= L.r.tNear) && (t1n <= L.h.t);
-    if (!h0 && !h1) return 1;
-    L.cur = h0 ? e.x : e.y;
-    if (h0 && h1)
-    {
-      const bool first0 = (t0n <= t1n);
-      L.cur = first0 ? e.x : e.y;
-      if (L.top >= kStack2)
-      {
-        atomicOr(errorWord, kErrStack);
-        return -1;
-      }
-      stack[L.top * THREADS] = first0 ? e.y : e.x;
-      L.top++;
-    }
-    return 0;
-  }
+    return visit_pair<COUNT, THREADS, DEPTH>(L, d.recs, stack, nPairs, errorWord);
 }
 
 // One traversal step (an internal node, or a leaf followed by a pop).
 // Returns true when the lane's ray is finished.
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
-__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
+// Ray of the lane in world space (the instance tree is not transformed).
+__device__ __forceinline__ void world_ray(Lane& L)
+{
+  L.r.tNear = L.po.w;
+  L.r.ox = L.po.x; L.r.oy = L.po.y; L.r.oz = L.po.z;
+  L.r.dx = L.di.x; L.r.dy = L.di.y; L.r.dz = L.di.z;
+  L.r.ix = safe_inv(L.r.dx);
+  L.r.iy = safe_inv(L.r.dy);
+  L.r.iz = safe_inv(L.r.dz);
+}
+
+__device__ __forceinline__ void tlas_begin(Lane& L)
+{
+  L.inst = kTlasMode;
+  world_ray(L);
+  L.cur = 0;
+  L.top = 0;
+  L.base = 0;
+  L.tnext = kNoRay;
+}
+
+// Pops the instance tree's stack; true when the ray is finished.
+template <int THREADS>
+__device__ __forceinline__ bool tlas_pop(Lane& L, const uint32_t* __restrict__ stack)
+{
+  if (L.top == 0) return true;
+  L.top--;
+  L.cur = stack[L.top * THREADS];
+  return false;
+}
+
+// Enters the next instance (with triangles) of the current TLAS leaf run; when
+// the run is done, returns to the instance tree.  True when the ray is finished.
+template <int THREADS>
+__device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
+                                          const uint32_t* __restrict__ stack)
+{
+  while (L.tnext != kNoRay)
+  {
+    const float4* q = reinterpret_cast<const float4*>(tl.tris + L.tnext);
+    const uint32_t flags = __float_as_uint(__ldg(q).w);
+    const uint32_t k = __float_as_uint(__ldg(q + 1).w);
+    L.tnext = (flags & 1u) ? kNoRay : L.tnext + 1;
+    if (k < tl.nInst && inst[k].valid)
+    {
+      L.inst = k;
+      make_ray(inst[k], L.po, L.di, L.r);
+      L.base = L.top;
+      L.cur = 0;
+      return false;
+    }
+  }
+  L.inst = kTlasMode;
+  world_ray(L);
+  return tlas_pop<THREADS>(L, stack);
+}
+
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
+__device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
+                                     uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
                                      uint32_t* errorWord)
 {
+  constexpr int DEPTH = StackDepth<LAYOUT, TLAS>::value;
+  if (TLAS && L.inst == kTlasMode)
+  {
+    // instance tree: a pair of instance boxes, or a leaf (a run of instances)
+    if ((L.cur & kLeafBit) == 0u)
+    {
+      const int r = visit_pair<COUNT, THREADS, DEPTH>(L, tl.recs, stack, nPairs, errorWord);
+      if (r < 0) return true;
+      return r == 1 ? tlas_pop<THREADS>(L, stack) : false;
+    }
+    if (L.cur == kEmptyRef) return tlas_pop<THREADS>(L, stack);
+    L.tnext = L.cur & ~kLeafBit;
+    return tlas_next<THREADS>(L, inst, tl, stack);
+  }
   const InstanceDesc& d = inst[L.inst];
   bool pop;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, COUNT, THREADS>(L, d, stack, nPairs, errorWord);
+    const int r = visit_node<LAYOUT, COUNT, THREADS, DEPTH>(L, d, stack, nPairs, errorWord);
     if (r < 0) return true;
     pop = (r == 1);
   }
@@ -397,9 +492,14 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
   }
   if (pop)
   {
-    L.top--;
-    if (L.top < 0) return !begin_instance(L, inst, L.inst + 1);
-    L.cur = stack[L.top * THREADS];
+    if (L.top > L.base)
+    {
+      L.top--;
+      L.cur = stack[L.top * THREADS];
+      return false;
+    }
+    if (TLAS) return tlas_next<THREADS>(L, inst, tl, stack);
+    return !begin_instance(L, inst, L.inst + 1);
   }
   return false;
 }
@@ -478,13 +578,13 @@ __device__ __forceinline__ void flush_counters(uint64_t nPairs, uint64_t nTris, 
 
 // Persistent warp pool.  Lanes run `steps` traversal steps between refills; a
 // warp refills when at least `refill` lanes are idle (or all are).
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
 __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict__ rays, uint32_t n,
-                                                        const InstanceDesc* __restrict__ inst, Segments sg, void* out,
-                                                        unsigned long long* counters, uint32_t* errorWord,
+                                                        const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
+                                                        void* out, unsigned long long* counters, uint32_t* errorWord,
                                                         unsigned int* rayCounter, int steps, int refill)
 {
-  __shared__ uint32_t s_stack[StackDepth<LAYOUT>::value * THREADS];
+  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT, TLAS>::value * THREADS entries
   uint32_t* stack = s_stack + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ltMask = (1u << lane) - 1u;
@@ -508,7 +608,10 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
         if (i < n)
         {
           start_ray(L, i, rays);
-          if (!begin_instance(L, inst, first_instance(L, i, sg)))
+          bool live = true;
+          if (TLAS) tlas_begin(L);
+          else live = begin_instance(L, inst, first_instance(L, i, sg));
+          if (!live)
           {
             write_result<ANY>(L, out);
             L.ray = kNoRay;
@@ -521,7 +624,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
       for (int s = 0; s < steps; s++)
       {
         if (out_of_budget(L, errorWord) ||
-            step<LAYOUT, ANY, COUNT, THREADS>(L, inst, stack, nPairs, nTris, errorWord))
+            step<LAYOUT, ANY, COUNT, THREADS, TLAS>(L, inst, tl, stack, nPairs, nTris, errorWord))
         {
           write_result<ANY>(L, out);
           L.ray = kNoRay;
@@ -534,12 +637,12 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
 }
 
 // One thread per ray.
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
 __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict__ rays, uint32_t n,
-                                                        const InstanceDesc* __restrict__ inst, Segments sg, void* out,
-                                                        unsigned long long* counters, uint32_t* errorWord)
+                                                        const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
+                                                        void* out, unsigned long long* counters, uint32_t* errorWord)
 {
-  __shared__ uint32_t s_stack[StackDepth<LAYOUT>::value * THREADS];
+  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT, TLAS>::value * THREADS entries
   uint32_t* stack = s_stack + threadIdx.x;
   uint64_t nPairs = 0, nTris = 0;
   const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
@@ -547,24 +650,39 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
   {
     Lane L;
     start_ray(L, i, rays);
-    if (begin_instance(L, inst, first_instance(L, i, sg)))
+    bool live = true;
+    if (TLAS) tlas_begin(L);
+    else live = begin_instance(L, inst, first_instance(L, i, sg));
+    if (live)
       while (!out_of_budget(L, errorWord) &&
-             !step<LAYOUT, ANY, COUNT, THREADS>(L, inst, stack, nPairs, nTris, errorWord)) {}
+             !step<LAYOUT, ANY, COUNT, THREADS, TLAS>(L, inst, tl, stack, nPairs, nTris, errorWord)) {}
     write_result<ANY>(L, out);
   }
   flush_counters<COUNT>(nPairs, nTris, counters);
 }
 
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS>
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
 cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   const uint32_t n = (uint32_t)a.n;
   const Segments sg{a.rayOffsets, a.segInst, a.nSeg, a.nInst};
+  const Tlas tl{a.tlasRecs, a.tlasTris, a.nInst};
+  // the short stack is dynamic shared memory: above 48 KB a block needs the opt-in attribute
+  constexpr size_t smem = sizeof(uint32_t) * StackDepth<LAYOUT, TLAS>::value * THREADS;
+  if (smem > 48 * 1024)
+  {
+    cudaError_t e = cudaFuncSetAttribute(k_trace_pool<LAYOUT, ANY, COUNT, THREADS, TLAS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_trace_grid<LAYOUT, ANY, COUNT, THREADS, TLAS>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   if (c.persistent && !COUNT)
   {
     int perSM = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_pool<LAYOUT, ANY, COUNT, THREADS>,
-                                                                  THREADS, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &perSM, k_trace_pool<LAYOUT, ANY, COUNT, THREADS, TLAS>, THREADS, smem);
     if (e != cudaSuccess) return e;
     if (perSM < 1) perSM = 1;
     uint64_t blocks = (uint64_t)numSMs * perSM;
@@ -572,36 +690,47 @@ cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStr
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    k_trace_pool<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(
-        a.rays, n, a.inst, sg, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes);
+    k_trace_pool<LAYOUT, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes);
   }
   else
   {
     const uint64_t blocks = ((uint64_t)n + THREADS - 1) / THREADS;
-    k_trace_grid<LAYOUT, ANY, COUNT, THREADS><<<(uint32_t)blocks, THREADS, 0, s>>>(a.rays, n, a.inst, sg, a.hits,
-                                                                                 a.counters, a.errorWord);
+    k_trace_grid<LAYOUT, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord);
   }
   return cudaGetLastError();
 }
 
-// Counting runs use the one-thread-per-ray grid at 128 threads: the counts do
-// not depend on the schedule.
-template <int LAYOUT>
-cudaError_t trace_layout(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
+template <int LAYOUT, bool TLAS>
+cudaError_t trace_tlas(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   if (counting)
-    return kind == 0 ? launch<LAYOUT, false, true, 128>(a, c, numSMs, s) : launch<LAYOUT, true, true, 128>(a, c, numSMs, s);
+    return kind == 0 ? launch<LAYOUT, false, true, 128, TLAS>(a, c, numSMs, s)
+                     : launch<LAYOUT, true, true, 128, TLAS>(a, c, numSMs, s);
   switch (c.threadsPerBlock)
   {
     case 64:
-      return kind == 0 ? launch<LAYOUT, false, false, 64>(a, c, numSMs, s) : launch<LAYOUT, true, false, 64>(a, c, numSMs, s);
+      return kind == 0 ? launch<LAYOUT, false, false, 64, TLAS>(a, c, numSMs, s)
+                       : launch<LAYOUT, true, false, 64, TLAS>(a, c, numSMs, s);
     case 256:
-      return kind == 0 ? launch<LAYOUT, false, false, 256>(a, c, numSMs, s)
-                       : launch<LAYOUT, true, false, 256>(a, c, numSMs, s);
+      return kind == 0 ? launch<LAYOUT, false, false, 256, TLAS>(a, c, numSMs, s)
+                       : launch<LAYOUT, true, false, 256, TLAS>(a, c, numSMs, s);
     default:
-      return kind == 0 ? launch<LAYOUT, false, false, 128>(a, c, numSMs, s)
-                       : launch<LAYOUT, true, false, 128>(a, c, numSMs, s);
+      return kind == 0 ? launch<LAYOUT, false, false, 128, TLAS>(a, c, numSMs, s)
+                       : launch<LAYOUT, true, false, 128, TLAS>(a, c, numSMs, s);
   }
+}
+
+// Counting runs use the one-thread-per-ray grid at 128 threads: the counts do
+// not depend on the schedule.  A scene with an instance tree uses the
+// two-level kernels, except in segmented queries (one instance per ray).
+template <int LAYOUT>
+cudaError_t trace_layout(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  if (a.tlasRecs != nullptr && a.rayOffsets == nullptr)
+    return trace_tlas<LAYOUT, true>(a, kind, counting, c, numSMs, s);
+  return trace_tlas<LAYOUT, false>(a, kind, counting, c, numSMs, s);
 }
 
 }  // namespace

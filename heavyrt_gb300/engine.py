@@ -278,6 +278,10 @@ class SceneRT:
         """0: the reference's leaf merge rule; M: merge subtrees of <= M triangles."""
         self.ctx.check(lib().hrt_scene_set_option(self._h, 1, int(value)), "set_option")
 
+    def set_tlas(self, enabled: bool):
+        """Instance tree over the instances (default on; takes effect at CommitScene)."""
+        self.ctx.check(lib().hrt_scene_set_option(self._h, 2, int(bool(enabled))), "set_option")
+
     @property
     def layout(self) -> int:
         v = C.c_int()

@@ -120,6 +120,15 @@ int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
  *                          M in 1..64: a subtree of at most M triangles becomes
  *                          one leaf (1 never merges). */
 #define HRT_OPTION_BVH4_MERGE 1
+/*   HRT_OPTION_TLAS        1 (default): hrt_commit_scene builds an instance tree
+ *                          (a binary LBVH over the instances' world-space boxes,
+ *                          the role of the reference's TLAS, core/BVH2CommonRT_host.cpp:118-129)
+ *                          when the scene has two or more instances, and queries
+ *                          traverse it and the instances' trees in one kernel;
+ *                          0: every instance is traversed in instance order.
+ *                          Results are the same either way, except which of two
+ *                          instances wins an exact tie in t. */
+#define HRT_OPTION_TLAS 2
 int hrt_scene_set_option(hrt_scene* scene, int option, int value);
 
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */
