@@ -352,4 +352,36 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
   return cudaGetLastError();
 }
 
+// Refit: the geometry's vertices moved, its triangles and their sorted order
+// did not.  Leaves, triangle records and the sorted index buffer are rewritten
+// from the new vertices in the existing order, the hierarchy's parent links are
+// recomputed from the unchanged codes, and the boxes refit bottom-up; the
+// Morton frame in params stays that of the build.  The geometry's new vertex
+// box goes to boxOut (bmin/bmax).
+cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, cudaStream_t s)
+{
+  const uint32_t N = b.nTris;
+  if (N == 0) return cudaSuccess;
+  float4* partial = (float4*)b.scratch;  // refit_scratch_bytes()
+  uint32_t* err = &b.params->error;
+  uint32_t pb = grid_for(b.nVerts, numSMs, 4);
+  if (pb > 1024) pb = 1024;
+  k_box_partial<<<pb, kThreads, 0, s>>>(b.verts, b.nVerts, partial);
+  k_box_final<<<1, 32, 0, s>>>(partial, pb, boxOut);
+  const uint32_t g = grid_for(N, numSMs, 8);
+  k_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vals, b.runStarts, N, b.nVerts, b.params, b.lr, b.tris, b.sortedIdx,
+                                  err);
+  cudaError_t e = cudaMemsetAsync(b.parent, 0xFF, sizeof(uint32_t) * (2 * (size_t)N - 1), s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);
+  if (e != cudaSuccess) return e;
+  k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent);
+  k_refit<<<g, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit);
+  k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
+  k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
+  return cudaGetLastError();
+}
+
+size_t refit_scratch_bytes() { return 2 * sizeof(float4) * 1024; }
+
 }  // namespace hrt

@@ -228,6 +228,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
     b4.scratch = scratch4;
     b4.mergeMode = s->bvh4Merge;
     b4.hostNodeCount = &count4;
+    g.bvh4Merge = s->bvh4Merge;
     HRT_CUDA(ctx, bvh4_plan(b4, ctx->numSMs, st));
     HRT_CUDA(ctx, cudaStreamSynchronize(st));
     if (count4 == 0) count4 = 1;  // a single leaf still gets a root node
@@ -461,6 +462,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
     const uint32_t Ni = ht[i + 1] - ht[i];
     const uint32_t Li = hLeaf[i + 1] - hLeaf[i];
     g.shared = true;
+    g.bvh4Merge = s->bvh4Merge;
     g.nTris = Ni;
     g.nVerts = hv[i + 1] - hv[i];
     g.nLeaves = Li;
@@ -588,6 +590,119 @@ int build_tlas(hrt_scene* s)
     std::memcpy(&r.e1.w, &ids[k], 4);
   }
   HRT_CUDA(s->ctx, cudaMemcpy(s->tlas.tris, tr.data(), sizeof(TriRec) * n, cudaMemcpyHostToDevice));
+  return HRT_OK;
+}
+
+// Copies nVert host vertices of `stride` bytes (xyz first) to float4 (w = 1) on the device.
+int upload_verts(hrt_context* ctx, cudaStream_t st, float4* dst, const float* vpos, uint64_t nVert, uint64_t stride)
+{
+  if (nVert == 0) return HRT_OK;
+  if (stride == 16) HRT_CUDA(ctx, cudaMemcpyAsync(dst, vpos, 16 * nVert, cudaMemcpyHostToDevice, st));
+  uint8_t* raw = nullptr;
+  if (stride != 16)
+  {
+    HRT_CUDA(ctx, cudaMallocAsync((void**)&raw, stride * nVert, st));
+    HRT_CUDA(ctx, cudaMemcpyAsync(raw, vpos, stride * nVert, cudaMemcpyHostToDevice, st));
+  }
+  uint64_t blocks = (nVert + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  k_pack_verts<<<(uint32_t)blocks, 256, 0, st>>>(raw ? raw : reinterpret_cast<const uint8_t*>(dst), nVert, stride, dst);
+  HRT_CUDA(ctx, cudaGetLastError());
+  if (raw) HRT_CUDA(ctx, cudaFreeAsync(raw, st));
+  return HRT_OK;
+}
+
+// Refit of geometry g to new vertex positions (same vertex and index counts,
+// same index buffer): the build's tree topology and sorted order are kept,
+// every box, triangle record and traversal record is recomputed, and a 4-wide
+// layout is collapsed again into the same node array.
+int refit_geometry(hrt_scene* s, Geom& g, const float* vpos, const uint32_t* idx, uint64_t stride)
+{
+  hrt_context* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  const uint32_t N = g.nTris;
+  int rc = upload_verts(ctx, st, g.verts, vpos, g.nVerts, stride);
+  if (rc != HRT_OK) return rc;
+  if (N == 0)
+  {
+    HRT_CUDA(ctx, cudaStreamSynchronize(st));
+    return HRT_OK;
+  }
+  uint32_t *dIdx = nullptr, *parent = nullptr, *visit = nullptr;
+  BuildParams* box = nullptr;
+  void* scratch = nullptr;
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&dIdx, sizeof(uint32_t) * 3 * (size_t)N, st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * 3 * (size_t)N, cudaMemcpyHostToDevice, st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * (2 * (size_t)N - 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * N, st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&box, sizeof(BuildParams), st));
+  HRT_CUDA(ctx, cudaMallocAsync(&scratch, refit_scratch_bytes(), st));
+  HRT_CUDA(ctx, cudaMemsetAsync(&g.params->error, 0, sizeof(uint32_t), st));
+  BuildBuffers b{};
+  b.verts = g.verts;
+  b.idx = dIdx;
+  b.nVerts = g.nVerts;
+  b.nTris = N;
+  b.vals = g.vals;
+  b.compressed = g.compressed;
+  b.runStarts = g.runStarts;
+  b.lr = g.lr;
+  b.lrCount = g.lrCount;
+  b.parent = parent;
+  b.visit = visit;
+  b.recs = g.recs;
+  b.tris = g.tris;
+  b.sortedIdx = g.sortedIdx;
+  b.params = g.params;
+  b.scratch = scratch;
+  cudaEvent_t e0, e1;
+  HRT_CUDA(ctx, cudaEventCreate(&e0));
+  HRT_CUDA(ctx, cudaEventCreate(&e1));
+  HRT_CUDA(ctx, cudaEventRecord(e0, st));
+  cudaError_t e = refit_lbvh(b, box, ctx->numSMs, st);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "refit_lbvh");
+  if (s->layout != HRT_LAYOUT_BVH2)
+  {
+    void* scratch4 = nullptr;
+    uint32_t count4 = 0;
+    HRT_CUDA(ctx, cudaMallocAsync(&scratch4, bvh4_scratch_bytes(N), st));
+    Bvh4Buffers b4;
+    b4.nTris = N;
+    b4.params = g.params;
+    b4.lr = g.lr;
+    b4.runStarts = g.runStarts;
+    b4.parent = parent;
+    b4.tris = g.tris;
+    b4.scratch = scratch4;
+    b4.mergeMode = g.bvh4Merge;
+    b4.hostNodeCount = &count4;
+    HRT_CUDA(ctx, bvh4_plan(b4, ctx->numSMs, st));
+    HRT_CUDA(ctx, cudaStreamSynchronize(st));
+    if (count4 == 0) count4 = 1;
+    if (count4 != g.nNodes4) return fail(ctx, HRT_ERR_DEVICE_CHECK, "refit changed the 4-wide node count");
+    HRT_CUDA(ctx, bvh4_emit(b4, s->layout - 1, g.nodes4, count4, ctx->numSMs, st));
+    HRT_CUDA(ctx, cudaFreeAsync(scratch4, st));
+  }
+  HRT_CUDA(ctx, cudaEventRecord(e1, st));
+  BuildParams hb{}, hp{};
+  HRT_CUDA(ctx, cudaMemcpyAsync(&hb, box, sizeof(BuildParams), cudaMemcpyDeviceToHost, st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(&hp, g.params, sizeof(BuildParams), cudaMemcpyDeviceToHost, st));
+  HRT_CUDA(ctx, cudaFreeAsync(dIdx, st));
+  HRT_CUDA(ctx, cudaFreeAsync(parent, st));
+  HRT_CUDA(ctx, cudaFreeAsync(visit, st));
+  HRT_CUDA(ctx, cudaFreeAsync(box, st));
+  HRT_CUDA(ctx, cudaFreeAsync(scratch, st));
+  HRT_CUDA(ctx, cudaStreamSynchronize(st));
+  cudaEventElapsedTime(&g.buildMs, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (hp.error & kErrIndexRange) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "triangle index >= vertex count");
+  if (hp.error & (kErrLayout | kErrLeafCount)) return fail(ctx, HRT_ERR_DEVICE_CHECK, "inconsistent tree after refit");
+  for (int c = 0; c < 4; c++)
+  {
+    g.box[c] = hb.bmin[c];
+    g.box[4 + c] = hb.bmax[c];
+  }
   return HRT_OK;
 }
 
@@ -837,10 +952,46 @@ int hrt_add_geoms_triangles3f_batched(hrt_scene* s, uint32_t count, const float*
   return HRT_OK;
 }
 
-int hrt_update_geom_triangles3f(hrt_scene* s, uint32_t, const float*, uint64_t, const uint32_t*, uint64_t, int, uint64_t)
+int hrt_update_geom_triangles3f(hrt_scene* s, uint32_t geomId, const float* vpos, uint64_t nVert, const uint32_t* idx,
+                                uint64_t nIdx, int quality, uint64_t vByteStride)
 {
   if (!s) return HRT_ERR_INVALID_ARGUMENT;
-  return fail(s->ctx, HRT_ERR_UNSUPPORTED, "UpdateGeom_Triangles3f is not provided (the reference stubs it too)");
+  hrt_context* ctx = s->ctx;
+  if (vByteStride == 0) vByteStride = 12;
+  if (vByteStride < 12 || vByteStride % 4 != 0)
+    return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "vByteStride must be >= 12 and a multiple of 4");
+  if (nIdx % 3 != 0) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "index count is not a multiple of 3");
+  if ((nVert && !vpos) || (nIdx && !idx)) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "null vertex or index pointer");
+  if (nIdx / 3 > HRT_MAX_TRIS_PER_GEOM) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^24-1 triangles in one geometry");
+  if (nVert > 0xFFFFFFFFull) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^32-1 vertices in one geometry");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (geomId >= s->geoms.size()) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "unknown geometry id");
+  cudaSetDevice(ctx->device);
+  Geom& g = s->geoms[geomId];
+  int st;
+  if (quality == HRT_BUILD_REFIT)
+  {
+    if (nVert != g.nVerts || nIdx != 3 * (uint64_t)g.nTris)
+      return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "a refit keeps the geometry's vertex and index counts");
+    st = refit_geometry(s, g, vpos, idx, vByteStride);
+  }
+  else
+  {
+    if (g.shared)
+      return fail(ctx, HRT_ERR_UNSUPPORTED, "a batch-built geometry can only be refit (BUILD_REFIT)");
+    Geom ng;
+    st = build_geometry(s, ng, vpos, nVert, idx, nIdx, vByteStride, s->layout);
+    cudaStreamSynchronize(ctx->stream);
+    if (st == HRT_OK)
+    {
+      free_geom(g);
+      g = ng;
+    }
+    else
+      free_geom(ng);
+  }
+  s->committed = false;  // instance descriptors and the instance tree see the new geometry at the next commit
+  return st;
 }
 
 int hrt_clear_scene(hrt_scene* s)

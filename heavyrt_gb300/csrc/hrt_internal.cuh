@@ -49,6 +49,7 @@ struct Geom
   void*        nodes4 = nullptr;  // 4-wide nodes of the scene's layout
   uint32_t     nNodes4 = 0;
   bool         shared = false;    // arrays point into a batch allocation (hrt_add_geoms_triangles3f_batched)
+  int          bvh4Merge = 0;     // leaf merge bound the 4-wide nodes were built with
 };
 
 struct Instance

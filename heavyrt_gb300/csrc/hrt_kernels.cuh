@@ -56,6 +56,14 @@ size_t build_scratch_bytes(uint32_t nTris);
 // Runs the whole LBVH build asynchronously on `stream`.  Errors found on the
 // device are ORed into params->error.
 cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t stream);
+// Refit of a built LBVH after its vertices moved (same triangles, same sorted
+// order): leaves, triangle records, hierarchy links, boxes and records are
+// recomputed; keys, codes and runs are kept.  Uses b.verts, b.idx, b.nVerts,
+// b.nTris, b.vals, b.compressed, b.runStarts, b.lr, b.lrCount, b.parent,
+// b.visit, b.recs, b.tris, b.sortedIdx, b.params and b.scratch
+// (refit_scratch_bytes()); the new vertex box is written to boxOut.
+size_t refit_scratch_bytes();
+cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, cudaStream_t stream);
 
 // ---------------------------------------------------------------- build_batch.cu
 // G geometries built together.  Geometry s owns vertices

@@ -142,9 +142,17 @@ int hrt_clear_geom(hrt_scene* scene);
 int hrt_add_geom_triangles3f(hrt_scene* scene, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
                              int quality, uint64_t vByteStride, uint32_t* geomId);
 
-/* ISceneObject::UpdateGeom_Triangles3f (core/CrossRT.h:105).  The reference
- * stubs it (core/BVH2CommonRT_host.cpp:100-103); here it returns
- * HRT_ERR_UNSUPPORTED. */
+/* ISceneObject::UpdateGeom_Triangles3f (core/CrossRT.h:105; every reference
+ * implementation stubs it, e.g. core/BVH2CommonRT_host.cpp:100-103).
+ *   quality == HRT_BUILD_REFIT: the vertices moved, the triangles did not
+ *     (same vertex and index counts, same index buffer): the tree's topology
+ *     and sorted order are kept and every box and record is recomputed on the
+ *     GPU (the reference's BUILD_REFIT intent, core/CrossRT.h:13); works for
+ *     batch-built geometries too.
+ *   any other quality: the geometry is rebuilt from the new arrays (any size)
+ *     under the same id.
+ * Either way the scene must be committed again before the next query (the
+ * instance tree and descriptors follow the new geometry). */
 int hrt_update_geom_triangles3f(hrt_scene* scene, uint32_t geomId, const float* vpos, uint64_t nVert,
                                 const uint32_t* idx, uint64_t nIdx, int quality, uint64_t vByteStride);
 
