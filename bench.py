@@ -863,6 +863,42 @@ def run_engine(args):
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_value = world * rays_per_step / e2e_s / 1e6
     got_any = pin_any.array(np.uint8)[:n_ao].copy()
+
+    # the same frame with its rays made on the device: camera parameters in,
+    # eye hits and AO flags out (no ray crosses the host link)
+    pp = w.params
+    cap = n_eye * pp["ao_per_hit"]
+    g_eye = torch.empty((n_eye, 8), dtype=torch.float32, device="cuda")
+    g_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
+    g_ao = torch.empty((cap, 8), dtype=torch.float32, device="cuda")
+    g_any = torch.empty(cap, dtype=torch.uint8, device="cuda")
+
+    def raygen_step():
+        ctx.gen_pinhole_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, args.width, args.height, 0.0, 1e9,
+                             g_eye.data_ptr(), sh)
+        scene.query_device(0, g_eye.data_ptr(), n_eye, g_hits.data_ptr(), sh)
+        k = scene.gen_ao_rays(pp["ao_seed"], g_eye.data_ptr(), g_hits.data_ptr(), n_eye, pp["ao_per_hit"],
+                              pp["ao_length"], pp["ao_offset"], g_ao.data_ptr(), cap, 0, sh)
+        scene.query_device(1, g_ao.data_ptr(), k, g_any.data_ptr(), sh)
+        pin_hits_d.copy_(g_hits, non_blocking=True)
+        pin_any_d[:k].copy_(g_any[:k], non_blocking=True)
+        torch.cuda.synchronize()
+        return k
+
+    pin_hits_d = torch.empty((n_eye, 8), dtype=torch.int32).pin_memory()
+    pin_any_d = torch.empty(cap, dtype=torch.uint8).pin_memory()
+    for _ in range(3):
+        n_ao_dev = raygen_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        n_ao_dev = raygen_step()
+    rg_s = (time.perf_counter() - t0) / args.steps
+    raygen_e2e = {"value": round(world * (n_eye + n_ao_dev) / rg_s / 1e6, 3), "unit": UNIT,
+                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(32 * n_eye + n_ao_dev),
+                  "ao_rays": int(n_ao_dev), "ao_rays_equal_host_count": bool(n_ao_dev == n_ao),
+                  "anyhit_equal_host_frame": bool(np.array_equal(pin_any_d[:n_ao_dev].numpy(), got_any))
+                  if n_ao_dev == n_ao else False}
+    del g_eye, g_hits, g_ao, g_any
     for b in (pin_eye, pin_ao, pin_hits, pin_any):
         b.free()
 
@@ -922,6 +958,7 @@ def run_engine(args):
                    "node_pairs_per_ao_ray": round(ao_pairs / n_ao, 3)},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(RAY_BYTES * (n_eye + n_ao)),
                 "d2h_bytes_per_step": int(32 * n_eye + n_ao)},
+        "e2e_device_raygen": raygen_e2e,
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),

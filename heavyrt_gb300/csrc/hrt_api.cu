@@ -39,12 +39,6 @@ int cuda_fail(hrt_context* ctx, cudaError_t e, const char* what)
   return fail(ctx, st, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define HRT_CUDA(ctx, call)                               \
-  do                                                      \
-  {                                                       \
-    cudaError_t e_ = (call);                              \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
 
 void free_geom(Geom& g)
 {

@@ -119,3 +119,11 @@ bool is_identity(const float* m);
 
 }  // namespace api
 }  // namespace hrt
+
+// Returns the mapped status from the enclosing function when a CUDA call fails.
+#define HRT_CUDA(ctx, call)                                            \
+  do                                                                   \
+  {                                                                    \
+    cudaError_t e_ = (call);                                           \
+    if (e_ != cudaSuccess) return hrt::api::cuda_fail(ctx, e_, #call); \
+  } while (0)

@@ -120,6 +120,17 @@ static void wl_norm(double v[3])
   v[0] /= l; v[1] /= l; v[2] /= l;
 }
 
+/* Normalised in float: each component divided by the length. */
+static void wl_normf(float v[3])
+{
+  const float l = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  v[0] = v[0] / l;
+  v[1] = v[1] / l;
+  v[2] = v[2] / l;
+}
+
+static float wl_uniformf(wl_pcg* r) { return (float)(wl_next(r) >> 8) * (1.0f / 16777216.0f); }
+
 static void wl_cross(const double a[3], const double b[3], double o[3])
 {
   o[0] = a[1] * b[2] - a[2] * b[1];
@@ -128,8 +139,11 @@ static void wl_cross(const double a[3], const double b[3], double o[3])
 }
 
 /* Pinhole camera at eye looking at target, `up` hint, vertical field of view
- * fovDeg; one normalised ray per pixel centre, row 0 at the top.
- * rays: width*height*8 floats. */
+ * fovDeg; one normalised ray per pixel centre, row 0 at the top.  The frame
+ * (forward, right, up, tan of the half angle, aspect) is set up in double and
+ * rounded once to float; each pixel's direction then takes only correctly
+ * rounded float operations in a fixed order, so the device generator
+ * (hrt_gen_pinhole_rays) makes the same rays bit for bit. */
 void hrt_wl_camera_rays(const float eye[3], const float target[3], const float up[3], float fovDeg, uint32_t width,
                         uint32_t height, float tmin, float tmax, float* rays)
 {
@@ -140,18 +154,22 @@ void hrt_wl_camera_rays(const float eye[3], const float target[3], const float u
   wl_cross(f, u0, rgt);
   wl_norm(rgt);
   wl_cross(rgt, f, u);
-  const double th = tan(0.5 * (double)fovDeg * 3.14159265358979323846 / 180.0);
-  const double aspect = (double)width / (double)height;
+  const float ff[3] = {(float)f[0], (float)f[1], (float)f[2]};
+  const float fr[3] = {(float)rgt[0], (float)rgt[1], (float)rgt[2]};
+  const float fu[3] = {(float)u[0], (float)u[1], (float)u[2]};
+  const float th = (float)tan(0.5 * (double)fovDeg * 3.14159265358979323846 / 180.0);
+  const float aspect = (float)((double)width / (double)height);
   for (uint32_t y = 0; y < height; y++)
     for (uint32_t x = 0; x < width; x++)
     {
-      const double sx = (2.0 * ((double)x + 0.5) / (double)width - 1.0) * th * aspect;
-      const double sy = (1.0 - 2.0 * ((double)y + 0.5) / (double)height) * th;
-      double d[3] = {f[0] + sx * rgt[0] + sy * u[0], f[1] + sx * rgt[1] + sy * u[1], f[2] + sx * rgt[2] + sy * u[2]};
-      wl_norm(d);
+      const float sx = ((2.0f * ((float)x + 0.5f)) / (float)width - 1.0f) * th * aspect;
+      const float sy = (1.0f - (2.0f * ((float)y + 0.5f)) / (float)height) * th;
+      float d[3];
+      for (int k = 0; k < 3; k++) d[k] = (ff[k] + sx * fr[k]) + sy * fu[k];
+      wl_normf(d);
       float* r = rays + 8 * ((size_t)y * width + x);
       r[0] = eye[0]; r[1] = eye[1]; r[2] = eye[2]; r[3] = tmin;
-      r[4] = (float)d[0]; r[5] = (float)d[1]; r[6] = (float)d[2]; r[7] = tmax;
+      r[4] = d[0]; r[5] = d[1]; r[6] = d[2]; r[7] = tmax;
     }
 }
 
@@ -182,11 +200,16 @@ void hrt_wl_sphere_rays(uint64_t seed, uint32_t n, float radius, float* rays)
  * vertex ids are sortedIdx[3*primId .. 3*primId+2] (the index buffer in the
  * BVH's sorted order, as HeavyRT returns sorted primIds).  For every hit,
  * `perHit` cosine-weighted directions about the geometric normal turned toward
- * the eye; origin = hit point + offset * normal; tmin = 0, tmax = length.
- * Each hit draws from its own PCG stream (seed, hit index), so the output does
- * not depend on how the loop is split.  Returns the number of rays written;
- * aoRays needs room for perHit * (number of hits) rays; owner (optional)
- * receives the eye-ray index of each AO ray. */
+ * the eye (Malley's method: a uniform point of the unit disk, by rejection
+ * from the square, lifted to the hemisphere; basis of Duff et al., "Building
+ * an Orthonormal Basis, Revisited", 2017); origin = hit point + offset *
+ * normal; tmin = 0, tmax = length.  Float arithmetic with correctly rounded
+ * operations only, in a fixed order, so the device generator
+ * (hrt_gen_ao_rays) makes the same rays bit for bit.  Each hit draws from its
+ * own PCG stream (seed, eye-ray index + 16), so the output does not depend on
+ * how the loop is split.  Returns the number of rays written; aoRays needs
+ * room for perHit * (number of hits) rays; owner (optional) receives the
+ * eye-ray index of each AO ray. */
 uint64_t hrt_wl_ao_rays(uint64_t seed, uint64_t nEye, const float* eyeRays, const uint32_t* hits, const float* verts,
                         const uint32_t* sortedIdx, uint32_t perHit, float length, float offset, float* aoRays,
                         uint32_t* owner)
@@ -199,40 +222,42 @@ uint64_t hrt_wl_ao_rays(uint64_t seed, uint64_t nEye, const float* eyeRays, cons
     float t;
     memcpy(&t, &h[0], 4);
     const float* er = eyeRays + 8 * i;
-    const double p[3] = {(double)er[0] + (double)t * er[4], (double)er[1] + (double)t * er[5],
-                         (double)er[2] + (double)t * er[6]};
+    const float p[3] = {er[0] + t * er[4], er[1] + t * er[5], er[2] + t * er[6]};
     const uint32_t prim = h[1];
     const float* A = verts + 4 * (size_t)sortedIdx[3 * (size_t)prim + 0];
     const float* B = verts + 4 * (size_t)sortedIdx[3 * (size_t)prim + 1];
     const float* C = verts + 4 * (size_t)sortedIdx[3 * (size_t)prim + 2];
-    const double e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
-    const double e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
-    double n[3];
-    wl_cross(e1, e2, n);
-    wl_norm(n);
-    if (n[0] * er[4] + n[1] * er[5] + n[2] * er[6] > 0.0) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
-    /* orthonormal basis about n (Duff et al., "Building an Orthonormal Basis, Revisited", 2017) */
-    const double sgn = n[2] >= 0.0 ? 1.0 : -1.0;
-    const double aa = -1.0 / (sgn + n[2]);
-    const double bb = n[0] * n[1] * aa;
-    const double tx[3] = {1.0 + sgn * n[0] * n[0] * aa, sgn * bb, -sgn * n[0]};
-    const double ty[3] = {bb, sgn + n[1] * n[1] * aa, -n[1]};
+    const float e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
+    const float e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+    float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    wl_normf(n);
+    if ((n[0] * er[4] + n[1] * er[5]) + n[2] * er[6] > 0.0f) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
+    const float sgn = n[2] >= 0.0f ? 1.0f : -1.0f;
+    const float aa = -1.0f / (sgn + n[2]);
+    const float bb = (n[0] * n[1]) * aa;
+    const float tx[3] = {1.0f + ((sgn * n[0]) * n[0]) * aa, sgn * bb, -(sgn * n[0])};
+    const float ty[3] = {bb, sgn + (n[1] * n[1]) * aa, -n[1]};
+    const float o[3] = {p[0] + offset * n[0], p[1] + offset * n[1], p[2] + offset * n[2]};
     wl_pcg r;
     wl_seed(&r, seed, i + 16);
     for (uint32_t s = 0; s < perHit; s++)
     {
-      const double r1 = wl_uniform(&r), r2 = wl_uniform(&r);
-      const double phi = 2.0 * 3.14159265358979323846 * r1;
-      const double st = sqrt(r2), ct = sqrt(1.0 - r2);
-      double d[3];
-      for (int k = 0; k < 3; k++) d[k] = st * cos(phi) * tx[k] + st * sin(phi) * ty[k] + ct * n[k];
-      wl_norm(d);
-      float* o = aoRays + 8 * w;
-      o[0] = (float)(p[0] + offset * n[0]);
-      o[1] = (float)(p[1] + offset * n[1]);
-      o[2] = (float)(p[2] + offset * n[2]);
-      o[3] = 0.0f;
-      o[4] = (float)d[0]; o[5] = (float)d[1]; o[6] = (float)d[2]; o[7] = length;
+      float x = 0.0f, y = 0.0f, rr = 0.0f;
+      for (int tries = 0; tries < 64; tries++)
+      {
+        x = 2.0f * wl_uniformf(&r) - 1.0f;
+        y = 2.0f * wl_uniformf(&r) - 1.0f;
+        rr = x * x + y * y;
+        if (rr <= 1.0f) break;
+      }
+      if (rr > 1.0f) { x = 0.0f; y = 0.0f; rr = 0.0f; } /* probability (1 - pi/4)^64 */
+      const float z = sqrtf(1.0f - rr);
+      float d[3];
+      for (int k = 0; k < 3; k++) d[k] = (x * tx[k] + y * ty[k]) + z * n[k];
+      wl_normf(d);
+      float* ry = aoRays + 8 * w;
+      ry[0] = o[0]; ry[1] = o[1]; ry[2] = o[2]; ry[3] = 0.0f;
+      ry[4] = d[0]; ry[5] = d[1]; ry[6] = d[2]; ry[7] = length;
       if (owner) owner[w] = (uint32_t)i;
       w++;
     }

@@ -191,6 +191,9 @@ def lib() -> C.CDLL:
         "hrt_server_wait": (i32, [vp, u64, C.c_double, C.POINTER(RequestInfo)]),
         "hrt_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
         "hrt_server_scene_bytes": (i32, [vp, u64, u64, C.POINTER(u64)]),
+        "hrt_gen_eye_rays": (i32, [vp, vp, vp, u32, u32, C.c_float, C.c_float, vp, vp]),
+        "hrt_gen_pinhole_rays": (i32, [vp, vp, vp, vp, C.c_float, u32, u32, C.c_float, C.c_float, vp, vp]),
+        "hrt_gen_ao_rays": (i32, [vp, u64, vp, vp, u64, u32, C.c_float, C.c_float, vp, vp, u64, C.POINTER(u64), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -223,6 +226,21 @@ class Context:
     def check(self, st: int, what: str):
         if st != HRT_OK:
             raise HrtError(st, f"{what}: {self.last_error() or lib().hrt_status_string(st).decode()}")
+
+    def gen_eye_rays(self, proj_inv, world_view_inv, width: int, height: int, t_near: float, t_far: float,
+                     rays_ptr: int, stream: int = 0):
+        """The renderers' eye rays on the device (hrt_gen_eye_rays); matrices 4x4 row-major numpy."""
+        pi = np.ascontiguousarray(np.asarray(proj_inv, np.float32).T)
+        wi = np.ascontiguousarray(np.asarray(world_view_inv, np.float32).T)
+        self.check(lib().hrt_gen_eye_rays(self._h, _ptr(pi), _ptr(wi), width, height, t_near, t_far,
+                                          C.c_void_p(rays_ptr), C.c_void_p(stream)), "hrt_gen_eye_rays")
+
+    def gen_pinhole_rays(self, eye, target, up, fov_deg: float, width: int, height: int, tmin: float, tmax: float,
+                         rays_ptr: int, stream: int = 0):
+        """The benchmark camera's eye rays on the device (hrt_gen_pinhole_rays)."""
+        e, t, u = (np.ascontiguousarray(x, dtype=np.float32) for x in (eye, target, up))
+        self.check(lib().hrt_gen_pinhole_rays(self._h, _ptr(e), _ptr(t), _ptr(u), fov_deg, width, height, tmin, tmax,
+                                              C.c_void_p(rays_ptr), C.c_void_p(stream)), "hrt_gen_pinhole_rays")
 
     def close(self):
         if self._h:
@@ -394,6 +412,15 @@ class SceneRT:
                                                                _ptr(ioff), int(a_qualityLevel), 16, C.byref(first)),
                        "add_geoms_batched")
         return list(range(first.value, first.value + len(vs)))
+
+    def gen_ao_rays(self, seed: int, eye_ptr: int, hits_ptr: int, n_eye: int, per_hit: int, length: float,
+                    offset: float, out_ptr: int, capacity: int, owner_ptr: int = 0, stream: int = 0) -> int:
+        """AO rays from device eye rays and their hits (hrt_gen_ao_rays); returns the count."""
+        n = C.c_uint64()
+        self.ctx.check(lib().hrt_gen_ao_rays(self._h, seed, C.c_void_p(eye_ptr), C.c_void_p(hits_ptr), n_eye, per_hit,
+                                             length, offset, C.c_void_p(out_ptr), C.c_void_p(owner_ptr or None),
+                                             capacity, C.byref(n), C.c_void_p(stream)), "hrt_gen_ao_rays")
+        return n.value
 
     def query_multi(self, desc: QueryDesc, stream: int = 0):
         """Asynchronous (optionally segmented) query on device arrays (hrt_query_multi)."""

@@ -350,6 +350,37 @@ int hrt_server_get_stats(hrt_server* server, hrt_server_stats* stats);
  * once built it holds its actual, smaller size. */
 int hrt_server_scene_bytes(const hrt_server* server, uint64_t nVert, uint64_t nTris, uint64_t* bytes);
 
+/* ---------------------------------------------------------------- ray generation on the GPU
+ * A frame's rays made where they are traced, so that neither the eye rays
+ * nor the AO rays chained from their hits cross the host link.  Output arrays
+ * are device memory (8 floats per ray); asynchronous on `stream` unless noted. */
+
+/* The renderers' eye rays: RTAO::kernel_InitEyeRay (examples/02_rtao/rtao.cpp:133-144,
+ * examples/01_eye_rays/eye_ray.cpp:26-47) with EyeRayDirNormalized / transform_ray3f
+ * (examples/render_common.h:6-36).  projInv, worldViewInv: column-major 4x4;
+ * one ray per pixel centre, row-major (pixel x, y at index y * width + x). */
+int hrt_gen_eye_rays(hrt_context* ctx, const float projInv[16], const float worldViewInv[16], uint32_t width,
+                     uint32_t height, float tNear, float tFar, float* rays, void* stream);
+
+/* Pinhole camera at eye looking at target (up hint, vertical field of view
+ * fovDeg): the benchmark workloads' eye rays, equal to the host generator's
+ * (heavyrt_gb300/workload.py camera_rays) bit for bit. */
+int hrt_gen_pinhole_rays(hrt_context* ctx, const float eye[3], const float target[3], const float up[3], float fovDeg,
+                         uint32_t width, uint32_t height, float tmin, float tmax, float* rays, void* stream);
+
+/* Ambient-occlusion rays from primary hits (device eye rays and their hits):
+ * for every hit, perHit cosine-weighted directions about the hit triangle's
+ * geometric normal turned toward the eye, from the PCG32 stream (seed, hit's
+ * eye-ray index + 16); origin = hit point + offset * normal, tmin 0, tmax =
+ * length.  Hits are compacted in eye-ray order, as the host generator
+ * (heavyrt_gb300/workload.py ao_rays) orders them; owner (device, optional)
+ * receives each AO ray's eye-ray index.  Needs identity instances.
+ * Synchronous: *count receives the number of AO rays (HRT_ERR_CAPACITY when
+ * it exceeds capacity). */
+int hrt_gen_ao_rays(hrt_scene* scene, uint64_t seed, const float* eyeRays, const hrt_hit* hits, uint64_t nEye,
+                    uint32_t perHit, float length, float offset, float* aoRays, uint32_t* owner, uint64_t capacity,
+                    uint64_t* count, void* stream);
+
 /* ---------------------------------------------------------------- scene info */
 
 /* ISceneObject::GetGeomNum / GetInstNum / GetGeomBoxes (core/CrossRT.h:163-165). */

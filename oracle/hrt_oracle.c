@@ -744,3 +744,50 @@ int ora_trace(const ora_bvh* B, const float* rays, uint64_t n, int mode, ora_hit
   if (counters) { counters[0] = c0; counters[1] = c1; }
   return used;
 }
+
+/* ---------------------------------------------------------------- ray set-up
+ * Eye rays of HeavyRT's renderers: RTAO::kernel_InitEyeRay
+ * (examples/02_rtao/rtao.cpp:133-144; the same body in
+ * examples/01_eye_rays/eye_ray.cpp:26-47) with EyeRayDirNormalized and
+ * transform_ray3f (examples/render_common.h:6-12,20-36), one ray per pixel
+ * centre in row-major order.  Matrices are column-major; mat x vec sums
+ * ((m0*x + m1*y) + m2*z) + m3*w per row, normalize(v) = v * (1/sqrt(dot(v,v)))
+ * with dot = (x*x + y*y) + z*z, as the LiteMath stand-in evaluates them. */
+static void ora_mat_vec(const float* m, const float v[4], float o[4])
+{
+  for (int r = 0; r < 4; r++) o[r] = ((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * v[3];
+}
+
+static void ora_normalize3(float v[3])
+{
+  const float inv = 1.0f / sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  v[0] = v[0] * inv;
+  v[1] = v[1] * inv;
+  v[2] = v[2] * inv;
+}
+
+void ora_eye_rays(const float* projInv, const float* worldViewInv, uint32_t width, uint32_t height, float tNear,
+                  float tFar, float* rays)
+{
+  for (uint32_t y = 0; y < height; y++)
+    for (uint32_t x = 0; x < width; x++)
+    {
+      const float fx = ((float)x + 0.5f) / (float)width, fy = ((float)y + 0.5f) / (float)height;
+      const float pos[4] = {2.0f * fx - 1.0f, -2.0f * fy + 1.0f, 0.0f, 1.0f};
+      float p[4];
+      ora_mat_vec(projInv, pos, p);
+      const float w = p[3];
+      float d[3] = {p[0] / w, p[1] / w, p[2] / w};
+      ora_normalize3(d);
+      const float o0[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+      const float o1[4] = {0.0f + 100.0f * d[0], 0.0f + 100.0f * d[1], 0.0f + 100.0f * d[2], 1.0f};
+      float a[4], b[4];
+      ora_mat_vec(worldViewInv, o0, a);
+      ora_mat_vec(worldViewInv, o1, b);
+      float dir[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+      ora_normalize3(dir);
+      float* r = rays + 8 * ((size_t)y * width + x);
+      r[0] = a[0]; r[1] = a[1]; r[2] = a[2]; r[3] = tNear;
+      r[4] = dir[0]; r[5] = dir[1]; r[6] = dir[2]; r[7] = tFar;
+    }
+}

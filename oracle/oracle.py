@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
         L.ora_copy_u32.argtypes = [vp, i32, vp]
         L.ora_trace.restype = i32
         L.ora_trace.argtypes = [vp, vp, u64, i32, vp, vp, i32, vp]
+        L.ora_eye_rays.argtypes = [vp, vp, u32, u32, C.c_float, C.c_float, vp]
         _lib = L
     return _lib
 
@@ -134,6 +135,32 @@ class OracleBVH:
 
 
 # ---------------------------------------------------------------- reference checker
+
+def eye_rays(proj_inv: np.ndarray, world_view_inv: np.ndarray, width: int, height: int, t_near: float = 0.0,
+             t_far: float = 3.4028234663852886e38) -> np.ndarray:
+    """The renderers' eye rays (C restatement); matrices as 4x4 row-major numpy arrays."""
+    pi = np.ascontiguousarray(np.asarray(proj_inv, np.float32).T)  # column-major storage
+    wi = np.ascontiguousarray(np.asarray(world_view_inv, np.float32).T)
+    out = np.empty((width * height, 8), np.float32)
+    lib().ora_eye_rays(_p(pi), _p(wi), width, height, t_near, t_far, _p(out))
+    return out
+
+
+def reference_eye_rays(proj_inv, world_view_inv, width: int, height: int, t_near: float = 0.0,
+                       t_far: float = 3.4028234663852886e38):
+    """The same rays from the reference's own helpers (oracle/_ref/raygen_harness), or None."""
+    exe = HERE / "_ref" / "raygen_harness"
+    if not exe.exists():
+        return None
+    pi = np.asarray(proj_inv, np.float32).T.reshape(-1)
+    wi = np.asarray(world_view_inv, np.float32).T.reshape(-1)
+    with tempfile.TemporaryDirectory() as d:
+        src, dst = Path(d) / "p.bin", Path(d) / "o.bin"
+        src.write_bytes(np.concatenate([pi, wi]).astype(np.float32).tobytes() +
+                        np.array([width, height], np.uint32).tobytes() + np.array([t_near, t_far], np.float32).tobytes())
+        subprocess.run([str(exe), "eye", str(src), str(dst)], check=True)
+        return np.fromfile(dst, dtype=np.float32).reshape(-1, 8)
+
 
 def reference_harness(fast: bool = False) -> Path | None:
     p = HERE / "_ref" / ("ref_harness_fast" if fast else "ref_harness")

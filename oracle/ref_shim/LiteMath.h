@@ -28,6 +28,9 @@
 #ifndef MAXFLOAT
 #define MAXFLOAT FLT_MAX
 #endif
+#ifndef M_TWOPI
+#define M_TWOPI 6.28318530717958647692f  // 2 pi as a float (the renderers' sample mapping)
+#endif
 
 namespace LiteMath
 {
@@ -111,6 +114,9 @@ namespace LiteMath
   template <typename T> static inline vec4_t<T>& operator+=(vec4_t<T>& a, vec4_t<T> b) { a = a + b; return a; }
   template <typename T> static inline vec3_t<T>& operator*=(vec3_t<T>& a, T s) { a = a * s; return a; }
   template <typename T> static inline vec4_t<T>& operator*=(vec4_t<T>& a, T s) { a = a * s; return a; }
+  // component-wise division by a scalar (the renderers' `pos /= pos.w`)
+  template <typename T> static inline vec3_t<T>& operator/=(vec3_t<T>& a, T s) { a = a / s; return a; }
+  template <typename T> static inline vec4_t<T>& operator/=(vec4_t<T>& a, T s) { a = a / s; return a; }
 
   static inline float3 min(float3 a, float3 b) { return float3(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)); }
   static inline float3 max(float3 a, float3 b) { return float3(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }

@@ -52,10 +52,54 @@ def cases():
     yield "heightfield8x5_tnear", v, idx, rays
 
 
+def perspective(fov_deg, aspect, near, far):
+    t = 1.0 / np.tan(np.radians(fov_deg) / 2.0)
+    m = np.zeros((4, 4))
+    m[0, 0], m[1, 1] = t / aspect, t
+    m[2, 2], m[2, 3], m[3, 2] = (far + near) / (near - far), 2.0 * far * near / (near - far), -1.0
+    return m
+
+
+def look_at(eye, target, up):
+    eye, target, up = (np.asarray(x, np.float64) for x in (eye, target, up))
+    f = (target - eye) / np.linalg.norm(target - eye)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[:3, 3] = -m[:3, :3] @ eye
+    return m
+
+
+def eye_ray_cases():
+    """Inverse projection / world-view matrices for the renderers' eye-ray set-up:
+    the heightfield camera, and two perturbed (non-affine) matrix pairs."""
+    p = np.linalg.inv(perspective(60.0, 16.0 / 9.0, 0.01, 100.0)).astype(np.float32)
+    v = np.linalg.inv(look_at((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1))).astype(np.float32)
+    yield p, v, 160, 90, 0.0, 3.4028234663852886e38
+    rng = np.random.default_rng(1)
+    for w, h in ((33, 17), (64, 64)):
+        yield ((p + rng.normal(0, 0.05, (4, 4))).astype(np.float32), (v + rng.normal(0, 0.05, (4, 4))).astype(np.float32),
+               w, h, 0.5, 7.0)
+
+
+def make_eye_rays():
+    """raygen_eye.npz: the reference's own eye-ray set-up (oracle/_ref/raygen_harness)."""
+    out = {}
+    for k, (p, v, w, h, tn, tf) in enumerate(eye_ray_cases()):
+        rays = orc.reference_eye_rays(p, v, w, h, tn, tf)
+        out.update({f"proj_inv{k}": p, f"world_view_inv{k}": v, f"size{k}": np.array([w, h]),
+                    f"range{k}": np.array([tn, tf], np.float32), f"rays{k}": rays})
+        print("eye rays", k, w, h)
+    np.savez_compressed(OUT / "raygen_eye.npz", **out)
+
+
 def main():
     native_build.build_all()
     if orc.reference_harness() is None:
         raise SystemExit("reference sources not available: cannot regenerate golden vectors")
+    make_eye_rays()
     for name, v, idx, rays in cases():
         ref = orc.run_reference(v, idx, rays)
         np.savez_compressed(

@@ -102,3 +102,25 @@ def test_oracle_matches_reference_live(host_libs, kind, n):
     np.testing.assert_array_equal(o.prim_indices(), ref["prim_indices"])
     np.testing.assert_array_equal(o.trace(rays).view(np.uint32), ref["hits"].view(np.uint32))
     np.testing.assert_array_equal(o.trace(rays, any_hit=True), ref["any"])
+
+
+def _eye_cases():
+    z = np.load(GOLDEN / "raygen_eye.npz")
+    k = 0
+    while f"rays{k}" in z:
+        yield (z[f"proj_inv{k}"], z[f"world_view_inv{k}"], *[int(x) for x in z[f"size{k}"]],
+               *[float(x) for x in z[f"range{k}"]], z[f"rays{k}"])
+        k += 1
+
+
+def test_eye_rays_restatement_matches_reference_fixture(host_libs):
+    """The renderers' eye-ray set-up restated in C equals the reference's own
+    helpers (examples/render_common.h, compiled against the LiteMath stand-in)."""
+    from oracle import oracle as orc
+
+    for p, v, w, h, tn, tf, want in _eye_cases():
+        got = orc.eye_rays(p, v, w, h, tn, tf)
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        live = orc.reference_eye_rays(p, v, w, h, tn, tf)
+        if live is not None:
+            np.testing.assert_array_equal(live.view(np.uint32), want.view(np.uint32))
