@@ -192,6 +192,11 @@ def lib() -> C.CDLL:
         "hrt_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
         "hrt_server_scene_bytes": (i32, [vp, u64, u64, C.POINTER(u64)]),
         "hrt_gen_eye_rays": (i32, [vp, vp, vp, u32, u32, C.c_float, C.c_float, vp, vp]),
+        "hrt_vsgf_info": (i32, [C.c_char_p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]),
+        "hrt_vsgf_read": (i32, [C.c_char_p, vp, vp, vp]),
+        "hrt_vsgf_write": (i32, [C.c_char_p, vp, u64, vp, u64]),
+        "hrt_geom_save": (i32, [vp, u32, C.c_char_p]),
+        "hrt_geom_load": (i32, [vp, C.c_char_p, C.POINTER(u32)]),
         "hrt_gen_pinhole_rays": (i32, [vp, vp, vp, vp, C.c_float, u32, u32, C.c_float, C.c_float, vp, vp]),
         "hrt_gen_ao_rays": (i32, [vp, u64, vp, vp, u64, u32, C.c_float, C.c_float, vp, vp, u64, C.POINTER(u64), vp]),
     }
@@ -422,6 +427,16 @@ class SceneRT:
                                              capacity, C.byref(n), C.c_void_p(stream)), "hrt_gen_ao_rays")
         return n.value
 
+    def save_geom(self, geom_id: int, path) -> None:
+        """Writes a BVH blob of a built geometry (hrt_geom_save)."""
+        self.ctx.check(lib().hrt_geom_save(self._h, geom_id, str(path).encode()), "hrt_geom_save")
+
+    def load_geom(self, path) -> int:
+        """Restores a geometry from a BVH blob without building (hrt_geom_load); returns its id."""
+        gid = C.c_uint32()
+        self.ctx.check(lib().hrt_geom_load(self._h, str(path).encode(), C.byref(gid)), "hrt_geom_load")
+        return gid.value
+
     def query_multi(self, desc: QueryDesc, stream: int = 0):
         """Asynchronous (optionally segmented) query on device arrays (hrt_query_multi)."""
         self.ctx.check(lib().hrt_query_multi(self._h, C.byref(desc), C.c_void_p(stream)), "query_multi")
@@ -579,6 +594,33 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def load_vsgf(path, normals: bool = False):
+    """A VSGF mesh (hrt_vsgf_read): float32 [V, 4] positions (w = 1), uint32 indices
+    (and float32 [V, 4] normals when asked)."""
+    nv, ni, fl = C.c_uint64(), C.c_uint64(), C.c_uint32()
+    st = lib().hrt_vsgf_info(str(path).encode(), C.byref(nv), C.byref(ni), C.byref(fl))
+    if st != HRT_OK:
+        raise HrtError(st, f"hrt_vsgf_info({path}): not a readable VSGF mesh")
+    v = np.empty((nv.value, 4), np.float32)
+    idx = np.empty(ni.value, np.uint32)
+    nrm = np.empty((nv.value, 4), np.float32) if normals else None
+    st = lib().hrt_vsgf_read(str(path).encode(), _ptr(v), _ptr(idx), _ptr(nrm) if normals else None)
+    if st != HRT_OK:
+        raise HrtError(st, f"hrt_vsgf_read({path})")
+    return (v, idx, nrm) if normals else (v, idx)
+
+
+def save_vsgf(path, verts, idx):
+    """Writes positions + indices as a VSGF mesh (hrt_vsgf_write)."""
+    v = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, np.asarray(verts).shape[-1]))
+    if v.shape[1] == 3:
+        v = np.ascontiguousarray(np.concatenate([v, np.ones((len(v), 1), np.float32)], axis=1))
+    i = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1)
+    st = lib().hrt_vsgf_write(str(path).encode(), _ptr(v), len(v), _ptr(i), i.size)
+    if st != HRT_OK:
+        raise HrtError(st, f"hrt_vsgf_write({path})")
 
 
 def CreateSceneRT(a_implName: str = "GB300_LBVH", a_buildName: str = "cbvh_lbvh", a_layoutName: str = "") -> SceneRT:

@@ -381,6 +381,29 @@ int hrt_gen_ao_rays(hrt_scene* scene, uint64_t seed, const float* eyeRays, const
                     uint32_t perHit, float length, float offset, float* aoRays, uint32_t* owner, uint64_t capacity,
                     uint64_t* count, void* stream);
 
+/* ---------------------------------------------------------------- on-disk formats */
+
+/* VSGF meshes, HeavyRT's binary mesh files (examples/loader/cmesh.cpp:80-173):
+ * a 24-byte header {u64 file size, u32 vertices, u32 indices, u32 materials,
+ * u32 flags}, float4 positions, float4 normals (absent with flag 8), float4
+ * tangents (with flag 1), float2 texture coordinates, u32 indices, one u32
+ * material per triangle.  Host-only; no context needed.
+ * hrt_vsgf_info: counts and flags (HRT_ERR_INVALID_ARGUMENT for a missing,
+ * truncated or malformed file).  hrt_vsgf_read: positions (nVert float4) and
+ * indices into caller buffers; normals too when norm4 is not NULL (zeros when
+ * the file has none).  hrt_vsgf_write: positions + indices (no normals). */
+int hrt_vsgf_info(const char* path, uint64_t* nVert, uint64_t* nIdx, uint32_t* flags);
+int hrt_vsgf_read(const char* path, float* vpos4, uint32_t* idx, float* norm4);
+int hrt_vsgf_write(const char* path, const float* vpos4, uint64_t nVert, const uint32_t* idx, uint64_t nIdx);
+
+/* BVH blobs: every device array of a built geometry in one file, so that a
+ * geometry is restored by copies alone, without a build (a warm start for
+ * resident scenes).  A blob loads only into a scene of the layout it was
+ * built for (HRT_ERR_STATE otherwise); hrt_geom_load appends a geometry and
+ * returns its id. */
+int hrt_geom_save(const hrt_scene* scene, uint32_t geomId, const char* path);
+int hrt_geom_load(hrt_scene* scene, const char* path, uint32_t* geomId);
+
 /* ---------------------------------------------------------------- scene info */
 
 /* ISceneObject::GetGeomNum / GetInstNum / GetGeomBoxes (core/CrossRT.h:163-165). */
