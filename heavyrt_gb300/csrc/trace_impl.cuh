@@ -95,7 +95,7 @@ __device__ __forceinline__ void slab(const Ray& r, float bx0, float by0, float b
 struct Hit
 {
   float    t, u, v;
-  uint32_t prim, inst, geom;
+  uint32_t prim, inst;  // sorted triangle, instance index (0xFFFFFFFF: no hit)
 };
 
 // matmul4x3 / matmul3x3 (core/raytrace_common.h:82-90) with the column sum
@@ -133,7 +133,7 @@ __device__ __forceinline__ void make_ray(const InstanceDesc& d, const float4& po
 // Returns true when ANY and a triangle was accepted.
 template <bool ANY, bool COUNT, uint32_t ENDBIT = 1u>
 __device__ __forceinline__ bool leaf_test(const TriRec* __restrict__ tris, uint32_t j, const Ray& r, Hit& h,
-                                          uint32_t instId, uint32_t geomId, uint64_t& nTris)
+                                          uint32_t instIndex, uint64_t& nTris)
 {
   while (true)
   {
@@ -164,8 +164,7 @@ __device__ __forceinline__ bool leaf_test(const TriRec* __restrict__ tris, uint3
       h.u = u;
       h.v = v;
       h.prim = j;
-      h.inst = instId;
-      h.geom = geomId;
+      h.inst = instIndex;
       if (ANY) return true;
     }
     if (__float_as_uint(A.w) & ENDBIT) return false;  // last triangle of the leaf
@@ -260,6 +259,8 @@ struct Lane
   uint32_t ray;       // ray index or kNoRay
   uint32_t inst;      // current instance
   uint32_t instEnd;   // one past the last instance this ray is traced against
+  const void*   nodes;  // the current instance's records (binary) or 4-wide nodes
+  const TriRec* tris;   // the current instance's triangle records
   uint32_t cur;       // current record / leaf reference
   int      top;       // stack depth
   int      base;      // stack depth at which the current instance's traversal began
@@ -287,17 +288,29 @@ __device__ __forceinline__ bool out_of_budget(Lane& L, uint32_t* errorWord)
   return true;
 }
 
+// Makes instance k the lane's current instance: its ray, and its node and
+// triangle arrays held in registers for the steps that follow.
+template <int LAYOUT>
+__device__ __forceinline__ void enter_instance(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t k)
+{
+  const InstanceDesc& d = inst[k];
+  L.inst = k;
+  make_ray(d, L.po, L.di, L.r);
+  L.nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
+  L.tris = d.tris;
+  L.cur = 0;  // record / node 0 = the root
+}
+
 // Advances the lane's instance cursor to the next instance with triangles,
 // starting at `from` and ending before L.instEnd; prepares the ray for it.
 // Returns false when none is left.
+template <int LAYOUT>
 __device__ __forceinline__ bool begin_instance(Lane& L, const InstanceDesc* __restrict__ inst, uint32_t from)
 {
   for (uint32_t k = from; k < L.instEnd; k++)
     if (inst[k].valid)
     {
-      L.inst = k;
-      make_ray(inst[k], L.po, L.di, L.r);
-      L.cur = 0;  // record 0 = the root's two children
+      enter_instance<LAYOUT>(L, inst, k);
       L.top = 0;
       L.base = 0;
       return true;
@@ -349,15 +362,14 @@ __device__ __forceinline__ int visit_pair(Lane& L, const PairRec* __restrict__ r
 }
 
 template <int LAYOUT, bool COUNT, int THREADS, int DEPTH>
-__device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32_t* __restrict__ stack,
-                                          uint64_t& nPairs, uint32_t* errorWord)
+__device__ __forceinline__ int visit_node(Lane& L, uint32_t* __restrict__ stack, uint64_t& nPairs, uint32_t* errorWord)
 {
   if constexpr (LAYOUT != 0)
   {
     // 4-wide node: HeavyRT's BVH4 order (core/BVH4CommonRT.cpp:49-246)
     using N = typename Node4Type<LAYOUT>::type;
     Boxes4 B;
-    load_node4(reinterpret_cast<const N*>(d.nodes4) + L.cur, B);
+    load_node4(reinterpret_cast<const N*>(L.nodes) + L.cur, B);
     if (COUNT) nPairs++;
     float key[4];
     uint32_t ref[4] = {B.ref.x, B.ref.y, B.ref.z, B.ref.w};
@@ -394,7 +406,7 @@ __device__ __forceinline__ int visit_node(Lane& L, const InstanceDesc& d, uint32
     return 0;
   }
   else
-    return visit_pair<COUNT, THREADS, DEPTH>(L, d.recs, stack, nPairs, errorWord);
+    return visit_pair<COUNT, THREADS, DEPTH>(L, reinterpret_cast<const PairRec*>(L.nodes), stack, nPairs, errorWord);
 }
 
 // One traversal step (an internal node, or a leaf followed by a pop).
@@ -432,7 +444,7 @@ __device__ __forceinline__ bool tlas_pop(Lane& L, const uint32_t* __restrict__ s
 
 // Enters the next instance (with triangles) of the current TLAS leaf run; when
 // the run is done, returns to the instance tree.  True when the ray is finished.
-template <int THREADS>
+template <int LAYOUT, int THREADS>
 __device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
                                           const uint32_t* __restrict__ stack)
 {
@@ -444,10 +456,8 @@ __device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restric
     L.tnext = (flags & 1u) ? kNoRay : L.tnext + 1;
     if (k < tl.nInst && inst[k].valid)
     {
-      L.inst = k;
-      make_ray(inst[k], L.po, L.di, L.r);
+      enter_instance<LAYOUT>(L, inst, k);
       L.base = L.top;
-      L.cur = 0;
       return false;
     }
   }
@@ -473,20 +483,19 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
     }
     if (L.cur == kEmptyRef) return tlas_pop<THREADS>(L, stack);
     L.tnext = L.cur & ~kLeafBit;
-    return tlas_next<THREADS>(L, inst, tl, stack);
+    return tlas_next<LAYOUT, THREADS>(L, inst, tl, stack);
   }
-  const InstanceDesc& d = inst[L.inst];
   bool pop;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, COUNT, THREADS, DEPTH>(L, d, stack, nPairs, errorWord);
+    const int r = visit_node<LAYOUT, COUNT, THREADS, DEPTH>(L, stack, nPairs, errorWord);
     if (r < 0) return true;
     pop = (r == 1);
   }
   else
   {
     if (L.cur != kEmptyRef &&
-        leaf_test<ANY, COUNT, EndBit<LAYOUT>::value>(d.tris, L.cur & ~kLeafBit, L.r, L.h, d.instId, d.geomId, nTris))
+        leaf_test<ANY, COUNT, EndBit<LAYOUT>::value>(L.tris, L.cur & ~kLeafBit, L.r, L.h, L.inst, nTris))
       return true;  // any-hit found
     pop = true;
   }
@@ -498,21 +507,26 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
       L.cur = stack[L.top * THREADS];
       return false;
     }
-    if (TLAS) return tlas_next<THREADS>(L, inst, tl, stack);
-    return !begin_instance(L, inst, L.inst + 1);
+    if (TLAS) return tlas_next<LAYOUT, THREADS>(L, inst, tl, stack);
+    return !begin_instance<LAYOUT>(L, inst, L.inst + 1);
   }
   return false;
 }
 
+// The hit holds the instance's index; its instance and geometry ids are read
+// once, here.
 template <bool ANY>
-__device__ __forceinline__ void write_result(const Lane& L, void* out)
+__device__ __forceinline__ void write_result(const Lane& L, const InstanceDesc* __restrict__ inst, void* out)
 {
+  const bool hit = L.h.prim != 0xFFFFFFFFu;
   if (ANY)
-    reinterpret_cast<uint8_t*>(out)[L.ray] = (L.h.geom != 0xFFFFFFFFu) ? 1 : 0;
+    reinterpret_cast<uint8_t*>(out)[L.ray] = hit ? 1 : 0;
   else
   {
+    const uint32_t instId = hit ? inst[L.h.inst].instId : 0xFFFFFFFFu;
+    const uint32_t geomId = hit ? inst[L.h.inst].geomId : 0xFFFFFFFFu;
     float4* o = reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray);
-    o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(L.h.inst), __uint_as_float(L.h.geom));
+    o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(instId), __uint_as_float(geomId));
     o[1] = make_float4(L.h.u, L.h.v, 0.0f, 0.0f);
   }
 }
@@ -555,7 +569,7 @@ __device__ __forceinline__ void start_ray(Lane& L, uint32_t i, const float4* __r
   L.di = __ldg(rays + 2 * (size_t)i + 1);
   L.h.t = L.di.w;
   L.h.u = L.h.v = 0.0f;
-  L.h.prim = L.h.inst = L.h.geom = 0xFFFFFFFFu;
+  L.h.prim = L.h.inst = 0xFFFFFFFFu;
   L.budget = kStepBudget;
 }
 
@@ -610,10 +624,10 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
           start_ray(L, i, rays);
           bool live = true;
           if (TLAS) tlas_begin(L);
-          else live = begin_instance(L, inst, first_instance(L, i, sg));
+          else live = begin_instance<LAYOUT>(L, inst, first_instance(L, i, sg));
           if (!live)
           {
-            write_result<ANY>(L, out);
+            write_result<ANY>(L, inst, out);
             L.ray = kNoRay;
           }
         }
@@ -626,7 +640,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
         if (out_of_budget(L, errorWord) ||
             step<LAYOUT, ANY, COUNT, THREADS, TLAS>(L, inst, tl, stack, nPairs, nTris, errorWord))
         {
-          write_result<ANY>(L, out);
+          write_result<ANY>(L, inst, out);
           L.ray = kNoRay;
           break;
         }
@@ -652,11 +666,11 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
     start_ray(L, i, rays);
     bool live = true;
     if (TLAS) tlas_begin(L);
-    else live = begin_instance(L, inst, first_instance(L, i, sg));
+    else live = begin_instance<LAYOUT>(L, inst, first_instance(L, i, sg));
     if (live)
       while (!out_of_budget(L, errorWord) &&
              !step<LAYOUT, ANY, COUNT, THREADS, TLAS>(L, inst, tl, stack, nPairs, nTris, errorWord)) {}
-    write_result<ANY>(L, out);
+    write_result<ANY>(L, inst, out);
   }
   flush_counters<COUNT>(nPairs, nTris, counters);
 }
