@@ -361,7 +361,7 @@ __device__ __forceinline__ int visit_pair(Lane& L, const PairRec* __restrict__ r
   return 0;
 }
 
-template <int LAYOUT, bool COUNT, int THREADS, int DEPTH>
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, int DEPTH>
 __device__ __forceinline__ int visit_node(Lane& L, uint32_t* __restrict__ stack, uint64_t& nPairs, uint32_t* errorWord)
 {
   if constexpr (LAYOUT != 0)
@@ -381,6 +381,31 @@ __device__ __forceinline__ int visit_node(Lane& L, uint32_t* __restrict__ stack,
       const bool hit = ref[k] != kEmptyRef && tn <= tf && tf >= L.r.tNear && tn <= L.h.t;
       key[k] = hit ? tn : INFINITY;
       ref[k] = hit ? ref[k] : kEmptyRef;
+    }
+    if constexpr (ANY)
+    {
+      // any hit: the answer does not depend on the visit order, so the hit
+      // children are taken in slot order without sorting
+      uint32_t first = kEmptyRef;
+#pragma unroll
+      for (int k = 3; k >= 0; k--)
+      {
+        if (ref[k] == kEmptyRef) continue;
+        if (first != kEmptyRef)
+        {
+          if (L.top >= DEPTH)
+          {
+            atomicOr(errorWord, kErrStack);
+            return -1;
+          }
+          stack[L.top * THREADS] = first;
+          L.top++;
+        }
+        first = ref[k];
+      }
+      if (first == kEmptyRef) return 1;
+      L.cur = first;
+      return 0;
     }
     cswap(key[0], ref[0], key[1], ref[1]);
     cswap(key[2], ref[2], key[3], ref[3]);
@@ -488,7 +513,7 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
   bool pop;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, COUNT, THREADS, DEPTH>(L, stack, nPairs, errorWord);
+    const int r = visit_node<LAYOUT, ANY, COUNT, THREADS, DEPTH>(L, stack, nPairs, errorWord);
     if (r < 0) return true;
     pop = (r == 1);
   }
