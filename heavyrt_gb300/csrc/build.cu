@@ -57,16 +57,32 @@ __global__ void __launch_bounds__(kThreads) k_box_partial(const float4* __restri
 
 // Final box and ZIndexMultCoeff on the box widened by 1e-4
 // (core/builders/lbvh.cpp:41-51,263).
-__global__ void k_box_final(const float4* __restrict__ partial, uint32_t nPartial, BuildParams* params)
+__global__ void __launch_bounds__(kThreads) k_box_final(const float4* __restrict__ partial, uint32_t nPartial,
+                                                         BuildParams* params)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
   float mn[4] = {1e10f, 1e10f, 1e10f, 1e10f}, mx[4] = {-1e10f, -1e10f, -1e10f, -1e10f};
-  for (uint32_t b = 0; b < nPartial; b++)
+  for (uint32_t b = threadIdx.x; b < nPartial; b += kThreads)
   {
     const float4 a = partial[2 * b], c = partial[2 * b + 1];
     mn[0] = lm_min(mn[0], a.x); mn[1] = lm_min(mn[1], a.y); mn[2] = lm_min(mn[2], a.z); mn[3] = lm_min(mn[3], a.w);
     mx[0] = lm_max(mx[0], c.x); mx[1] = lm_max(mx[1], c.y); mx[2] = lm_max(mx[2], c.z); mx[3] = lm_max(mx[3], c.w);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+    {
+      mn[k] = lm_min(mn[k], __shfl_down_sync(0xFFFFFFFFu, mn[k], o));
+      mx[k] = lm_max(mx[k], __shfl_down_sync(0xFFFFFFFFu, mx[k], o));
+    }
+  __shared__ float smn[kThreads / 32][4], smx[kThreads / 32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int k = 0; k < 4; k++) { smn[warp][k] = mn[k]; smx[warp][k] = mx[k]; }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < kThreads / 32; w++)
+    for (int k = 0; k < 4; k++) { mn[k] = lm_min(mn[k], smn[w][k]); mx[k] = lm_max(mx[k], smx[w][k]); }
   bc::zindex_scale(mn, mx, params);
 }
 
@@ -325,7 +341,7 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
   uint32_t pb = grid_for(b.nVerts, numSMs, 4);
   if (pb > 1024) pb = 1024;
   k_box_partial<<<pb, kThreads, 0, s>>>(b.verts, b.nVerts, partial);
-  k_box_final<<<1, 32, 0, s>>>(partial, pb, b.params);
+  k_box_final<<<1, kThreads, 0, s>>>(partial, pb, b.params);
   // 2. Morton codes
   k_morton<<<(N + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.verts, b.idx, N, b.nVerts, b.params, b.keys, b.vals, err);
   cudaError_t e = cudaMemcpyAsync(b.keysUnsorted, b.keys, sizeof(uint32_t) * N, cudaMemcpyDeviceToDevice, s);
@@ -367,7 +383,7 @@ cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, c
   uint32_t pb = grid_for(b.nVerts, numSMs, 4);
   if (pb > 1024) pb = 1024;
   k_box_partial<<<pb, kThreads, 0, s>>>(b.verts, b.nVerts, partial);
-  k_box_final<<<1, 32, 0, s>>>(partial, pb, boxOut);
+  k_box_final<<<1, kThreads, 0, s>>>(partial, pb, boxOut);
   const uint32_t g = grid_for(N, numSMs, 8);
   k_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vals, b.runStarts, N, b.nVerts, b.params, b.lr, b.tris, b.sortedIdx,
                                   err);
