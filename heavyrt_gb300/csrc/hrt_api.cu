@@ -132,12 +132,12 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   if (nVert)
   {
     if (stride == 16)
-      HRT_CUDA(ctx, cudaMemcpyAsync(g.verts, vpos, 16 * nVert, cudaMemcpyHostToDevice, st));
+      HRT_CUDA(ctx, cudaMemcpyAsync(g.verts, vpos, 16 * nVert, cudaMemcpyDefault, st));
     uint8_t* raw = nullptr;
     if (stride != 16)
     {
       HRT_CUDA(ctx, cudaMallocAsync((void**)&raw, stride * nVert, st));
-      HRT_CUDA(ctx, cudaMemcpyAsync(raw, vpos, stride * nVert, cudaMemcpyHostToDevice, st));
+      HRT_CUDA(ctx, cudaMemcpyAsync(raw, vpos, stride * nVert, cudaMemcpyDefault, st));
     }
     const uint8_t* src = raw ? raw : reinterpret_cast<const uint8_t*>(g.verts);
     uint64_t blocks = (nVert + 255) / 256;
@@ -161,7 +161,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   uint32_t *keysAlt = nullptr, *valsAlt = nullptr, *parent = nullptr, *visit = nullptr;
   void* scratch = nullptr;
   HRT_CUDA(ctx, cudaMallocAsync((void**)&dIdx, sizeof(uint32_t) * nIdx, st));
-  HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * nIdx, cudaMemcpyHostToDevice, st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * nIdx, cudaMemcpyDefault, st));
   HRT_CUDA(ctx, dalloc(&g.keys, N, bytes));
   HRT_CUDA(ctx, dalloc(&g.vals, N, bytes));
   HRT_CUDA(ctx, dalloc(&g.keysUnsorted, N, bytes));

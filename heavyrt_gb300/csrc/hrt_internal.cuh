@@ -106,7 +106,7 @@ int cuda_fail(hrt_context* ctx, cudaError_t e, const char* what);
 // Frees a geometry's device arrays (not those of a batch-built geometry).
 void free_geom(Geom& g);
 // Builds one geometry (LBVH, and the 4-wide collapse for a 4-wide layout) on
-// s->ctx->stream from host arrays; synchronous.  The scene supplies the
+// s->ctx->stream from host or device arrays; synchronous.  The scene supplies the
 // context and the BVH4 merge option; it is not modified.
 int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
                    uint64_t stride, int layout);

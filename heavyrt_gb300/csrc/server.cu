@@ -55,8 +55,9 @@ struct SceneRec
   uint64_t              lastUse = 0;
   uint64_t              reserved = 0;  // bytes held against the budget
   Geom                  geom;
-  std::vector<uint8_t>  hostVerts;     // inputs of a pending build
-  std::vector<uint32_t> hostIdx;
+  void*                 dVerts = nullptr;  // inputs of a pending build, copied to the device
+  uint32_t*             dIdx = nullptr;
+  uint64_t              nIdx = 0;
   uint64_t              nVert = 0, stride = 0;
 };
 
@@ -68,6 +69,7 @@ struct hrt_server
 {
   hrt_context*            ctx = nullptr;  // the caller's context (device)
   hrt_context             bctx;           // builder's stream
+  cudaStream_t            stageStream = nullptr;  // copies of new scenes' inputs
   hrt_scene               proto;          // layout / merge options for builds
   hrt_server_config       cfg{};
   TraceConfig             trace[2];
@@ -120,6 +122,8 @@ uint64_t estimate_scene_bytes(uint64_t nTris, uint64_t nVert, int layout)
   if (layout != HRT_LAYOUT_BVH2) b += N * (layout == HRT_LAYOUT_BVH4_F32 ? sizeof(Node4F32) : sizeof(Node4F16));
   // transient build arrays (ping-pong, parents, visit counters, sort scratch)
   b += N * 4 * 6 + radix_sort_scratch_bytes((uint32_t)N) + 4 * 1024 * 32;
+  // the staged copy of the inputs (16-byte vertices, indices) held until the build
+  b += 16 * nVert + 12 * (uint64_t)nTris;
   return b;
 }
 
@@ -332,15 +336,18 @@ void builder_main(hrt_server* S)
     const uint32_t slot = S->buildQueue.front();
     S->buildQueue.pop_front();
     SceneRec& sc = S->scenes[slot];
-    std::vector<uint8_t> verts;
-    std::vector<uint32_t> idx;
-    verts.swap(sc.hostVerts);
-    idx.swap(sc.hostIdx);
-    const uint64_t nVert = sc.nVert, stride = sc.stride;
+    void* dVerts = sc.dVerts;
+    uint32_t* dIdx = sc.dIdx;
+    sc.dVerts = nullptr;
+    sc.dIdx = nullptr;
+    const uint64_t nVert = sc.nVert, nIdx = sc.nIdx, stride = sc.stride;
     lk.unlock();
     Geom g;
-    int st = build_geometry(&S->proto, g, reinterpret_cast<const float*>(verts.data()), nVert, idx.data(), idx.size(),
-                            stride, S->cfg.layout);
+    int st = build_geometry(&S->proto, g, reinterpret_cast<const float*>(dVerts), nVert, dIdx, nIdx, stride,
+                            S->cfg.layout);
+    // the staged inputs are released in stream order, after the build's copies
+    if (dVerts) cudaFreeAsync(dVerts, S->bctx.stream);
+    if (dIdx) cudaFreeAsync(dIdx, S->bctx.stream);
     InstanceDesc d;
     if (st == HRT_OK)
     {
@@ -456,11 +463,14 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
     destroy_slots(S);
     if (S->dTable) cudaFree(S->dTable);
     if (S->bctx.stream) cudaStreamDestroy(S->bctx.stream);
+    if (S->stageStream) cudaStreamDestroy(S->stageStream);
     delete S;
     return cuda_fail(ctx, e, what);
   };
   cudaError_t e = cudaStreamCreateWithFlags(&S->bctx.stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(e, "builder stream");
+  e = cudaStreamCreateWithFlags(&S->stageStream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(e, "staging stream");
   e = cudaMalloc((void**)&S->dTable, sizeof(InstanceDesc) * c.maxScenes);
   if (e != cudaSuccess) return bail(e, "scene table");
   e = cudaMemset(S->dTable, 0, sizeof(InstanceDesc) * c.maxScenes);  // valid = 0 everywhere
@@ -515,6 +525,8 @@ int hrt_server_destroy(hrt_server* S)
   for (Geom& g : S->toFree) free_geom(g);
   for (auto& kv : S->tickets) delete kv.second;
   cudaFree(S->dTable);
+  cudaStreamSynchronize(S->stageStream);
+  cudaStreamDestroy(S->stageStream);
   cudaStreamDestroy(S->bctx.stream);
   delete S;
   return HRT_OK;
@@ -532,20 +544,48 @@ int hrt_server_add_scene(hrt_server* S, const float* vpos, uint64_t nVert, const
   if ((nVert && !vpos) || (nIdx && !idx)) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "null vertex or index pointer");
   if (nIdx / 3 > HRT_MAX_TRIS_PER_GEOM) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^24-1 triangles in one scene");
   if (nVert > 0xFFFFFFFFull) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^32-1 vertices in one scene");
-  const uint64_t need = estimate_scene_bytes(nIdx / 3, nVert, S->cfg.layout);
-  // copy the inputs before taking the lock (the caller owns them only for the call)
-  std::vector<uint8_t> hv(vByteStride * nVert);
-  std::vector<uint32_t> hi(idx, idx + nIdx);
-  if (nVert) std::memcpy(hv.data(), vpos, hv.size());
-  std::lock_guard<std::mutex> g(S->mu);
-  if (S->stop) return fail(ctx, HRT_ERR_STATE, "server is shutting down");
+  const uint64_t need =
+      estimate_scene_bytes(nIdx / 3, nVert, S->cfg.layout) + (vByteStride > 16 ? (vByteStride - 16) * nVert : 0);
+  // Copy the inputs to the device before taking the lock (the caller owns
+  // them only for the call): one copy, at full link speed from page-locked
+  // memory; the builder reads them from there.
+  cudaSetDevice(ctx->device);
+  void* dV = nullptr;
+  uint32_t* dI = nullptr;
+  auto unstage = [&]() {
+    if (dV) cudaFreeAsync(dV, S->stageStream);
+    if (dI) cudaFreeAsync(dI, S->stageStream);
+    dV = nullptr;
+    dI = nullptr;
+  };
+  {
+    cudaError_t e = cudaSuccess;
+    if (nVert) e = cudaMallocAsync(&dV, vByteStride * nVert, S->stageStream);
+    if (e == cudaSuccess && nIdx) e = cudaMallocAsync((void**)&dI, 4 * nIdx, S->stageStream);
+    if (e == cudaSuccess && nVert)
+      e = cudaMemcpyAsync(dV, vpos, vByteStride * nVert, cudaMemcpyDefault, S->stageStream);
+    if (e == cudaSuccess && nIdx) e = cudaMemcpyAsync(dI, idx, 4 * nIdx, cudaMemcpyDefault, S->stageStream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S->stageStream);
+    if (e != cudaSuccess)
+    {
+      unstage();
+      return cuda_fail(ctx, e, "staging a new scene's inputs");
+    }
+  }
+  std::unique_lock<std::mutex> g(S->mu);
+  auto reject = [&](int status, const char* msg) {
+    g.unlock();
+    unstage();
+    return fail(ctx, status, msg);
+  };
+  if (S->stop) return reject(HRT_ERR_STATE, "server is shutting down");
   // admission: evict idle evictable scenes, least recently used first - and
   // only when evicting all of them would make room
   uint64_t freeable = 0;
   for (const SceneRec& sc : S->scenes)
     if (sc.state == HRT_SCENE_READY && sc.evictable && sc.refs == 0) freeable += sc.reserved;
   if (S->resident - freeable + need > S->cfg.memoryBudget)
-    return fail(ctx, HRT_ERR_OUT_OF_MEMORY, "scene does not fit the memory budget");
+    return reject(HRT_ERR_OUT_OF_MEMORY, "scene does not fit the memory budget");
   while (S->resident + need > S->cfg.memoryBudget)
   {
     int64_t victim = -1;
@@ -556,11 +596,11 @@ int hrt_server_add_scene(hrt_server* S, const float* vpos, uint64_t nVert, const
           (victim < 0 || sc.lastUse < S->scenes[victim].lastUse))
         victim = i;
     }
-    if (victim < 0) return fail(ctx, HRT_ERR_OUT_OF_MEMORY, "scene does not fit the memory budget");
+    if (victim < 0) return reject(HRT_ERR_OUT_OF_MEMORY, "scene does not fit the memory budget");
     release_scene(S, (uint32_t)victim);
     S->stats.evictions++;
   }
-  if (S->freeSlots.empty()) return fail(ctx, HRT_ERR_CAPACITY, "scene table full");
+  if (S->freeSlots.empty()) return reject(HRT_ERR_CAPACITY, "scene table full");
   const uint32_t slot = S->freeSlots.back();
   S->freeSlots.pop_back();
   SceneRec& sc = S->scenes[slot];
@@ -569,8 +609,9 @@ int hrt_server_add_scene(hrt_server* S, const float* vpos, uint64_t nVert, const
   sc.refs = 0;
   sc.lastUse = ++S->useClock;
   sc.reserved = need;
-  sc.hostVerts.swap(hv);
-  sc.hostIdx.swap(hi);
+  sc.dVerts = dV;
+  sc.dIdx = dI;
+  sc.nIdx = nIdx;
   sc.nVert = nVert;
   sc.stride = vByteStride;
   S->resident += need;

@@ -327,9 +327,10 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
 /* Finishes queued builds and requests, then frees everything. */
 int hrt_server_destroy(hrt_server* server);
 /* Queues the build of a scene of one triangle geometry under the identity
- * (arguments as hrt_add_geom_triangles3f; the arrays are copied before the call
- * returns).  Requests may be submitted at once; they run when the build is
- * done.  evictable = 0 keeps the scene until it is removed.
+ * (arguments as hrt_add_geom_triangles3f; the arrays are copied to the device
+ * before the call returns, at full link speed when they are page-locked).
+ * Requests may be submitted at once; they run when the build is done.
+ * evictable = 0 keeps the scene until it is removed.
  * HRT_ERR_OUT_OF_MEMORY when it cannot fit the budget even after evictions. */
 int hrt_server_add_scene(hrt_server* server, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
                          uint64_t vByteStride, int evictable, uint32_t* sceneId);
@@ -346,8 +347,9 @@ int hrt_server_submit(hrt_server* server, uint32_t sceneId, int kind, const floa
 int hrt_server_wait(hrt_server* server, uint64_t ticket, double timeoutSeconds, hrt_request_info* info);
 int hrt_server_get_stats(hrt_server* server, hrt_server_stats* stats);
 /* Bytes a scene of nVert vertices and nTris triangles reserves against the
- * budget while it is built (its arrays plus the build's transient arrays);
- * once built it holds its actual, smaller size. */
+ * budget while it is built (its arrays, the build's transient arrays and the
+ * device copy of its inputs, for vertices of up to 16 bytes); once built it
+ * holds its actual, smaller size. */
 int hrt_server_scene_bytes(const hrt_server* server, uint64_t nVert, uint64_t nTris, uint64_t* bytes);
 
 /* ---------------------------------------------------------------- ray generation on the GPU
