@@ -81,10 +81,10 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from heavyrt_gb300 import replicas
+
+    r = replicas.from_env()
+    return r.rank, r.world, r.local
 
 
 def measured_peak():
@@ -745,12 +745,12 @@ def run_served(ctx, args) -> dict:
 def run_engine(args):
     import torch
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
+    from heavyrt_gb300 import replicas
 
-        dist.init_process_group("nccl")
+    rk = replicas.from_env()
+    rank, world, local = rk.rank, rk.world, rk.local
+    torch.cuda.set_device(local)
+    replicas.init(rk, "nccl")
     from heavyrt_gb300 import Context, PinnedBuffer, SceneRT
     from heavyrt_gb300 import engine as E
 
@@ -835,8 +835,7 @@ def run_engine(args):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier(rk)
     torch.cuda.synchronize()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -845,19 +844,15 @@ def run_engine(args):
         step(evs[k])
     t_end.record(stream)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier(rk)
     clk = clocks.stop()
     total_ms = t_start.elapsed_time(t_end)
     eye_ms = [e[0].elapsed_time(e[1]) for e in evs]
     ao_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(rk, total_ms, "cuda")  # the slowest replica's time
     ms_per_step = total_ms / args.steps
     rays_per_step = n_eye + n_ao
-    value = world * rays_per_step / (ms_per_step * 1e-3) / 1e6
+    value = replicas.job_throughput(rk, rays_per_step, ms_per_step) / 1e6
     if args.ncu:
         print(json.dumps({"ncu_run": True, "ms_per_step": ms_per_step, "value": value}), flush=True)
         return 0
@@ -884,8 +879,8 @@ def run_engine(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_value = world * rays_per_step / e2e_s / 1e6
+    e2e_s = replicas.max_over_ranks(rk, (time.perf_counter() - t0) / args.steps, "cuda")
+    e2e_value = replicas.job_throughput(rk, rays_per_step, 1e3 * e2e_s) / 1e6
     got_any = pin_any.array(np.uint8)[:n_ao].copy()
 
     # the same frame with its rays made on the device: camera parameters in,
@@ -916,8 +911,8 @@ def run_engine(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         n_ao_dev = raygen_step()
-    rg_s = (time.perf_counter() - t0) / args.steps
-    raygen_e2e = {"value": round(world * (n_eye + n_ao_dev) / rg_s / 1e6, 3), "unit": UNIT,
+    rg_s = replicas.max_over_ranks(rk, (time.perf_counter() - t0) / args.steps, "cuda")
+    raygen_e2e = {"value": round(replicas.job_throughput(rk, n_eye + n_ao_dev, 1e3 * rg_s) / 1e6, 3), "unit": UNIT,
                   "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(32 * n_eye + n_ao_dev),
                   "ao_rays": int(n_ao_dev), "ao_rays_equal_host_count": bool(n_ao_dev == n_ao),
                   "anyhit_equal_host_frame": bool(np.array_equal(pin_any_d[:n_ao_dev].numpy(), got_any))
@@ -1017,8 +1012,7 @@ def run_engine(args):
         line["config"]["e2e_anyhit_matches_oracle_sample"] = bool(np.array_equal(got_any[::step_ao].astype(bool), want))
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish(rk)
     return 0
 
 
