@@ -961,6 +961,7 @@ def run_engine(args):
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     lay = "" if args.layout == "bvh2" else f"_{args.layout}"
     traffic = profile_traffic(f"trace_{dom}{lay}_heightfield2M.txt")
+    eye_achieved = eye_bytes / (eye_avg * 1e-3) / 1e9  # the coherent (eye-ray) kernel
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -983,7 +984,10 @@ def run_engine(args):
                      "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "algorithmic_bytes_per_launch": int(dom_bytes),
                      "note": f"algorithmic bytes = {node_bytes} B per node fetch + 36 B per triangle test + ray in/out; "
-                             "node fetches mostly hit L1/L2, so frac can exceed 1 (see traffic)"},
+                             "node fetches mostly hit L1/L2, so frac can exceed 1 (see traffic)",
+                     "coherent_eye": {"kernel": "k_trace<nearest>", "achieved": round(eye_achieved, 1),
+                                      "frac": round(eye_achieved / peak, 4), "algorithmic_bytes_per_launch": int(eye_bytes),
+                                      "traffic": profile_traffic(f"trace_nearest{lay}_heightfield2M.txt")}},
         "clocks": clk,
     }
     line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
