@@ -4,9 +4,16 @@ Workload (one "step" = one frame of HeavyRT's RTAO renderer on the
 1024 x 1024-quad heightfield, 2,097,152 triangles):
   * 1920 x 1080 eye rays, RayQuery_NearestHit;
   * 16 cosine-weighted AO rays per primary hit, RayQuery_AnyHit.
-value = (eye rays + AO rays) / step time, inputs resident in HBM.
+value = (eye rays + AO rays) / step time, inputs resident in HBM, on the
+        quantised-node scene (BVH4 FP16) with autotuned launch shapes;
+        "plain" = the binary FP32 tree (the reference's decisions) on the same rays.
 e2e   = the same through the host-pointer C-ABI calls: every step copies the
-        step's rays from pinned host memory and the results back.
+        step's rays from pinned host memory and the results back;
+        e2e_device_raygen = the frame with its rays made on the device.
+Further sections of the same JSON line: "batched" (256 scenes, segmented build
+and graph-captured launches vs per-scene plain), "served" (request stream over
+64 resident scenes: p50/p99 vs one-at-a-time plain), "precision" (heightfield
++ 8.4M-triangle soup in every node layout, hit agreement, FP64 t error).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -497,11 +504,14 @@ def run_precision(ctx, args) -> dict:
         t_ao /= steps
         anyf = d_any.cpu().numpy()
         pairs_eye, _ = sc.query_counters(0, d_eye.data_ptr(), n_eye, sh)
-        pairs_ao, _ = sc.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+        pairs_ao, tris_ao = sc.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+        ao_bytes = LAYOUT_NODE_BYTES[layout] * pairs_ao + TRI_BYTES * tris_ao + (RAY_BYTES + 1) * n_ao
+        pk, _ = measured_peak()
         entry = {"eye_ms": round(t_eye, 4), "ao_ms": round(t_ao, 4),
                  "mrays_s": round((n_eye + n_ao) / (t_eye + t_ao) / 1e3, 2), "build_ms": round(build_ms, 3),
                  "node_fetches_per_eye_ray": round(pairs_eye / n_eye, 3),
                  "node_fetches_per_ao_ray": round(pairs_ao / n_ao, 3),
+                 "ao_roofline_frac": round(ao_bytes / (t_ao * 1e-3) / 1e9 / pk, 4),
                  "bvh_bytes": int(sum(sc.geom_info(g)["bytes"] for g in gids))}
         if ref_hits is None:
             ref_hits, ref_any = hits, anyf
@@ -949,6 +959,14 @@ def run_engine(args):
                  "nearest_mismatch": int(np.count_nonzero(diff & (hp[:, 0] != hq[:, 0]))),
                  "nearest_equal_t_other_triangle": int(np.count_nonzero(diff & (hp[:, 0] == hq[:, 0]))),
                  "anyhit_mismatch": int(np.count_nonzero(p_any.cpu().numpy() != d_any.cpu().numpy()))}
+        if not args.ncu:
+            pp_eye, pt_eye = ps.query_counters(0, d_eye.data_ptr(), n_eye, sh)
+            p_bytes = 64 * pp_eye + TRI_BYTES * pt_eye + RAY_BYTES * n_eye + 32 * n_eye
+            p_ach = p_bytes / (pe_ms * 1e-3) / 1e9
+            pk, _ = measured_peak()
+            plain["coherent_eye_roofline"] = {"achieved": round(p_ach, 1), "frac": round(p_ach / pk, 4),
+                                              "algorithmic_bytes_per_launch": int(p_bytes),
+                                              "node_pairs_per_eye_ray": round(pp_eye / n_eye, 3)}
         ps.close()
 
     # roofline of the dominant kernel
