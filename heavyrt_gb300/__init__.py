@@ -14,12 +14,14 @@ from .engine import (  # noqa: F401
     Context,
     CreateSceneRT,
     DeleteSceneRT,
+    Frame,
     HrtError,
     PinnedBuffer,
     SceneRT,
+    rtao_qmc_tile,
 )
 
 __all__ = [
     "BUILD_HIGH", "BUILD_LOW", "BUILD_MEDIUM", "BUILD_REFIT", "HIT_DTYPE", "NODE_DTYPE", "Context", "CreateSceneRT",
-    "DeleteSceneRT", "HrtError", "PinnedBuffer", "SceneRT",
+    "DeleteSceneRT", "Frame", "HrtError", "PinnedBuffer", "SceneRT", "rtao_qmc_tile",
 ]

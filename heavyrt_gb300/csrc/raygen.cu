@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "hrt_internal.cuh"
+#include "raygen_common.cuh"
 
 using namespace hrt;
 using namespace hrt::api;
@@ -27,28 +28,7 @@ namespace
 constexpr int kThreads = 256;
 
 // ---------------------------------------------------------------- renderer eye rays
-struct Mat4
-{
-  float m[16];  // column-major
-};
-
-__device__ __forceinline__ void mat_vec(const Mat4& M, const float v[4], float o[4])
-{
-  const float* m = M.m;
-#pragma unroll
-  for (int r = 0; r < 4; r++)
-    o[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[r], v[0]), __fmul_rn(m[4 + r], v[1])), __fmul_rn(m[8 + r], v[2])),
-                     __fmul_rn(m[12 + r], v[3]));
-}
-
-__device__ __forceinline__ void normalize3(float v[3])
-{
-  const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(v[0], v[0]), __fmul_rn(v[1], v[1])), __fmul_rn(v[2], v[2])));
-  const float inv = __fdiv_rn(1.0f, len);
-  v[0] = __fmul_rn(v[0], inv);
-  v[1] = __fmul_rn(v[1], inv);
-  v[2] = __fmul_rn(v[2], inv);
-}
+using hrt::rg::Mat4;
 
 __global__ void __launch_bounds__(kThreads) k_eye_rays(Mat4 projInv, Mat4 worldViewInv, uint32_t width, uint32_t height,
                                                        float tNear, float tFar, float4* __restrict__ rays)
@@ -57,23 +37,7 @@ __global__ void __launch_bounds__(kThreads) k_eye_rays(Mat4 projInv, Mat4 worldV
   for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kThreads)
   {
     const uint32_t y = (uint32_t)(i / width), x = (uint32_t)(i % width);
-    const float fx = __fdiv_rn(__fadd_rn((float)x, 0.5f), (float)width);
-    const float fy = __fdiv_rn(__fadd_rn((float)y, 0.5f), (float)height);
-    const float pos[4] = {__fsub_rn(__fmul_rn(2.0f, fx), 1.0f), __fadd_rn(__fmul_rn(-2.0f, fy), 1.0f), 0.0f, 1.0f};
-    float p[4];
-    mat_vec(projInv, pos, p);
-    float d[3] = {__fdiv_rn(p[0], p[3]), __fdiv_rn(p[1], p[3]), __fdiv_rn(p[2], p[3])};
-    normalize3(d);
-    const float o0[4] = {0.0f, 0.0f, 0.0f, 1.0f};
-    const float o1[4] = {__fadd_rn(0.0f, __fmul_rn(100.0f, d[0])), __fadd_rn(0.0f, __fmul_rn(100.0f, d[1])),
-                         __fadd_rn(0.0f, __fmul_rn(100.0f, d[2])), 1.0f};
-    float a[4], b[4];
-    mat_vec(worldViewInv, o0, a);
-    mat_vec(worldViewInv, o1, b);
-    float dir[3] = {__fsub_rn(b[0], a[0]), __fsub_rn(b[1], a[1]), __fsub_rn(b[2], a[2])};
-    normalize3(dir);
-    rays[2 * i + 0] = make_float4(a[0], a[1], a[2], tNear);
-    rays[2 * i + 1] = make_float4(dir[0], dir[1], dir[2], tFar);
+    hrt::rg::eye_ray(projInv, worldViewInv, x, y, width, height, tNear, tFar, rays[2 * i + 0], rays[2 * i + 1]);
   }
 }
 

@@ -121,6 +121,12 @@ class ServerStats(C.Structure):
 SCENE_BUILDING, SCENE_READY, SCENE_FAILED, SCENE_EVICTED = 0, 1, 2, 3
 
 
+class RtaoParams(C.Structure):  # hrt_rtao_params
+    _fields_ = [("projInv", C.c_float * 16), ("worldViewInv", C.c_float * 16), ("zNear", C.c_float),
+                ("zFar", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32), ("aoMaxRadius", C.c_float),
+                ("power", C.c_float)]
+
+
 class HrtError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"hrt status {status}: {message}")
@@ -199,6 +205,16 @@ def lib() -> C.CDLL:
         "hrt_geom_load": (i32, [vp, C.c_char_p, C.POINTER(u32)]),
         "hrt_gen_pinhole_rays": (i32, [vp, vp, vp, vp, C.c_float, u32, u32, C.c_float, C.c_float, vp, vp]),
         "hrt_gen_ao_rays": (i32, [vp, u64, vp, vp, u64, u32, C.c_float, C.c_float, vp, vp, u64, C.POINTER(u64), vp]),
+        "hrt_frame_create": (i32, [vp, C.POINTER(vp)]),
+        "hrt_frame_destroy": (i32, [vp]),
+        "hrt_frame_render_eye": (i32, [vp, vp, vp, vp, u32, u32, vp, vp]),
+        "hrt_rtao_qmc_table": (i32, [vp]),
+        "hrt_rtao_qmc_tile": (i32, [u32, vp]),
+        "hrt_frame_set_ao_tile": (i32, [vp, vp, u32]),
+        "hrt_frame_set_normals": (i32, [vp, u32, vp, u64]),
+        "hrt_frame_render_rtao": (i32, [vp, vp, C.POINTER(RtaoParams), vp, vp, vp]),
+        "hrt_frame_get_buffer": (i32, [vp, i32, C.POINTER(vp), C.POINTER(u64)]),
+        "hrt_frame_read_buffer": (i32, [vp, i32, vp, u64, C.POINTER(u64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -587,6 +603,104 @@ class Server:
     def close(self):
         if self._h:
             lib().hrt_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+AO_TILE_SIZE = 128
+HRT_MAX_AO_RAYS_PER_PIXEL = 1024
+FRAME_EYE_RAYS, FRAME_RAY_PIXEL, FRAME_EYE_HITS, FRAME_POSITIONS = 0, 1, 2, 3
+FRAME_VISIBILITY, FRAME_AO_PIXEL, FRAME_AO_RAYS, FRAME_AO_HITS = 4, 5, 6, 7
+
+
+def rtao_qmc_table() -> np.ndarray:
+    """The direction numbers of RTAO's quasi-random generator (hrt_rtao_qmc_table), uint32 [4, 31]."""
+    out = np.empty((4, 31), np.uint32)
+    st = lib().hrt_rtao_qmc_table(_ptr(out))
+    if st != HRT_OK:
+        raise HrtError(st, "hrt_rtao_qmc_table")
+    return out
+
+
+def rtao_qmc_tile(rays_per_pixel: int) -> np.ndarray:
+    """RTAO's 128x128 AO sample tile (hrt_rtao_qmc_tile): float32 [128*128*R, 2]."""
+    out = np.empty((AO_TILE_SIZE * AO_TILE_SIZE * rays_per_pixel, 2), np.float32)
+    st = lib().hrt_rtao_qmc_tile(rays_per_pixel, _ptr(out))
+    if st != HRT_OK:
+        raise HrtError(st, f"hrt_rtao_qmc_tile({rays_per_pixel})")
+    return out
+
+
+class Frame:
+    """Frames of HeavyRT's example renderers on the device (hrt_frame): colours go to
+    a device buffer (a pointer), the frame's own buffers stay on the device."""
+
+    _BUF = {FRAME_EYE_RAYS: (np.float32, 8), FRAME_RAY_PIXEL: (np.uint32, 1), FRAME_EYE_HITS: (np.uint32, 8),
+            FRAME_POSITIONS: (np.float32, 4), FRAME_VISIBILITY: (np.float32, 1), FRAME_AO_PIXEL: (np.uint32, 1),
+            FRAME_AO_RAYS: (np.float32, 8), FRAME_AO_HITS: (np.uint8, 1)}
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._h = C.c_void_p()
+        self.ctx.check(lib().hrt_frame_create(self.ctx.handle, C.byref(self._h)), "hrt_frame_create")
+
+    def render_eye(self, scene: "SceneRT", proj_inv, world_view_inv, width: int, height: int, colors_ptr: int,
+                   stream: int = 0):
+        pi = np.ascontiguousarray(np.asarray(proj_inv, np.float32).T)
+        wi = np.ascontiguousarray(np.asarray(world_view_inv, np.float32).T)
+        self.ctx.check(lib().hrt_frame_render_eye(self._h, scene._h, _ptr(pi), _ptr(wi), width, height,
+                                                  C.c_void_p(colors_ptr), C.c_void_p(stream)), "hrt_frame_render_eye")
+
+    def set_ao_tile(self, tile: np.ndarray, rays_per_pixel: int):
+        t = np.ascontiguousarray(tile, np.float32)
+        if t.size != AO_TILE_SIZE * AO_TILE_SIZE * rays_per_pixel * 2:
+            raise ValueError("tile must hold 128*128*rays_per_pixel float pairs")
+        self.ctx.check(lib().hrt_frame_set_ao_tile(self._h, _ptr(t), rays_per_pixel), "hrt_frame_set_ao_tile")
+
+    def set_normals(self, geom_id: int, normals: np.ndarray):
+        nn = np.ascontiguousarray(normals, np.float32).reshape(-1, 4)
+        self.ctx.check(lib().hrt_frame_set_normals(self._h, geom_id, _ptr(nn), nn.shape[0]), "hrt_frame_set_normals")
+
+    def render_rtao(self, scene: "SceneRT", proj_inv, world_view_inv, width: int, height: int, colors_ptr: int,
+                    z_near: float = 0.0, z_far: float = 3.4028234663852886e38, ao_max_radius: float = 2.0,
+                    power: float = 1.0, norm_matrices=None, stream: int = 0):
+        """norm_matrices: (nInst, 4, 4) row-major (identity for every instance when None)."""
+        p = RtaoParams()
+        p.projInv[:] = np.asarray(proj_inv, np.float32).T.reshape(-1).tolist()
+        p.worldViewInv[:] = np.asarray(world_view_inv, np.float32).T.reshape(-1).tolist()
+        p.zNear, p.zFar, p.width, p.height = z_near, z_far, width, height
+        p.aoMaxRadius, p.power = ao_max_radius, power
+        n_inst = scene.GetInstNum()
+        if norm_matrices is None:
+            norm_matrices = np.broadcast_to(np.eye(4, dtype=np.float32), (max(n_inst, 1), 4, 4))
+        nm = np.ascontiguousarray(np.transpose(np.asarray(norm_matrices, np.float32).reshape(-1, 4, 4), (0, 2, 1)))
+        self.ctx.check(lib().hrt_frame_render_rtao(self._h, scene._h, C.byref(p), _ptr(nm), C.c_void_p(colors_ptr),
+                                                   C.c_void_p(stream)), "hrt_frame_render_rtao")
+
+    def buffer(self, which: int):
+        """(device pointer, count, numpy dtype, values per entry) of one of the last frame's buffers."""
+        d, n = C.c_void_p(), C.c_uint64()
+        self.ctx.check(lib().hrt_frame_get_buffer(self._h, which, C.byref(d), C.byref(n)), "hrt_frame_get_buffer")
+        dt, per = self._BUF[which]
+        return (d.value or 0), int(n.value), dt, per
+
+    def read(self, which: int) -> np.ndarray:
+        """A copy of one of the last frame's buffers on the host: (count, values) or (count,)."""
+        _, n, dt, per = self.buffer(which)
+        out = np.empty((n, per) if per > 1 else n, dt)
+        nb = C.c_uint64()
+        self.ctx.check(lib().hrt_frame_read_buffer(self._h, which, _ptr(out), out.nbytes, C.byref(nb)),
+                       "hrt_frame_read_buffer")
+        return out
+
+    def close(self):
+        if self._h:
+            lib().hrt_frame_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

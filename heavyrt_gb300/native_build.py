@@ -5,7 +5,7 @@ Outputs (git-ignored, rebuilt on every machine that runs them):
   heavyrt_gb300/_build/libhrt_workload.so  seeded scene / ray generators
   oracle/_build/liboracle.so               CPU restatement of the reference (test oracle)
   oracle/_ref/ref_harness{,_fast}          the reference's own CPU code (only where its
-                                           sources are present)
+  oracle/_ref/{raygen,render}_harness      sources are present)
 
 Translation units compile in parallel; a target is rebuilt only when one of its
 sources is newer than it.
@@ -26,8 +26,9 @@ ORACLE = ROOT / "oracle"
 INCLUDE = ROOT / "include"
 
 CUDA_SOURCES = ["radix_sort.cu", "build.cu", "build_batch.cu", "bvh4.cu", "trace.cu", "trace_l0.cu", "trace_l1.cu",
-                "trace_l2.cu", "trace_l3.cu", "hrt_api.cu", "server.cu", "raygen.cu", "formats.cu"]
-CUDA_HEADERS = ["hrt_common.cuh", "build_common.cuh", "hrt_kernels.cuh", "hrt_internal.cuh", "trace_impl.cuh"]
+                "trace_l2.cu", "trace_l3.cu", "hrt_api.cu", "server.cu", "raygen.cu", "render.cu", "formats.cu"]
+CUDA_HEADERS = ["hrt_common.cuh", "build_common.cuh", "hrt_kernels.cuh", "hrt_internal.cuh", "trace_impl.cuh",
+                "raygen_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
 HOST_CFLAGS = ["-O3", "-fPIC", "-ffp-contract=off", "-Wall"]

@@ -81,6 +81,47 @@ def camera_rays(eye, target, up, fov_deg: float, width: int, height: int, tmin: 
     return rays
 
 
+def perspective(fov_deg: float, aspect: float, near: float, far: float) -> np.ndarray:
+    """OpenGL-style projection matrix (row-major 4x4, float64)."""
+    t = 1.0 / np.tan(np.radians(fov_deg) / 2.0)
+    m = np.zeros((4, 4))
+    m[0, 0], m[1, 1] = t / aspect, t
+    m[2, 2], m[2, 3], m[3, 2] = (far + near) / (near - far), 2.0 * far * near / (near - far), -1.0
+    return m
+
+
+def look_at(eye, target, up) -> np.ndarray:
+    """World-to-view matrix of a camera at eye looking at target (row-major 4x4, float64)."""
+    eye, target, up = (np.asarray(x, np.float64) for x in (eye, target, up))
+    f = (target - eye) / np.linalg.norm(target - eye)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[:3, 3] = -m[:3, :3] @ eye
+    return m
+
+
+def camera_inverses(eye, target, up, fov_deg: float, width: int, height: int):
+    """(projInv, worldViewInv) as float32 row-major 4x4, the renderers' camera inputs."""
+    p = np.linalg.inv(perspective(fov_deg, width / height, 0.01, 100.0)).astype(np.float32)
+    v = np.linalg.inv(look_at(eye, target, up)).astype(np.float32)
+    return p, v
+
+
+def vertex_normals(verts: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """Area-weighted vertex normals (float4, w = 0) of an indexed mesh."""
+    p = np.asarray(verts, np.float64).reshape(-1, 4)[:, :3]
+    t = np.asarray(idx, np.int64).reshape(-1, 3)
+    fn = np.cross(p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]])
+    n = np.zeros_like(p)
+    for k in range(3):
+        np.add.at(n, t[:, k], fn)
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-30)
+    return np.concatenate([n, np.zeros((n.shape[0], 1))], axis=1).astype(np.float32)
+
+
 def sphere_rays(seed: int, n: int, radius: float = 3.0):
     rays = np.empty((n, 8), dtype=np.float32)
     lib().hrt_wl_sphere_rays(seed, n, radius, _p(rays))

@@ -383,6 +383,90 @@ int hrt_gen_ao_rays(hrt_scene* scene, uint64_t seed, const float* eyeRays, const
                     uint32_t perHit, float length, float offset, float* aoRays, uint32_t* owner, uint64_t capacity,
                     uint64_t* count, void* stream);
 
+/* ---------------------------------------------------------------- renderer frames
+ * Whole frames of HeavyRT's two example renderers on the device (replacing
+ * EyeRayCaster::CastRaySingleBlock, examples/01_eye_rays/eye_ray_host.cpp:332-362,
+ * and RTAO::CalcAOBlock, examples/02_rtao/rtao.cpp:28-44, over this engine's
+ * scene): rays generated, traced and shaded on the GPU, every value equal bit
+ * for bit to the renderers' own kernels run on the same hits.  A frame object
+ * owns its buffers (grown on demand) and is used by one thread at a time.
+ * Colours: width * height uint32 RGBA in device memory, row-major pixels
+ * (x, y at y * width + x).  Rays are traced in EyeRayCaster's packed order
+ * (kernel_PackXY, eye_ray.cpp:106-134: 4x4 blocks in 2x2 super-blocks) when
+ * both sides are multiples of 8, row by row otherwise; the images are the same. */
+typedef struct hrt_frame hrt_frame;
+int hrt_frame_create(hrt_context* ctx, hrt_frame** out);
+int hrt_frame_destroy(hrt_frame* frame);
+
+/* EyeRayCaster frame (eye_ray.cpp:10-74): kernel_InitEyeRay (tNear 0, tFar
+ * MAXFLOAT), nearest hit, colour 0 on a miss, else the renderer's 20-entry
+ * palette at primId % 20 (primId = the hit's sorted position, as the
+ * reference's BVH2CommonRT returns it).  Asynchronous on `stream`. */
+int hrt_frame_render_eye(hrt_frame* frame, hrt_scene* scene, const float projInv[16], const float worldViewInv[16],
+                         uint32_t width, uint32_t height, uint32_t* colors, void* stream);
+
+/* RTAO's quasi-random AO samples (RTAO::InitQMCTable, examples/02_rtao/rtao_host.cpp:383-414):
+ * hrt_rtao_qmc_table: the 4 x 31 direction numbers of initQuasirandomGenerator
+ * (core/common/qmc_sobol_niederreiter.cpp:179-186); hrt_rtao_qmc_tile: the
+ * 128 x 128 texel tile, raysPerPixel (r1, r2) pairs per texel (2 floats each,
+ * texel (x, y) at (y * 128 + x) * raysPerPixel), host memory, no context. */
+#define HRT_AO_TILE_SIZE          128
+#define HRT_MAX_AO_RAYS_PER_PIXEL 1024
+int hrt_rtao_qmc_table(uint32_t* table);
+int hrt_rtao_qmc_tile(uint32_t raysPerPixel, float* tile);
+
+/* The RTAO frame's inputs that outlive a frame: the sample tile (host memory,
+ * 128 * 128 * raysPerPixel float pairs, e.g. from hrt_rtao_qmc_tile; sets the
+ * frame's raysPerPixel) and each geometry's vertex normals (float4 per vertex
+ * in the geometry's vertex order, host or device memory; RTAO::m_vNorm4f). */
+int hrt_frame_set_ao_tile(hrt_frame* frame, const float* tile, uint32_t raysPerPixel);
+int hrt_frame_set_normals(hrt_frame* frame, uint32_t geomId, const float* normals, uint64_t nVerts);
+
+/* RTAO's camera and AO settings (RTAO::m_projInv, m_worldViewInv, m_zNearFar,
+ * m_aoMaxRadius, m_power); matrices column-major. */
+typedef struct hrt_rtao_params
+{
+  float    projInv[16];
+  float    worldViewInv[16];
+  float    zNear, zFar;
+  uint32_t width, height;
+  float    aoMaxRadius;
+  float    power;
+} hrt_rtao_params;
+
+/* RTAO frame (RTAO::CalcAO, rtao.cpp:46-60, for every pixel): kernel_InitEyeRay,
+ * nearest hit, kernel_TraceEyeRay2's hit point and packed shading normal
+ * (vertex normals of the hit triangle through normMatrices[instId]: 16 floats
+ * per instance, column-major, host memory; RTAO::m_normMatrices),
+ * kernel_InitAORay's raysPerPixel rays for every pixel with a hit, their
+ * occlusion (any hit), kernel_AO2Color.  Synchronises `stream` once (to size
+ * the AO launch); the rest is asynchronous. */
+int hrt_frame_render_rtao(hrt_frame* frame, hrt_scene* scene, const hrt_rtao_params* params, const float* normMatrices,
+                          uint32_t* colors, void* stream);
+
+/* Device buffers of the frame's last render, valid until the next one:
+ *   EYE_RAYS   8 floats per traced eye ray, in trace order      (count = pixels)
+ *   RAY_PIXEL  uint32 pixel index of each traced eye ray       (count = pixels)
+ *   EYE_HITS   hrt_hit per traced eye ray                       (count = pixels)
+ *   POSITIONS  float4 per pixel: hit point + packed normal in w (RTAO; y = 1e7 without a hit)
+ *   VISIBILITY float per pixel: unoccluded AO samples           (RTAO; 0 without a hit)
+ *   AO_PIXEL   uint32 pixel of each AO slot (pixels with a hit, trace order)
+ *   AO_RAYS    8 floats per AO ray: slot s, sample z at s * raysPerPixel + z
+ *   AO_HITS    uint8 occlusion flag per AO ray */
+#define HRT_FRAME_EYE_RAYS   0
+#define HRT_FRAME_RAY_PIXEL  1
+#define HRT_FRAME_EYE_HITS   2
+#define HRT_FRAME_POSITIONS  3
+#define HRT_FRAME_VISIBILITY 4
+#define HRT_FRAME_AO_PIXEL   5
+#define HRT_FRAME_AO_RAYS    6
+#define HRT_FRAME_AO_HITS    7
+int hrt_frame_get_buffer(const hrt_frame* frame, int which, const void** data, uint64_t* count);
+/* The same buffer copied into dst (host or device memory, capacityBytes long)
+ * after the device has finished; *bytes receives its size (HRT_ERR_CAPACITY
+ * when dst is too small).  Synchronous. */
+int hrt_frame_read_buffer(const hrt_frame* frame, int which, void* dst, uint64_t capacityBytes, uint64_t* bytes);
+
 /* ---------------------------------------------------------------- on-disk formats */
 
 /* VSGF meshes, HeavyRT's binary mesh files (examples/loader/cmesh.cpp:80-173):

@@ -791,3 +791,350 @@ void ora_eye_rays(const float* projInv, const float* worldViewInv, uint32_t widt
       r[4] = dir[0]; r[5] = dir[1]; r[6] = dir[2]; r[7] = tFar;
     }
 }
+
+/* ---------------------------------------------------------------- renderer frames
+ * The frame kernels of HeavyRT's two example renderers, restated per ray /
+ * per pixel as the reference evaluates them under the LiteMath stand-in
+ * (float operations left to right; the unqualified sin, cos, pow and sqrt
+ * that examples/render_common.h calls on float arguments resolve to the double
+ * functions of <math.h>, std::sqrt / std::pow / std::abs to the float ones). */
+
+/* EyeRayCaster's palette (examples/01_eye_rays/eye_ray.h:105-113). */
+static const uint32_t ora_palette[20] = {
+    0xffe6194bu, 0xff3cb44bu, 0xffffe119u, 0xff0082c8u, 0xfff58231u, 0xff911eb4u, 0xff46f0f0u,
+    0xfff032e6u, 0xffd2f53cu, 0xfffabebeu, 0xff008080u, 0xffe6beffu, 0xffaa6e28u, 0xfffffac8u,
+    0xff800000u, 0xffaaffc3u, 0xff808000u, 0xffffd8b1u, 0xff000080u, 0xff808080u};
+
+/* kernel_PackXY with SuperBlockIndex2DOpt (examples/01_eye_rays/eye_ray.cpp:106-134):
+ * packed[offset(x, y)] = y << 16 | x, 4x4 blocks inside 2x2 super-blocks.
+ * Offsets at or past width*height are skipped (the reference writes past its
+ * array there: widths or heights that are not multiples of 8). */
+void ora_pack_xy(uint32_t width, uint32_t height, uint32_t* packed)
+{
+  const uint32_t n = width * height;
+  for (uint32_t y = 0; y < height; y++)
+    for (uint32_t x = 0; x < width; x++)
+    {
+      const uint32_t local = (y & 3u) * 4u + (x & 3u);
+      const uint32_t bx = x >> 2, by = y >> 2;
+      const uint32_t localH = (by & 1u) * 2u + (bx & 1u);
+      const uint32_t wH = (width >> 2) >> 1;
+      const uint32_t off = ((bx >> 1) + (by >> 1) * wH) * 64u + localH * 16u + local;
+      if (off < n) packed[off] = ((y << 16) & 0xFFFF0000u) | (x & 0x0000FFFFu);
+    }
+}
+
+/* kernel_RayTrace (examples/01_eye_rays/eye_ray.cpp:49-74), one colour per hit. */
+void ora_eye_colors(const ora_hit* hits, uint64_t n, uint32_t* colors)
+{
+  for (uint64_t i = 0; i < n; i++)
+    colors[i] = hits[i].primId == 0xFFFFFFFFu ? 0u : ora_palette[hits[i].primId % 20u];
+}
+
+/* Niederreiter base-2 direction numbers for 4 dimensions, as
+ * initQuasirandomGenerator computes them (core/common/qmc_sobol_niederreiter.cpp:
+ * GeneratePolynomials :13-67, GenerateCJ :81-174, table :179-186; Bratley, Fox and
+ * Niederreiter, ACM TOMACS 2(3), 1992).  Dimension d uses the d-th irreducible
+ * polynomial over GF(2) in numeric order (x, x+1, x^2+x+1, x^3+x+1).  Output bit r
+ * (r = 0 most significant) of row i is v[i + r mod e] of the linear recurrence
+ * with characteristic polynomial P^(r div e + 1), started from r div e * e zeros
+ * followed by ones up to that polynomial's degree.  table[d*31 + i] keeps bits
+ * 62..32 of the reference's 63-bit words. */
+static int gf2_deg(uint32_t p)
+{
+  int d = 31;
+  while (d > 0 && !((p >> d) & 1u)) d--;
+  return d;
+}
+
+static uint32_t gf2_rem(uint32_t a, uint32_t b)
+{
+  const int db = gf2_deg(b);
+  while (a != 0 && gf2_deg(a) >= db) a ^= b << (gf2_deg(a) - db);
+  return a;
+}
+
+void ora_qmc_table(uint32_t* table)
+{
+  uint32_t polys[4] = {2u, 0u, 0u, 0u};
+  for (int n = 1; n < 4; n++)
+    for (uint32_t p = polys[n - 1] + 1u;; p++)
+    {
+      int irreducible = 1;
+      for (int k = 0; k < n && irreducible; k++) irreducible = gf2_rem(p, polys[k]) != 0u;
+      if (irreducible) { polys[n] = p; break; }
+    }
+  for (int d = 0; d < 4; d++)
+  {
+    const uint32_t P = polys[d];
+    const int e = gf2_deg(P);
+    uint8_t pc[33];                      /* P's coefficients, pc[k] = coefficient of x^(e-k) */
+    for (int k = 0; k <= e; k++) pc[k] = (uint8_t)((P >> (e - k)) & 1u);
+    uint8_t b[64] = {1}, t[64];          /* b = P^q, b[k] = coefficient of x^(deg-k) */
+    int m = 0;
+    for (int i = 0; i < 31; i++) table[d * 31 + i] = 0u;
+    for (int r = 0; r < 31; r++)
+    {
+      const int u = r % e;
+      if (u == 0)
+      {
+        const int m1 = m;
+        memcpy(t, b, sizeof(b));
+        m = m1 + e;
+        for (int i = 0; i <= m; i++)
+        {
+          uint8_t c = 0;
+          for (int k = 0; k <= e; k++)
+            if (i - k >= 0 && i - k <= m1) c ^= (uint8_t)(pc[k] & t[i - k]);
+          b[i] = c;
+        }
+      }
+      uint8_t v[96];
+      const int m1 = m - e;
+      const int len = 31 + e;
+      for (int i = 0; i < len; i++)
+      {
+        if (i < m1) v[i] = 0;
+        else if (i < m) v[i] = 1;
+        else
+        {
+          uint8_t s = 0;
+          for (int k = 1; k <= m; k++) s ^= (uint8_t)(v[i - k] & b[k]);
+          v[i] = s;
+        }
+      }
+      for (int i = 0; i < 31; i++) table[d * 31 + i] |= (uint32_t)v[i + u] << (30 - r);
+    }
+  }
+}
+
+/* rndQmcSobolN (core/common/qmc_sobol_niederreiter.h:11-20). */
+static float ora_qmc(const uint32_t* table, uint32_t pos, int dim)
+{
+  uint32_t result = 0;
+  for (int bit = 0; bit < 31; bit++, pos >>= 1)
+    if (pos & 1u) result ^= table[bit + dim * 31];
+  return (float)(result + 1u) * (1.0f / (float)0x80000001u);
+}
+
+/* RTAO::InitQMCTable (examples/02_rtao/rtao_host.cpp:383-414): 128x128 texels of
+ * raysPerPixel (r1, r2) pairs; unfilled entries stay (0, 0). */
+void ora_rtao_tile(uint32_t raysPerPixel, float* tile)
+{
+  uint32_t table[4 * 31];
+  ora_qmc_table(table);
+  const size_t n = (size_t)128 * 128 * raysPerPixel;
+  uint32_t* filled = (uint32_t*)calloc(128 * 128, sizeof(uint32_t));
+  memset(tile, 0, sizeof(float) * 2 * n);
+  for (size_t i = 0; i < n; i++)
+  {
+    const float x = ora_qmc(table, (uint32_t)i, 0), y = ora_qmc(table, (uint32_t)i, 1);
+    const float z = ora_qmc(table, (uint32_t)i, 2), w = ora_qmc(table, (uint32_t)i, 3);
+    int ix = (int)(x * 128.0f), iy = (int)(y * 128.0f);
+    if (ix >= 128) ix = 127;
+    if (iy >= 128) iy = 127;
+    const uint32_t cell = (uint32_t)iy * 128u + (uint32_t)ix;
+    if (filled[cell] < raysPerPixel)
+    {
+      float* o = tile + 2 * ((size_t)cell * raysPerPixel + filled[cell]);
+      o[0] = z;
+      o[1] = w;
+      filled[cell]++;
+    }
+  }
+  free(filled);
+}
+
+/* LiteMath normalize under the stand-in: v * (1 / std::sqrt(dot(v, v))). */
+static void ora_norm3(float v[3])
+{
+  const float l = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  const float inv = 1.0f / l;
+  v[0] = v[0] * inv;
+  v[1] = v[1] * inv;
+  v[2] = v[2] * inv;
+}
+
+/* mymul3x3 (examples/render_common.h:14-17): the full column sum with w = 0. */
+static void ora_mul3x3(const float* m, const float v[3], float o[3])
+{
+  for (int r = 0; r < 3; r++) o[r] = ((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * 0.0f;
+}
+
+static inline float ora_dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+/* C++ float -> int conversion, with the NaN case (undefined in C++) mapped to 0. */
+static inline int ora_f2i(float f) { return f != f ? 0 : (int)f; }
+
+/* encodeNormal / decodeNormal (examples/render_common.h:114-137). */
+static uint32_t ora_encode_normal(const float n[3])
+{
+  const int x = ora_f2i(n[0] * 32767.0f);
+  const int y = ora_f2i(n[1] * 32767.0f);
+  const uint32_t sign = (n[2] >= 0) ? 0u : 1u;
+  const uint32_t sx = ((uint32_t)(x & 0xfffe) | sign);
+  const uint32_t sy = ((uint32_t)(y & 0xffff) << 16);
+  return sx | sy;
+}
+
+static void ora_decode_normal(uint32_t a, float n[3])
+{
+  const uint32_t ex = a & 0x0000FFFFu, ey = (a & 0xFFFF0000u) >> 16;
+  const float sign = (ex & 1u) != 0 ? -1.0f : 1.0f;
+  const float k = 1.0f / 32767.0f;
+  n[0] = (float)(int16_t)(uint16_t)(ex & 0xfffeu) * k;
+  n[1] = (float)(int16_t)(uint16_t)(ey & 0xffffu) * k;
+  n[2] = sign * sqrtf(fmax_std((1.0f - n[0] * n[0]) - n[1] * n[1], 0.0f));
+}
+
+/* RTAO::kernel_TraceEyeRay2 after its query (examples/02_rtao/rtao.cpp:81-131):
+ * the hit position pulled back by 0.9999995 t and the shading normal (vertex
+ * normals interpolated, both normals through the instance's normal matrix,
+ * flipped towards the triangle's side facing the ray) packed into w.  A hit's
+ * triangle is read from the geometry's index buffer in sorted order at the
+ * hit's primId (the sorted position), i.e. the triangle that was hit.
+ * sortedIdx[g], verts[g] (float4), normals[g] (float4) per geometry;
+ * normMatrices: 16 floats per instance, column-major. */
+void ora_rtao_positions(const float* eyeRays, const ora_hit* hits, uint64_t n, const uint32_t* const* sortedIdx,
+                        const float* const* verts, const float* const* normals, const float* normMatrices,
+                        float* positions)
+{
+  for (uint64_t i = 0; i < n; i++)
+  {
+    const ora_hit h = hits[i];
+    float* out = positions + 4 * i;
+    if (h.geomId == 0xFFFFFFFFu)
+    {
+      const float up[3] = {0.0f, 1.0f, 0.0f};
+      const uint32_t e = ora_encode_normal(up);
+      out[0] = 0.0f; out[1] = 10000000.0f; out[2] = 0.0f;
+      memcpy(out + 3, &e, 4);
+      continue;
+    }
+    const float* o = eyeRays + 8 * i;
+    const float* d = o + 4;
+    const float u = h.coords[0], v = h.coords[1];
+    const float s = 0.9999995f * h.t;
+    const float p[3] = {o[0] + s * d[0], o[1] + s * d[1], o[2] + s * d[2]};
+    const uint32_t* tri = sortedIdx[h.geomId] + 3 * (size_t)h.primId;
+    const float* A = verts[h.geomId] + 4 * (size_t)tri[0];
+    const float* B = verts[h.geomId] + 4 * (size_t)tri[1];
+    const float* Cv = verts[h.geomId] + 4 * (size_t)tri[2];
+    const float e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
+    const float e2[3] = {Cv[0] - A[0], Cv[1] - A[1], Cv[2] - A[2]};
+    const float tn0[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const float* nA = normals[h.geomId] + 4 * (size_t)tri[0];
+    const float* nB = normals[h.geomId] + 4 * (size_t)tri[1];
+    const float* nC = normals[h.geomId] + 4 * (size_t)tri[2];
+    const float w0 = (1.0f - u) - v;
+    float hn0[3];
+    for (int k = 0; k < 3; k++) hn0[k] = (w0 * nA[k] + v * nB[k]) + u * nC[k];
+    const float* M = normMatrices + 16 * (size_t)h.instId;
+    float hn[3], tn[3];
+    ora_mul3x3(M, hn0, hn);
+    ora_norm3(hn);
+    ora_mul3x3(M, tn0, tn);
+    ora_norm3(tn);
+    if (ora_dot3(tn, hn) < 0.0f)
+      for (int k = 0; k < 3; k++) hn[k] = hn[k] * -1.0f;
+    const float dotp = ora_dot3(d, tn);
+    const float flip = (dotp > 1e-5f) ? -1.0f : 1.0f;
+    const float fn[3] = {hn[0] * flip, hn[1] * flip, hn[2] * flip};
+    const uint32_t e = ora_encode_normal(fn);
+    out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
+    memcpy(out + 3, &e, 4);
+  }
+}
+
+/* RTAO::kernel_InitAORay (examples/02_rtao/rtao.cpp:147-165) with
+ * MapSampleToCosineDistribution (power 1), CoordinateSystem and OffsRayPos
+ * (examples/render_common.h:38-112), for every pixel (row-major) and sample z:
+ * aoRays[(pix*R + z)*8 ..] = {pos, 0, dir, aoMaxRadius}; pixels without a hit
+ * (positions y >= 1e7) get no rays (left as they are). */
+void ora_rtao_ao_rays(const float* positions, uint32_t width, uint32_t height, uint32_t R, const float* tile,
+                      float aoMaxRadius, float* aoRays)
+{
+  const float twoPi = 6.28318530717958647692f;
+  for (uint32_t y = 0; y < height; y++)
+    for (uint32_t x = 0; x < width; x++)
+    {
+      const size_t pix = (size_t)y * width + x;
+      const float* pos = positions + 4 * pix;
+      if (pos[1] >= 10000000.0f) continue;
+      uint32_t enc;
+      memcpy(&enc, pos + 3, 4);
+      float nrm[3];
+      ora_decode_normal(enc, nrm);
+      /* CoordinateSystem(normal): nx, then nz = cross(normal, nx) */
+      float nx[3], invLen;
+      if (fabsf(nrm[0]) > fabsf(nrm[1]))
+      {
+        invLen = 1.0f / sqrtf(nrm[0] * nrm[0] + nrm[2] * nrm[2]);
+        nx[0] = (-1.0f * nrm[2]) * invLen; nx[1] = 0.0f; nx[2] = nrm[0] * invLen;
+      }
+      else
+      {
+        invLen = (float)(1.0f / sqrt((double)(nrm[1] * nrm[1] + nrm[2] * nrm[2])));
+        nx[0] = 0.0f; nx[1] = nrm[2] * invLen; nx[2] = (-1.0f * nrm[1]) * invLen;
+      }
+      const float v3[3] = {nrm[1] * nx[2] - nrm[2] * nx[1], nrm[2] * nx[0] - nrm[0] * nx[2], nrm[0] * nx[1] - nrm[1] * nx[0]};
+      const float* ny = v3;   /* after the swap: ny = cross, nz = the normal */
+      const float* nz = nrm;
+      const float invSign = ora_dot3(nrm, nrm) > 0.0f ? 1.0f : -1.0f;
+      const float eps = fmax_std(fmax_std(fabsf(pos[0]), fmax_std(fabsf(pos[1]), fabsf(pos[2]))), 2.0f * 2e-5f) * 2e-5f;
+      for (uint32_t z = 0; z < R; z++)
+      {
+        const float* uv = tile + 2 * (((size_t)(y % 128u) * 128u + (x % 128u)) * R + z);
+        const float r1 = uv[0], r2 = uv[1];
+        const float phi = twoPi * r1;
+        const float sinPhi = (float)sin((double)phi);
+        const float cosPhi = (float)cos((double)phi);
+        const float cosTheta = (float)pow((double)(1.0f - r2), (double)(1.0f / (1.0f + 1.0f)));
+        const float sinTheta = (float)sqrt((double)(1.0f - cosTheta * cosTheta));
+        const float dev[3] = {sinTheta * cosPhi, sinTheta * sinPhi, cosTheta};
+        float res[3];
+        for (int k = 0; k < 3; k++) res[k] = (nx[k] * dev[0] + ny[k] * dev[1]) + nz[k] * dev[2];
+        if (invSign * ora_dot3(res, nrm) < 0.0f)
+          for (int k = 0; k < 3; k++) res[k] = ((-1.0f * nx[k]) * dev[0] + ny[k] * dev[1]) - nz[k] * dev[2];
+        const float s2 = ora_dot3(res, nrm) < 0.0f ? -1.0f : 1.0f;
+        const float se = s2 * eps;
+        float* r = aoRays + 8 * (pix * R + z);
+        r[0] = pos[0] + se * nrm[0];
+        r[1] = pos[1] + se * nrm[1];
+        r[2] = pos[2] + se * nrm[2];
+        r[3] = 0.0f;
+        r[4] = res[0]; r[5] = res[1]; r[6] = res[2];
+        r[7] = aoMaxRadius;
+      }
+    }
+}
+
+/* kernel_TraceAORay (closest-hit variant, attenuation 0) summed over the
+ * samples and kernel_AO2Color (examples/02_rtao/rtao.cpp:62-73,167-185):
+ * visibility = number of unoccluded samples, colour = grey of
+ * powf(visibility / R, power) quantised to 8 bits; 0 for pixels without a hit.
+ * aoHit: one flag per (pixel, sample). */
+void ora_rtao_colors(const float* positions, const uint8_t* aoHit, uint64_t nPix, uint32_t R, float power,
+                     float* visibility, uint32_t* colors)
+{
+  for (uint64_t p = 0; p < nPix; p++)
+  {
+    const int hit = positions[4 * p + 1] < 10000000.0f;
+    float vis = 0.0f;
+    if (hit)
+      for (uint32_t z = 0; z < R; z++) vis = vis + (aoHit[p * R + z] ? 0.0f : 1.0f);
+    visibility[p] = vis;
+    if (!hit)
+    {
+      colors[p] = 0u;
+      continue;
+    }
+    const float normCoeff = 1.0f / (float)(1u * R);
+    const float a = vis * normCoeff;
+    const float res = powf(a, power);
+    const float c = fmin_lm(fmax_lm(res, 0.0f), 1.0f) * 255.0f;
+    const float c1 = fmin_lm(fmax_lm(1.0f, 0.0f), 1.0f) * 255.0f;
+    const int g = ora_f2i(c), w = ora_f2i(c1);
+    colors[p] = (uint32_t)(g + (g << 8) + (g << 16) + (int)((uint32_t)w << 24));
+  }
+}

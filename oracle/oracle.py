@@ -47,6 +47,14 @@ def lib() -> C.CDLL:
         L.ora_trace.restype = i32
         L.ora_trace.argtypes = [vp, vp, u64, i32, vp, vp, i32, vp]
         L.ora_eye_rays.argtypes = [vp, vp, u32, u32, C.c_float, C.c_float, vp]
+        f32 = C.c_float
+        L.ora_pack_xy.argtypes = [u32, u32, vp]
+        L.ora_eye_colors.argtypes = [vp, u64, vp]
+        L.ora_qmc_table.argtypes = [vp]
+        L.ora_rtao_tile.argtypes = [u32, vp]
+        L.ora_rtao_positions.argtypes = [vp, vp, u64, vp, vp, vp, vp, vp]
+        L.ora_rtao_ao_rays.argtypes = [vp, u32, u32, u32, vp, f32, vp]
+        L.ora_rtao_colors.argtypes = [vp, vp, u64, u32, f32, vp, vp]
         _lib = L
     return _lib
 
@@ -226,3 +234,143 @@ def run_reference(verts, idx, rays=None, fast: bool = False, threads: int = 0) -
             out["hits"] = rd(".hits", HIT_DTYPE)
             out["any"] = rd(".any", np.uint8).astype(bool)
     return out
+
+
+# ---------------------------------------------------------------- renderer frames
+AO_TILE = 128
+AO_HIT_BACK = 10000000.0
+
+
+def pack_xy(width: int, height: int) -> np.ndarray:
+    """EyeRayCaster's packed pixel order: entry k = y << 16 | x of the k-th traced pixel."""
+    out = np.zeros(width * height, np.uint32)
+    lib().ora_pack_xy(width, height, _p(out))
+    return out
+
+
+def eye_colors(hits: np.ndarray) -> np.ndarray:
+    h = np.ascontiguousarray(hits).view(HIT_DTYPE)
+    out = np.empty(h.shape[0], np.uint32)
+    lib().ora_eye_colors(_p(h), h.shape[0], _p(out))
+    return out
+
+
+def qmc_table() -> np.ndarray:
+    out = np.empty((4, 31), np.uint32)
+    lib().ora_qmc_table(_p(out))
+    return out
+
+
+def rtao_tile(rays_per_pixel: int) -> np.ndarray:
+    out = np.empty((AO_TILE * AO_TILE * rays_per_pixel, 2), np.float32)
+    lib().ora_rtao_tile(rays_per_pixel, _p(out))
+    return out
+
+
+def rtao_positions(eye_rays, hits, geoms, norm_matrices) -> np.ndarray:
+    """kernel_TraceEyeRay2's shading.  geoms: per geometry (sorted index buffer,
+    float4 vertices, float4 normals); norm_matrices: (nInst, 4, 4) row-major."""
+    r = np.ascontiguousarray(eye_rays, np.float32).reshape(-1, 8)
+    h = np.ascontiguousarray(hits).view(HIT_DTYPE)
+    keep = []
+    arrs = []
+    for g in geoms:
+        si = np.ascontiguousarray(g[0], np.uint32).reshape(-1)
+        v = np.ascontiguousarray(g[1], np.float32).reshape(-1, 4)
+        nn = np.ascontiguousarray(g[2], np.float32).reshape(-1, 4)
+        keep += [si, v, nn]
+        arrs.append((si.ctypes.data, v.ctypes.data, nn.ctypes.data))
+    n_g = max(len(arrs), 1)
+    ptr_i = (C.c_void_p * n_g)(*[a[0] for a in arrs])
+    ptr_v = (C.c_void_p * n_g)(*[a[1] for a in arrs])
+    ptr_n = (C.c_void_p * n_g)(*[a[2] for a in arrs])
+    m = np.ascontiguousarray(np.transpose(np.asarray(norm_matrices, np.float32).reshape(-1, 4, 4), (0, 2, 1)))
+    out = np.empty((r.shape[0], 4), np.float32)
+    lib().ora_rtao_positions(_p(r), _p(h), r.shape[0], C.cast(ptr_i, C.c_void_p), C.cast(ptr_v, C.c_void_p),
+                             C.cast(ptr_n, C.c_void_p), _p(m), _p(out))
+    return out
+
+
+def rtao_ao_rays(positions, width: int, height: int, rays_per_pixel: int, tile, ao_max_radius: float):
+    """kernel_InitAORay for every (pixel, sample): (W*H*R, 8) rays, zero where the pixel has no hit."""
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+    t = np.ascontiguousarray(tile, np.float32).reshape(-1, 2)
+    out = np.zeros((width * height * rays_per_pixel, 8), np.float32)
+    lib().ora_rtao_ao_rays(_p(pos), width, height, rays_per_pixel, _p(t), ao_max_radius, _p(out))
+    return out
+
+
+def rtao_colors(positions, ao_hit, rays_per_pixel: int, power: float = 1.0):
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+    a = np.ascontiguousarray(ao_hit, np.uint8).reshape(-1)
+    vis = np.empty(pos.shape[0], np.float32)
+    col = np.empty(pos.shape[0], np.uint32)
+    lib().ora_rtao_colors(_p(pos), _p(a), pos.shape[0], rays_per_pixel, power, _p(vis), _p(col))
+    return vis, col
+
+
+def eye_frame(bvh: "OracleBVH", proj_inv, world_view_inv, width: int, height: int) -> np.ndarray:
+    """EyeRayCaster's frame over one geometry (identity instance): colours, row-major."""
+    rays = eye_rays(proj_inv, world_view_inv, width, height, 0.0, 3.4028234663852886e38)
+    return eye_colors(bvh.trace(rays))
+
+
+def rtao_frame(bvh: "OracleBVH", verts, normals, proj_inv, world_view_inv, width: int, height: int, z_near: float,
+               z_far: float, rays_per_pixel: int, ao_max_radius: float, power: float = 1.0, norm_matrix=None) -> dict:
+    """RTAO's frame over one geometry (identity instance), every stage."""
+    nm = np.eye(4, dtype=np.float32) if norm_matrix is None else np.asarray(norm_matrix, np.float32)
+    rays = eye_rays(proj_inv, world_view_inv, width, height, z_near, z_far)
+    hits = bvh.trace(rays)
+    pos = rtao_positions(rays, hits, [(bvh.sorted_indices(), verts, normals)], nm[None])
+    tile = rtao_tile(rays_per_pixel)
+    ao = rtao_ao_rays(pos, width, height, rays_per_pixel, tile, ao_max_radius)
+    valid = np.repeat(pos[:, 1] < AO_HIT_BACK, rays_per_pixel)
+    ao_hit = np.zeros(ao.shape[0], np.uint8)
+    if valid.any():
+        ao_hit[valid] = bvh.trace(ao[valid], any_hit=True).astype(np.uint8)
+    vis, col = rtao_colors(pos, ao_hit, rays_per_pixel, power)
+    return {"eye_rays": rays, "eye_hits": hits, "positions": pos, "tile": tile, "ao_rays": ao, "ao_valid": valid,
+            "ao_hit": ao_hit, "visibility": vis, "colors": col}
+
+
+def _render_params(proj_inv, world_view_inv, width, height, z_near, z_far, rays_per_pixel, radius, power,
+                   norm_matrix) -> bytes:
+    pi = np.asarray(proj_inv, np.float32).T.reshape(-1)
+    wi = np.asarray(world_view_inv, np.float32).T.reshape(-1)
+    nm = np.asarray(np.eye(4) if norm_matrix is None else norm_matrix, np.float32).T.reshape(-1)
+    return (np.concatenate([pi, wi]).astype(np.float32).tobytes() + np.array([width, height], np.uint32).tobytes() +
+            np.array([z_near, z_far], np.float32).tobytes() + np.array([rays_per_pixel], np.uint32).tobytes() +
+            np.array([radius, power], np.float32).tobytes() + nm.tobytes())
+
+
+def reference_render(kind: str, verts, idx, proj_inv, world_view_inv, width: int, height: int, normals=None,
+                     z_near: float = 0.0, z_far: float = 3.4028234663852886e38, rays_per_pixel: int = 4,
+                     radius: float = 1.0, power: float = 1.0, norm_matrix=None):
+    """The reference renderers' own frame kernels (oracle/_ref/render_harness), or None
+    where the reference sources are absent.  kind: "eye", "rtao" or "qmc"."""
+    exe = HERE / "_ref" / "render_harness"
+    if not exe.exists():
+        return None
+    with tempfile.TemporaryDirectory() as td:
+        pre = os.path.join(td, "out")
+        rd = lambda s, dt: np.fromfile(pre + s, dtype=dt)  # noqa: E731
+        if kind == "qmc":
+            subprocess.run([str(exe), "qmc", str(rays_per_pixel), pre], check=True)
+            return {"qmc": rd(".qmc", np.uint32).reshape(4, 31), "tile": rd(".tile", np.float32).reshape(-1, 2)}
+        sp, pp = os.path.join(td, "scene.bin"), os.path.join(td, "params.bin")
+        _write_scene(sp, verts, idx)
+        with open(pp, "wb") as f:
+            f.write(_render_params(proj_inv, world_view_inv, width, height, z_near, z_far, rays_per_pixel, radius,
+                                   power, norm_matrix))
+        if kind == "eye":
+            subprocess.run([str(exe), "eye", sp, pp, pre], check=True)
+            return {"packed": rd(".packed", np.uint32), "colors": rd(".colors", np.uint32)}
+        npth = os.path.join(td, "normals.bin")
+        nn = np.ascontiguousarray(normals, np.float32).reshape(-1, 4)
+        with open(npth, "wb") as f:
+            f.write(b"HRTNRM01" + np.array([nn.shape[0]], np.uint64).tobytes() + nn.tobytes())
+        subprocess.run([str(exe), "rtao", sp, npth, pp, pre], check=True)
+        return {"eye_rays": rd(".eye_rays", np.float32).reshape(-1, 8), "eye_hits": rd(".eye_hits", HIT_DTYPE),
+                "positions": rd(".positions", np.float32).reshape(-1, 4),
+                "ao_rays": rd(".ao_rays", np.float32).reshape(-1, 8), "ao_hit": rd(".ao_hit", np.uint8),
+                "visibility": rd(".visibility", np.float32), "colors": rd(".colors", np.uint32)}

@@ -79,6 +79,8 @@ namespace LiteMath
     vec4_t() : x(0), y(0), z(0), w(0) {}
     explicit vec4_t(T a) : x(a), y(a), z(a), w(a) {}
     vec4_t(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
+    // element-wise conversion, e.g. int4(float4) truncates each component
+    template <typename U> explicit vec4_t(const vec4_t<U>& o) : x(T(o.x)), y(T(o.y)), z(T(o.z)), w(T(o.w)) {}
     T&       operator[](int i)       { return (&x)[i]; }
     const T& operator[](int i) const { return (&x)[i]; }
   };
@@ -127,6 +129,9 @@ namespace LiteMath
   static inline float3 abs(float3 a) { return float3(abs(a.x), abs(a.y), abs(a.z)); }
   static inline float4 abs(float4 a) { return float4(abs(a.x), abs(a.y), abs(a.z), abs(a.w)); }
   static inline float3 sign(float3 a) { return float3(sign(a.x), sign(a.y), sign(a.z)); }
+  static inline float4 clamp(float4 u, float a, float b) { return float4(clamp(u.x, a, b), clamp(u.y, a, b), clamp(u.z, a, b), clamp(u.w, a, b)); }
+  // scalar given as any arithmetic type (the renderers' colour quantisation multiplies by an int)
+  static inline float4 operator*(float4 a, float s) { return float4(a.x * s, a.y * s, a.z * s, a.w * s); }
 
   static inline float  dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
   static inline float  dot(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }

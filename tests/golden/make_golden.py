@@ -1,8 +1,9 @@
 """Generate the golden vectors in tests/golden/ from HeavyRT's own CPU code.
 
-Runs the reference checker (oracle/_ref/ref_harness, compiled from the
-reference sources by oracle/Makefile.ref) on small seeded scenes and stores
-inputs and outputs in golden_*.npz.  The reference ships no golden vectors of
+Runs the reference checkers (oracle/_ref/ref_harness, raygen_harness and
+render_harness, compiled from the reference sources by oracle/Makefile.ref) on
+small seeded scenes and stores inputs and outputs in golden_*.npz,
+raygen_eye.npz and render_frames.npz.  The reference ships no golden vectors of
 its own for this path, so these fixtures are the pinned record of what its
 LBVH builder and BVH2CommonRT traversal produce.
 
@@ -52,24 +53,7 @@ def cases():
     yield "heightfield8x5_tnear", v, idx, rays
 
 
-def perspective(fov_deg, aspect, near, far):
-    t = 1.0 / np.tan(np.radians(fov_deg) / 2.0)
-    m = np.zeros((4, 4))
-    m[0, 0], m[1, 1] = t / aspect, t
-    m[2, 2], m[2, 3], m[3, 2] = (far + near) / (near - far), 2.0 * far * near / (near - far), -1.0
-    return m
-
-
-def look_at(eye, target, up):
-    eye, target, up = (np.asarray(x, np.float64) for x in (eye, target, up))
-    f = (target - eye) / np.linalg.norm(target - eye)
-    s = np.cross(f, up)
-    s /= np.linalg.norm(s)
-    u = np.cross(s, f)
-    m = np.eye(4)
-    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
-    m[:3, 3] = -m[:3, :3] @ eye
-    return m
+perspective, look_at = wl.perspective, wl.look_at
 
 
 def eye_ray_cases():
@@ -95,11 +79,67 @@ def make_eye_rays():
     np.savez_compressed(OUT / "raygen_eye.npz", **out)
 
 
+vertex_normals = wl.vertex_normals
+
+
+def render_cases():
+    """Frames of the two example renderers over a 48x48 heightfield: a packed-order
+    image (sides multiples of 8) and a row-order one with a z range and a
+    non-identity normal matrix."""
+    v, idx, _ = wl.heightfield(7, 48, 48)
+    nrm = vertex_normals(v, idx)
+    wv = np.linalg.inv(look_at((0.3, -1.7, 1.0), (0, 0, -0.1), (0, 0, 1))).astype(np.float32)
+    yield dict(name="a", verts=v, idx=idx, normals=nrm, width=64, height=48, z_near=0.0, z_far=3.4028234663852886e38,
+               rays_per_pixel=4, radius=0.3, power=1.0, norm_matrix=np.eye(4, dtype=np.float32),
+               proj_inv=np.linalg.inv(perspective(60.0, 64 / 48, 0.01, 100.0)).astype(np.float32), world_view_inv=wv)
+    yield dict(name="b", verts=v, idx=idx, normals=nrm, width=37, height=21, z_near=0.5, z_far=3.0,
+               rays_per_pixel=16, radius=0.1, power=1.0, norm_matrix=np.diag([1.0, 2.0, 0.5, 1.0]).astype(np.float32),
+               proj_inv=np.linalg.inv(perspective(50.0, 37 / 21, 0.01, 100.0)).astype(np.float32), world_view_inv=wv)
+
+
+def make_render():
+    """render_frames.npz: the example renderers' own frame kernels (oracle/_ref/render_harness)."""
+    import hashlib
+    out = {}
+    q = orc.reference_render("qmc", None, None, None, None, 0, 0, rays_per_pixel=4)
+    out["qmc_table"] = q["qmc"]
+    for r in (1, 3, 4, 16):
+        t = orc.reference_render("qmc", None, None, None, None, 0, 0, rays_per_pixel=r)["tile"]
+        out[f"tile_sha256_r{r}"] = np.frombuffer(hashlib.sha256(t.tobytes()).digest(), np.uint8)
+    for c in render_cases():
+        k = c["name"]
+        common = dict(verts=c["verts"], idx=c["idx"], proj_inv=c["proj_inv"], world_view_inv=c["world_view_inv"],
+                      width=c["width"], height=c["height"])
+        ref = orc.reference_render("rtao", normals=c["normals"], z_near=c["z_near"], z_far=c["z_far"],
+                                   rays_per_pixel=c["rays_per_pixel"], radius=c["radius"], power=c["power"],
+                                   norm_matrix=c["norm_matrix"], **common)
+        hit = ref["positions"][:, 1] < orc.AO_HIT_BACK
+        sel = np.repeat(hit, c["rays_per_pixel"])
+        for name in ("verts", "idx", "normals"):  # one scene for both frames
+            out[name] = c[name]
+        for name in ("proj_inv", "world_view_inv", "norm_matrix"):
+            out[f"{k}_{name}"] = c[name]
+        out[f"{k}_params"] = np.array([c["width"], c["height"], c["rays_per_pixel"]], np.uint32)
+        out[f"{k}_fparams"] = np.array([c["z_near"], c["z_far"], c["radius"], c["power"]], np.float32)
+        out[f"{k}_positions"] = ref["positions"]
+        out[f"{k}_ao_rays"] = ref["ao_rays"][sel]
+        out[f"{k}_ao_hit"] = ref["ao_hit"][sel]
+        out[f"{k}_visibility"] = np.where(hit, ref["visibility"], 0.0).astype(np.float32)
+        out[f"{k}_colors"] = ref["colors"]
+        if c["width"] % 8 == 0 and c["height"] % 8 == 0:  # the eye renderer's packing needs it
+            e = orc.reference_render("eye", **common)
+            out[f"{k}_eye_packed"] = e["packed"]
+            out[f"{k}_eye_colors"] = e["colors"]
+        print("render", k, c["width"], c["height"], int(hit.sum()), int(ref["ao_hit"][sel].sum()))
+    np.savez_compressed(OUT / "render_frames.npz", **out)
+
+
 def main():
     native_build.build_all()
     if orc.reference_harness() is None:
         raise SystemExit("reference sources not available: cannot regenerate golden vectors")
     make_eye_rays()
+    make_render()
     for name, v, idx, rays in cases():
         ref = orc.run_reference(v, idx, rays)
         np.savez_compressed(

@@ -44,3 +44,21 @@ def test_engine_is_sm103a(native):
     from heavyrt_gb300 import native_build
 
     assert "arch=compute_103a,code=sm_103a" in native_build.ARCH
+
+
+def test_rtao_sample_tile_is_host_code(native, host_libs):
+    """hrt_rtao_qmc_table / hrt_rtao_qmc_tile run on the host: RTAO's quasi-random
+    AO sample tile equals the oracle's (pinned against the reference's own
+    generator by tests/test_oracle.py) for several sample counts."""
+    import numpy as np
+    from heavyrt_gb300 import engine
+    from oracle import oracle as orc
+
+    np.testing.assert_array_equal(engine.rtao_qmc_table(), orc.qmc_table())
+    for r in (1, 2, 3, 4, 7, 16, 32):
+        np.testing.assert_array_equal(engine.rtao_qmc_tile(r).view(np.uint32), orc.rtao_tile(r).view(np.uint32))
+    L = engine.lib()
+    assert L.hrt_rtao_qmc_tile(0, None) == engine.HRT_ERR_INVALID_ARGUMENT
+    assert L.hrt_rtao_qmc_tile(engine.HRT_MAX_AO_RAYS_PER_PIXEL + 1, None) == engine.HRT_ERR_INVALID_ARGUMENT
+    assert L.hrt_frame_destroy(None) == engine.HRT_ERR_INVALID_ARGUMENT
+    assert L.hrt_frame_create(None, None) == engine.HRT_ERR_INVALID_ARGUMENT

@@ -124,3 +124,81 @@ def test_eye_rays_restatement_matches_reference_fixture(host_libs):
         live = orc.reference_eye_rays(p, v, w, h, tn, tf)
         if live is not None:
             np.testing.assert_array_equal(live.view(np.uint32), want.view(np.uint32))
+
+
+def _render_fixture():
+    return dict(np.load(GOLDEN / "render_frames.npz"))
+
+
+def _render_case(z, k):
+    w, h, r = (int(x) for x in z[f"{k}_params"])
+    zn, zf, rad, pw = (float(x) for x in z[f"{k}_fparams"])
+    return dict(proj_inv=z[f"{k}_proj_inv"], world_view_inv=z[f"{k}_world_view_inv"], width=w, height=h, z_near=zn,
+                z_far=zf, rays_per_pixel=r, radius=rad, power=pw, norm_matrix=z[f"{k}_norm_matrix"])
+
+
+def test_qmc_tile_restatement_matches_reference_fixture(host_libs):
+    """RTAO's quasi-random sample tile: the generator's direction table and the
+    binned tile equal the reference's (core/common/qmc_sobol_niederreiter.cpp,
+    examples/02_rtao/rtao_host.cpp:383-414)."""
+    import hashlib
+
+    from oracle import oracle as orc
+
+    z = _render_fixture()
+    np.testing.assert_array_equal(orc.qmc_table(), z["qmc_table"])
+    for r in (1, 3, 4, 16):
+        digest = np.frombuffer(hashlib.sha256(orc.rtao_tile(r).tobytes()).digest(), np.uint8)
+        np.testing.assert_array_equal(digest, z[f"tile_sha256_r{r}"])
+
+
+def test_render_frames_restatement_matches_reference_fixture(host_libs):
+    """The example renderers' frames restated in C (eye-ray renderer: packed order
+    and palette; RTAO: hit points with packed normals, AO rays, occlusion,
+    visibility, colours) equal the reference's own kernels on both fixture frames."""
+    from oracle import oracle as orc
+
+    z = _render_fixture()
+    b = orc.OracleBVH(z["verts"], z["idx"])
+    for k in ("a", "b"):
+        c = _render_case(z, k)
+        o = orc.rtao_frame(b, z["verts"], z["normals"], c["proj_inv"], c["world_view_inv"], c["width"], c["height"],
+                           c["z_near"], c["z_far"], c["rays_per_pixel"], c["radius"], c["power"], c["norm_matrix"])
+        np.testing.assert_array_equal(o["positions"].view(np.uint32), z[f"{k}_positions"].view(np.uint32))
+        np.testing.assert_array_equal(o["ao_rays"][o["ao_valid"]].view(np.uint32), z[f"{k}_ao_rays"].view(np.uint32))
+        np.testing.assert_array_equal(o["ao_hit"][o["ao_valid"]], z[f"{k}_ao_hit"])
+        np.testing.assert_array_equal(o["visibility"].view(np.uint32), z[f"{k}_visibility"].view(np.uint32))
+        np.testing.assert_array_equal(o["colors"], z[f"{k}_colors"])
+        assert 0 < o["ao_valid"].mean() < 1 and 0 < z[f"{k}_ao_hit"].mean() < 1
+        if f"{k}_eye_packed" in z:
+            np.testing.assert_array_equal(orc.pack_xy(c["width"], c["height"]), z[f"{k}_eye_packed"])
+            np.testing.assert_array_equal(orc.eye_frame(b, c["proj_inv"], c["world_view_inv"], c["width"], c["height"]),
+                                          z[f"{k}_eye_colors"])
+
+
+def test_render_frames_match_reference_live(host_libs):
+    """Where the reference sources are present: a fresh frame of each renderer
+    (another camera, 8 samples) from the reference's own kernels equals the
+    restatement."""
+    from oracle import oracle as orc
+
+    z = _render_fixture()
+    c = _render_case(z, "a")
+    v, idx, nrm = z["verts"], z["idx"], z["normals"]
+    wv = np.linalg.inv(np.asarray(np.linalg.inv(c["world_view_inv"]), np.float64) @
+                       np.array([[0.96, -0.28, 0, 0.05], [0.28, 0.96, 0, 0], [0, 0, 1, 0.02], [0, 0, 0, 1]]))
+    wv = wv.astype(np.float32)
+    ref = orc.reference_render("rtao", v, idx, c["proj_inv"], wv, 40, 32, normals=nrm, rays_per_pixel=8, radius=0.25)
+    if ref is None:
+        pytest.skip("reference sources absent")
+    b = orc.OracleBVH(v, idx)
+    o = orc.rtao_frame(b, v, nrm, c["proj_inv"], wv, 40, 32, 0.0, 3.4028234663852886e38, 8, 0.25)
+    hit = o["positions"][:, 1] < orc.AO_HIT_BACK
+    np.testing.assert_array_equal(o["positions"].view(np.uint32), ref["positions"].view(np.uint32))
+    np.testing.assert_array_equal(o["ao_rays"].view(np.uint32), ref["ao_rays"].view(np.uint32))
+    np.testing.assert_array_equal(o["ao_hit"], ref["ao_hit"])
+    np.testing.assert_array_equal(o["visibility"][hit], ref["visibility"][hit])
+    np.testing.assert_array_equal(o["colors"], ref["colors"])
+    e = orc.reference_render("eye", v, idx, c["proj_inv"], wv, 40, 32)
+    np.testing.assert_array_equal(orc.eye_frame(b, c["proj_inv"], wv, 40, 32), e["colors"])
+    np.testing.assert_array_equal(orc.pack_xy(40, 32), e["packed"])
