@@ -10,7 +10,9 @@ value = (eye rays + AO rays) / step time, inputs resident in HBM, on the
 e2e   = the same through the host-pointer C-ABI calls: every step copies the
         step's rays from pinned host memory and the results back;
         e2e_device_raygen = the frame with its rays made on the device.
-Further sections of the same JSON line: "batched" (256 scenes, segmented build
+Further sections of the same JSON line: "frames" (whole frames of the example
+renderers, RTAO and eye rays, generated, traced and shaded on the device),
+"batched" (256 scenes, segmented build
 and graph-captured launches vs per-scene plain), "served" (request stream over
 64 resident scenes: p50/p99 vs one-at-a-time plain), "precision" (heightfield
 + 8.4M-triangle soup in every node layout, hit agreement, FP64 t error).
@@ -71,6 +73,8 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain BVH2 FP32 comparison")
     p.add_argument("--ncu", action="store_true",
                    help="profiling run: setup, warm-up and timed steps only (no extra builds, counters, e2e, CPU)")
+    p.add_argument("--no-frames", action="store_true", help="skip the example renderers' device frames")
+    p.add_argument("--only-frames", action="store_true", help="only the example renderers' device frames")
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched measurement")
     p.add_argument("--only-batched", action="store_true",
                    help="run only the 256-scene batched measurement (prints its JSON object)")
@@ -752,6 +756,77 @@ def run_served(ctx, args) -> dict:
 
 # ---------------------------------------------------------------- GPU engine
 
+def run_frames(ctx, args, w, trace_configs=None) -> dict:
+    """Whole frames of HeavyRT's two example renderers on the device (hrt_frame):
+    RTAO (examples/02_rtao: eye rays, nearest hit, hit shading, 16 AO rays per
+    hit pixel from the renderer's quasi-random tile, any-hit, AO2Color) and the
+    eye-ray renderer (examples/01_eye_rays: packed pixel order, nearest hit,
+    palette), on the heightfield scene, timed frame to frame."""
+    import torch
+
+    from heavyrt_gb300 import Frame, SceneRT, rtao_qmc_tile
+    from heavyrt_gb300 import workload as wl
+
+    W, H, R = args.width, args.height, 16
+    sc = SceneRT(ctx, layout=args.layout)
+    if args.layout != "bvh2":
+        sc.set_bvh4_merge(args.merge)
+    g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+    sc.AddInstance(g)
+    sc.CommitScene()
+    for kind, cfg in (trace_configs or {}).items():
+        sc.set_trace_config(kind, **cfg)
+    f = Frame(ctx)
+    f.set_normals(g, wl.vertex_normals(w.verts, w.idx))
+    f.set_ao_tile(rtao_qmc_tile(R), R)
+    p, v = wl.camera_inverses((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, W, H)
+    radius = float(w.params["ao_length"])
+    colors = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream()
+    frames = max(10, min(100, args.steps // 3))
+
+    def timed(render):
+        for _ in range(3):
+            render()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(frames):
+            render()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / frames
+
+    def rtao():
+        f.render_rtao(sc, p, v, W, H, colors.data_ptr(), 0.0, 3.4028234663852886e38, radius, 1.0,
+                      stream=st.cuda_stream)
+
+    def eye():
+        f.render_eye(sc, p, v, W, H, colors.data_ptr(), stream=st.cuda_stream)
+
+    ms_rtao = timed(rtao)
+    from heavyrt_gb300 import engine as E
+
+    slots = f.buffer(E.FRAME_AO_PIXEL)[1]
+    n_ao = f.buffer(E.FRAME_AO_RAYS)[1]
+    lit = colors.cpu().numpy().view(np.uint32)
+    ms_eye = timed(eye)
+    out = {"workload": f"{W}x{H} frames of the example renderers on heightfield{args.nx}x{args.nx} "
+                       f"({w.idx.size // 3} tris), {args.layout} (merge {args.merge})",
+           "rtao": {"ms_per_frame": round(ms_rtao, 4), "eye_rays": W * H, "hit_pixels": int(slots),
+                    "ao_rays": int(n_ao), "ao_rays_per_hit_pixel": R, "ao_max_radius": round(radius, 5),
+                    "mrays_s": round((W * H + n_ao) / (ms_rtao * 1e3), 2),
+                    "frames_per_s": round(1e3 / ms_rtao, 1),
+                    "mean_gray_of_hit_pixels": round(float((lit[lit != 0] & 0xFF).mean()) if (lit != 0).any() else 0.0, 2),
+                    "device_syncs_per_frame": 1},
+           "eye": {"ms_per_frame": round(ms_eye, 4), "mrays_s": round(W * H / (ms_eye * 1e3), 2),
+                   "frames_per_s": round(1e3 / ms_eye, 1)},
+           "frames_timed": frames}
+    f.close()
+    sc.close()
+    return out
+
+
 def run_engine(args):
     import torch
 
@@ -778,6 +853,11 @@ def run_engine(args):
             print(json.dumps({"precision": run_precision(ctx, args)}), flush=True)
         return 0
     w = make_frame(args)
+    if args.only_frames:
+        if rank == 0:
+            print(json.dumps({"frames": run_frames(ctx, args, w)}), flush=True)
+        return 0
+
     def make_scene(layout):
         sc = SceneRT(ctx, layout=layout)
         if layout != "bvh2":
@@ -1014,6 +1094,8 @@ def run_engine(args):
         line["plain"] = plain
         line["speedup_vs_plain"] = round(line["value"] / plain["mrays_s"], 3)
 
+    if not args.no_frames:
+        line["frames"] = run_frames(ctx, args, w, {k: scene.trace_config(k) for k in (0, 1)})
     if not args.no_batched:
         line["batched"] = run_batched(ctx, args)
         line["gpu_launches_batched_per_step"] = 2
