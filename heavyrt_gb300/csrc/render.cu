@@ -484,6 +484,9 @@ struct hrt_frame
   // small state: total (u64) + error word, device and pinned host
   unsigned long long* dTotal = nullptr;
   unsigned long long* hTotal = nullptr;
+  // colours for a destination in pageable host memory
+  uint32_t* colorBuf = nullptr;
+  uint64_t  colorCap = 0;
   // last frame
   uint64_t lastPixels = 0, lastSlots = 0;
   uint32_t lastRaysPerPixel = 0;
@@ -519,6 +522,38 @@ int ensure_pixels(hrt_frame* f, uint64_t n)
     if ((st = grow(ctx, (void**)&f->blockCount, 4 * blocks))) return st;
     f->blockCap = blocks;
   }
+  return HRT_OK;
+}
+
+// Where the kernels write a frame's colours: device-accessible memory
+// (device, managed, pinned host) directly; pageable host memory through the
+// frame's own buffer and one copy at the end of the frame.
+int color_target(hrt_frame* f, uint32_t* colors, uint64_t n, uint32_t** target)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, colors) == cudaSuccess &&
+      (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost))
+  {
+    *target = colors;
+    return HRT_OK;
+  }
+  cudaGetLastError();  // an unregistered pointer may leave an error behind
+  if (n > f->colorCap)
+  {
+    f->colorCap = 0;
+    const int st = grow(f->ctx, (void**)&f->colorBuf, 4 * n);
+    if (st) return st;
+    f->colorCap = n;
+  }
+  *target = f->colorBuf;
+  return HRT_OK;
+}
+
+int finish_colors(hrt_frame* f, uint32_t* colors, const uint32_t* target, uint64_t n, cudaStream_t cs)
+{
+  if (target == colors) return HRT_OK;
+  HRT_CUDA(f->ctx, cudaMemcpyAsync(colors, target, 4 * n, cudaMemcpyDeviceToHost, cs));
+  HRT_CUDA(f->ctx, cudaStreamSynchronize(cs));
   return HRT_OK;
 }
 
@@ -595,7 +630,7 @@ int hrt_frame_destroy(hrt_frame* f)
   if (!f) return HRT_ERR_INVALID_ARGUMENT;
   cudaSetDevice(f->ctx->device);
   void* dev[] = {f->rays, f->pixel, f->hits, f->positions, f->flag, f->visibility, f->blockCount, f->aoRays,
-                 f->aoPixel, f->aoHit, f->dev, f->dGeoms, f->dNormMat, f->dTotal};
+                 f->aoPixel, f->aoHit, f->dev, f->dGeoms, f->dNormMat, f->dTotal, f->colorBuf};
   for (void* p : dev)
     if (p) cudaFree(p);
   for (float4* p : f->normals)
@@ -677,12 +712,14 @@ int hrt_frame_render_eye(hrt_frame* f, hrt_scene* s, const float projInv[16], co
                                                                   f->pixel);
   HRT_CUDA(ctx, cudaGetLastError());
   if ((st = hrt_query_nearest(s, reinterpret_cast<const float*>(f->rays), n, f->hits, stream))) return st;
-  k_eye_colors<<<grid_for(n, ctx->numSMs), kThreads, 0, cs>>>(f->hits, f->pixel, n, colors);
+  uint32_t* out = nullptr;
+  if ((st = color_target(f, colors, n, &out))) return st;
+  k_eye_colors<<<grid_for(n, ctx->numSMs), kThreads, 0, cs>>>(f->hits, f->pixel, n, out);
   HRT_CUDA(ctx, cudaGetLastError());
   f->lastPixels = n;
   f->lastSlots = 0;
   f->lastRaysPerPixel = 0;
-  return HRT_OK;
+  return finish_colors(f, colors, out, n, cs);
 }
 
 int hrt_frame_render_rtao(hrt_frame* f, hrt_scene* s, const hrt_rtao_params* prm, const float* normMatrices,
@@ -760,7 +797,9 @@ int hrt_frame_render_rtao(hrt_frame* f, hrt_scene* s, const hrt_rtao_params* prm
     if ((st = grow(ctx, (void**)&f->aoRays, 32 * nAo)) || (st = grow(ctx, (void**)&f->aoHit, nAo))) return st;
     f->aoCap = nAo;
   }
-  HRT_CUDA(ctx, cudaMemsetAsync(colors, 0, 4 * n, cs));
+  uint32_t* out = nullptr;
+  if ((st = color_target(f, colors, n, &out))) return st;
+  HRT_CUDA(ctx, cudaMemsetAsync(out, 0, 4 * n, cs));
   HRT_CUDA(ctx, cudaMemsetAsync(f->visibility, 0, 4 * n, cs));
   if (slots > 0)
   {
@@ -769,13 +808,13 @@ int hrt_frame_render_rtao(hrt_frame* f, hrt_scene* s, const hrt_rtao_params* prm
     HRT_CUDA(ctx, cudaGetLastError());
     if ((st = hrt_query_any(s, reinterpret_cast<const float*>(f->aoRays), nAo, f->aoHit, stream))) return st;
     k_rtao_colors<<<grid_for(slots, ctx->numSMs), kThreads, 0, cs>>>(f->aoHit, f->aoPixel, slots, R, prm->power,
-                                                                     f->visibility, colors);
+                                                                     f->visibility, out);
     HRT_CUDA(ctx, cudaGetLastError());
   }
   f->lastPixels = n;
   f->lastSlots = slots;
   f->lastRaysPerPixel = R;
-  return HRT_OK;
+  return finish_colors(f, colors, out, n, cs);
 }
 
 int hrt_frame_get_buffer(const hrt_frame* f, int which, const void** data, uint64_t* count)

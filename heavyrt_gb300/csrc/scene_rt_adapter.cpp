@@ -171,6 +171,9 @@ public:
     return m_boxes.empty() ? nullptr : m_boxes.data();
   }
 
+  hrt_scene*   Scene() const { return m_scene; }
+  hrt_context* Context() const { return m_ctx; }
+
   // Batched queries for callers that hold whole ray arrays (one GPU call).
   void RayQuery_NearestHitBatch(const LiteMath::float4* posAndNear, const LiteMath::float4* dirAndFar, size_t n,
                                 CRT_Hit* out)
@@ -329,6 +332,11 @@ ISceneObject* MakeGpuLBVHRT(const char* a_implName, const char* a_buildName, con
 {
   return new GpuLBVHRT(a_implName, a_buildName, a_layoutName);
 }
+
+// The engine objects behind a scene made by MakeGpuLBVHRT, for the C-ABI calls
+// that go beyond ISceneObject (e.g. the renderer frames, hrt_frame_render_rtao).
+hrt_scene* GpuLBVHRT_Scene(ISceneObject* scene) { return static_cast<GpuLBVHRT*>(scene)->Scene(); }
+hrt_context* GpuLBVHRT_Context(ISceneObject* scene) { return static_cast<GpuLBVHRT*>(scene)->Context(); }
 
 // Batched form for callers that can pass ray arrays; `scene` must come from MakeGpuLBVHRT.
 void GpuLBVHRT_NearestHitBatch(ISceneObject* scene, const LiteMath::float4* posAndNear,

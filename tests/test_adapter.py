@@ -73,3 +73,31 @@ def test_adapter_per_ray_threads_match_oracle(native, tmp_path, layout):
     o = orc.OracleBVH(v, idx)
     np.testing.assert_array_equal(hits, o.trace(rays).view(np.uint32).reshape(-1, 8))
     np.testing.assert_array_equal(anyh, o.trace(rays, any_hit=True))
+
+
+@pytest.mark.gpu
+def test_adapter_scene_renders_frames_into_host_memory(native, tmp_path):
+    """A renderer holding the adapter's ISceneObject reaches the engine scene
+    (GpuLBVHRT_Scene) and renders RTAO and eye-ray frames into its own host
+    image arrays; the images equal the restatement's."""
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    exe = build_harness()
+    v, idx, _ = wl.heightfield(5, 90, 70)
+    nrm = wl.vertex_normals(v, idx)
+    W, H = 72, 40
+    p, wv = wl.camera_inverses((0.0, -2.0, 1.2), (0, 0, 0), (0, 0, 1), 60.0, W, H)
+    wl.scene_file(tmp_path / "s.bin", v, idx)
+    wl.ray_file(tmp_path / "r.bin", wl.sphere_rays(6, 16))
+    with open(tmp_path / "n.bin", "wb") as f:
+        f.write(b"HRTNRM01" + np.array([len(nrm)], np.uint64).tobytes() + nrm.tobytes())
+    (tmp_path / "p.bin").write_bytes(orc._render_params(p, wv, W, H, 0.0, 3.4028234663852886e38, 4, 0.3, 1.0, None))
+    r = subprocess.run([str(exe), str(tmp_path / "s.bin"), str(tmp_path / "r.bin"), str(tmp_path / "out"), "2", "",
+                        str(tmp_path / "n.bin"), str(tmp_path / "p.bin")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    b = orc.OracleBVH(v, idx)
+    want = orc.rtao_frame(b, v, nrm, p, wv, W, H, 0.0, 3.4028234663852886e38, 4, 0.3)
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "out.rtao", np.uint32), want["colors"])
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "out.eye", np.uint32), orc.eye_frame(b, p, wv, W, H))
+    assert (want["colors"] != 0).any()
