@@ -869,6 +869,8 @@ int hrt_scene_destroy(hrt_scene* s)
   if (s->dRayCounters) cudaFree(s->dRayCounters);
   if (s->stageRays) cudaFree(s->stageRays);
   if (s->stageOut) cudaFree(s->stageOut);
+  for (cudaStream_t p : s->pipe)
+    if (p) cudaStreamDestroy(p);
   delete s;
   return HRT_OK;
 }
@@ -1088,6 +1090,19 @@ int hrt_query_any(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out, voi
   return launch_query(s, 1, rays, n, out, 0, (cudaStream_t)stream);
 }
 
+// The device address of page-locked (or otherwise device-accessible) host
+// memory, or null for ordinary pageable memory.
+static void* mapped_host(const void* p)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out)
 {
   if (!s) return HRT_ERR_INVALID_ARGUMENT;
@@ -1096,14 +1111,58 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
   std::lock_guard<std::mutex> g(s->mu);
   hrt_context* ctx = s->ctx;
   cudaSetDevice(ctx->device);
-  int st = ensure_stage(s, n);
-  if (st != HRT_OK) return st;
   cudaStream_t cs = ctx->stream;
-  HRT_CUDA(ctx, cudaMemcpyAsync(s->stageRays, rays, 32 * n, cudaMemcpyHostToDevice, cs));
-  st = launch_query(s, kind, (const float*)s->stageRays, n, s->stageOut, 0, cs);
-  if (st != HRT_OK) return st;
-  const size_t outBytes = kind == 0 ? sizeof(hrt_hit) * n : n;
-  HRT_CUDA(ctx, cudaMemcpyAsync(out, s->stageOut, outBytes, cudaMemcpyDeviceToHost, cs));
+  int st = HRT_OK;
+  // Page-locked host arrays are mapped into the GPU's address space: the
+  // traversal reads such rays in place over the host link, and writes any-hit
+  // flags (1 byte per ray) in place too.  Nearest hits (32 bytes per ray) go
+  // to the device and come back by copy.  Other host memory is copied in.
+  const float* mappedRays = static_cast<const float*>(mapped_host(rays));
+  void* mappedOut = kind == 1 ? mapped_host(out) : nullptr;
+  const bool inPlace = mappedRays && mappedOut;
+  if (inPlace)
+  {
+    st = launch_query(s, kind, mappedRays, n, mappedOut, 0, cs);
+    if (st != HRT_OK) return st;
+  }
+  else if ((st = ensure_stage(s, n)) != HRT_OK)
+    return st;
+  // Otherwise large batches are cut into chunks that cycle over the scene's
+  // pipeline streams, so that one chunk's upload, another's traversal and a
+  // third's download overlap (the copy engines and the SMs work at once).
+  // Each chunk has its own part of the staging buffers; results do not depend
+  // on the cut.
+  constexpr uint64_t kMinChunk = 1u << 17, kChunks = 8;
+  const uint64_t chunk = n < 2 * kMinChunk ? n : std::max<uint64_t>(kMinChunk, (n + kChunks - 1) / kChunks);
+  const size_t outSize = kind == 0 ? sizeof(hrt_hit) : 1;
+  const int nPipe = (chunk == n || inPlace) ? 1 : 3;
+  if (nPipe > 1)
+    for (cudaStream_t& p : s->pipe)
+      if (!p) HRT_CUDA(ctx, cudaStreamCreateWithFlags(&p, cudaStreamNonBlocking));
+  for (uint64_t c0 = 0, k = 0; c0 < n && !inPlace; c0 += chunk, k++)
+  {
+    const uint64_t len = std::min(chunk, n - c0);
+    cudaStream_t ps = nPipe > 1 ? s->pipe[k % nPipe] : cs;
+    const float* src = rays + 8 * c0;
+    float* dRays = static_cast<float*>(s->stageRays) + 8 * c0;
+    uint8_t* dOut = static_cast<uint8_t*>(s->stageOut) + outSize * c0;
+    if (mappedRays)
+      st = launch_query(s, kind, mappedRays + 8 * c0, len, dOut, 0, ps);
+    else
+    {
+      HRT_CUDA(ctx, cudaMemcpyAsync(dRays, src, 32 * len, cudaMemcpyHostToDevice, ps));
+      st = launch_query(s, kind, dRays, len, dOut, 0, ps);
+    }
+    if (st != HRT_OK)
+    {
+      for (int p = 0; p < nPipe && nPipe > 1; p++) cudaStreamSynchronize(s->pipe[p]);
+      return st;
+    }
+    HRT_CUDA(ctx, cudaMemcpyAsync(static_cast<uint8_t*>(out) + outSize * c0, dOut, outSize * len,
+                                  cudaMemcpyDeviceToHost, ps));
+  }
+  if (nPipe > 1)
+    for (int p = 0; p < nPipe; p++) HRT_CUDA(ctx, cudaStreamSynchronize(s->pipe[p]));
   uint32_t ew[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   HRT_CUDA(ctx, cudaMemcpyAsync(ew, s->dError, sizeof(ew), cudaMemcpyDeviceToHost, cs));
   HRT_CUDA(ctx, cudaStreamSynchronize(cs));

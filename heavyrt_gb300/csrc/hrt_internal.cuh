@@ -87,10 +87,11 @@ struct hrt_scene
   unsigned int*         dRayCounters = nullptr;
   std::atomic<uint32_t> counterSlot{0};
   TraceConfig           cfg[2];  // [0] nearest, [1] any
-  // staging for the host-pointer queries
+  // staging for the host-pointer queries, and the streams that pipeline them
   void*                 stageRays = nullptr;
   void*                 stageOut = nullptr;
   uint64_t              stageCap = 0;
+  cudaStream_t          pipe[3] = {nullptr, nullptr, nullptr};
   std::mutex            mu;
 };
 

@@ -183,8 +183,12 @@ int hrt_query_nearest(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* 
  * triangle passes the ray-triangle test with tNear < t < tFar.  out: n bytes. */
 int hrt_query_any(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out, void* stream);
 
-/* Same as the two calls above with HOST arrays: the engine copies the rays to
- * the device, traces and copies the results back before returning. */
+/* Same as the two calls above with HOST arrays; the results are in place when
+ * the call returns.  Page-locked arrays (hrt_host_alloc, cudaHostAlloc,
+ * cudaHostRegister) are used where they are: the traversal reads their rays
+ * over the host link and writes any-hit flags straight into them; nearest hits
+ * come back by copy.  Other host memory is copied in.  Batches above 2^18 rays
+ * run as chunks whose copies overlap the traversal of other chunks. */
 int hrt_query_nearest_host(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits);
 int hrt_query_any_host(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out);
 

@@ -180,6 +180,51 @@ def test_device_queries_match_host_queries(native):
     assert HIT_DTYPE.itemsize == 32
 
 
+def test_large_host_queries_are_pipelined_exactly(native):
+    """Host-pointer queries of more than 2^18 rays run as overlapped chunks on
+    three streams, and page-locked arrays are read (and any-hit flags written)
+    in place; the results equal one device query of the whole batch, for an
+    uneven last chunk, from pageable and from page-locked host memory."""
+    import torch
+
+    from heavyrt_gb300 import PinnedBuffer
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(3, 200, 200)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 700, 500),
+                           wl.rays_at_triangles(4, v, idx, 300001, jitter=0.02)])
+    n = rays.shape[0]
+    s, _ = _scene(v, idx)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+    da = torch.empty(n, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    s.query_device(0, dr.data_ptr(), n, dh.data_ptr(), stream)
+    s.query_device(1, dr.data_ptr(), n, da.data_ptr(), stream)
+    torch.cuda.synchronize()
+    want_h, want_a = dh.cpu().numpy().view(np.uint32), da.cpu().numpy().astype(bool)
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32).reshape(-1, 8), want_h)
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), want_a)
+    # page-locked rays (read in place) and flags (written in place)
+    from heavyrt_gb300 import engine as E
+
+    pin = PinnedBuffer(rays.nbytes)
+    pin_out = PinnedBuffer(n)
+    pin.array(np.float32, rays.size)[:] = rays.reshape(-1)
+    pinned_rays = pin.array(np.float32, rays.size).reshape(-1, 8)
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(pinned_rays).view(np.uint32).reshape(-1, 8), want_h)
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(pinned_rays), want_a)
+    import ctypes
+
+    s.ctx.check(E.lib().hrt_query_any_host(s._h, ctypes.c_void_p(pin.ptr), n, ctypes.c_void_p(pin_out.ptr)), "any")
+    np.testing.assert_array_equal(pin_out.array(np.uint8, n).astype(bool), want_a)
+    small = pinned_rays[:1000]
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(small).view(np.uint32).reshape(-1, 8), want_h[:1000])
+    pin.free()
+    pin_out.free()
+    assert 0.2 < want_a.mean() < 1.0
+
+
 def test_instances_exact_transforms(native):
     """Several instances of one geometry; transforms exact in binary32 so the
     expected result is computed by tracing the oracle with transformed rays."""
