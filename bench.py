@@ -982,15 +982,22 @@ def run_engine(args):
     g_ao = torch.empty((cap, 8), dtype=torch.float32, device="cuda")
     g_any = torch.empty(cap, dtype=torch.uint8, device="cuda")
 
+    copy_stream = torch.cuda.Stream()
+    eye_done = torch.cuda.Event()
+
     def raygen_step():
+        # the eye hits go home on a second stream while the AO rays are made
+        # and traced; the AO flags are written straight into page-locked host memory
         ctx.gen_pinhole_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, args.width, args.height, 0.0, 1e9,
                              g_eye.data_ptr(), sh)
         scene.query_device(0, g_eye.data_ptr(), n_eye, g_hits.data_ptr(), sh)
+        eye_done.record(stream)
+        copy_stream.wait_event(eye_done)
+        with torch.cuda.stream(copy_stream):
+            pin_hits_d.copy_(g_hits, non_blocking=True)
         k = scene.gen_ao_rays(pp["ao_seed"], g_eye.data_ptr(), g_hits.data_ptr(), n_eye, pp["ao_per_hit"],
                               pp["ao_length"], pp["ao_offset"], g_ao.data_ptr(), cap, 0, sh)
-        scene.query_device(1, g_ao.data_ptr(), k, g_any.data_ptr(), sh)
-        pin_hits_d.copy_(g_hits, non_blocking=True)
-        pin_any_d[:k].copy_(g_any[:k], non_blocking=True)
+        scene.query_device(1, g_ao.data_ptr(), k, pin_any_d.data_ptr(), sh)
         torch.cuda.synchronize()
         return k
 
