@@ -707,6 +707,17 @@ bool lbvh_builder_name(const char* name)
   return s.find("lbvh") != std::string::npos;  // "cbvh_lbvh", "lbvh", "cbvh_lbvh_gpu" (core/builders/cbvh.cpp:45-55)
 }
 
+void* mapped_host(const void* p)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int ensure_stage(hrt_scene* s, uint64_t n)
 {
   if (n <= s->stageCap) return HRT_OK;
@@ -1088,19 +1099,6 @@ int hrt_query_any(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out, voi
 {
   if (!s) return HRT_ERR_INVALID_ARGUMENT;
   return launch_query(s, 1, rays, n, out, 0, (cudaStream_t)stream);
-}
-
-// The device address of page-locked (or otherwise device-accessible) host
-// memory, or null for ordinary pageable memory.
-static void* mapped_host(const void* p)
-{
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
-  {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out)

@@ -117,6 +117,9 @@ void make_instance_desc(const Geom& g, uint32_t geomId, uint32_t instId, const f
 // Column-major 4x4 -> rows 0..2 of its inverse (the reference checker's evaluation).
 void inverse4x4(const float* mc, float* inv12);
 bool is_identity(const float* m);
+// The device address of page-locked host memory (mapped into the GPU's
+// address space), or null for pageable memory.
+void* mapped_host(const void* p);
 
 }  // namespace api
 }  // namespace hrt

@@ -172,6 +172,12 @@ void CUDART_CB on_slot_done(void* p)
 cudaError_t issue(hrt_server* S, Slot* sl)
 {
   const uint32_t maxReq = S->cfg.maxBatchRequests;
+  // A batch of one request whose rays are page-locked reads them in place over
+  // the host link (no copy in); its any-hit flags are written in place too
+  // when the output is page-locked.
+  const Request* only = sl->reqs.size() == 1 ? sl->reqs[0] : nullptr;
+  const float4* inPlaceRays = only ? static_cast<const float4*>(mapped_host(only->rays)) : nullptr;
+  void* inPlaceOut = only && only->kind == 1 ? mapped_host(only->out) : nullptr;
   uint32_t* hOff[2] = {sl->hIdx, sl->hIdx + (2 * maxReq + 1)};
   uint32_t* dOff[2] = {sl->dIdx, sl->dIdx + (2 * maxReq + 1)};
   uint32_t cnt[2] = {0, 0};
@@ -184,8 +190,11 @@ cudaError_t issue(hrt_server* S, Slot* sl)
   {
     const int k = r->kind;
     const uint64_t base = (k == 0 ? 0 : total[0]) + hOff[k][cnt[k]];
-    e = cudaMemcpyAsync(sl->rays + 2 * base, r->rays, 32 * r->n, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
+    if (!inPlaceRays)
+    {
+      e = cudaMemcpyAsync(sl->rays + 2 * base, r->rays, 32 * r->n, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return e;
+    }
     hOff[k][maxReq + 1 + cnt[k]] = r->scene;  // segment -> scene table slot
     hOff[k][cnt[k] + 1] = hOff[k][cnt[k]] + (uint32_t)r->n;
     cnt[k]++;
@@ -198,11 +207,11 @@ cudaError_t issue(hrt_server* S, Slot* sl)
   {
     if (!cnt[k]) continue;
     TraceArgs a;
-    a.rays = sl->rays + 2 * (k == 0 ? 0 : total[0]);
+    a.rays = inPlaceRays ? inPlaceRays : sl->rays + 2 * (k == 0 ? 0 : total[0]);
     a.n = total[k];
     a.inst = S->dTable;
     a.nInst = S->cfg.maxScenes;
-    a.hits = k == 0 ? static_cast<void*>(sl->hits) : static_cast<void*>(sl->any);
+    a.hits = k == 0 ? static_cast<void*>(sl->hits) : (inPlaceOut ? inPlaceOut : static_cast<void*>(sl->any));
     a.counters = nullptr;
     a.errorWord = sl->dErr;
     a.rayCounter = sl->counters + k;
@@ -217,7 +226,7 @@ cudaError_t issue(hrt_server* S, Slot* sl)
   {
     const int k = r->kind;
     if (k == 0) e = cudaMemcpyAsync(r->out, sl->hits + pos[0], sizeof(hrt_hit) * r->n, cudaMemcpyDeviceToHost, st);
-    else e = cudaMemcpyAsync(r->out, sl->any + pos[1], r->n, cudaMemcpyDeviceToHost, st);
+    else if (!inPlaceOut) e = cudaMemcpyAsync(r->out, sl->any + pos[1], r->n, cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return e;
     pos[k] += (uint32_t)r->n;
   }
@@ -467,9 +476,15 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
     delete S;
     return cuda_fail(ctx, e, what);
   };
-  cudaError_t e = cudaStreamCreateWithFlags(&S->bctx.stream, cudaStreamNonBlocking);
+  // ray batches run at the highest stream priority, builds and uploads at the
+  // lowest: the block scheduler then serves a batch's blocks first whenever
+  // both wait for SMs, so builds on arrival delay queries as little as possible
+  int leastPriority = 0, greatestPriority = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&leastPriority, &greatestPriority);
+  if (e != cudaSuccess) return bail(e, "stream priorities");
+  e = cudaStreamCreateWithPriority(&S->bctx.stream, cudaStreamNonBlocking, leastPriority);
   if (e != cudaSuccess) return bail(e, "builder stream");
-  e = cudaStreamCreateWithFlags(&S->stageStream, cudaStreamNonBlocking);
+  e = cudaStreamCreateWithPriority(&S->stageStream, cudaStreamNonBlocking, leastPriority);
   if (e != cudaSuccess) return bail(e, "staging stream");
   e = cudaMalloc((void**)&S->dTable, sizeof(InstanceDesc) * c.maxScenes);
   if (e != cudaSuccess) return bail(e, "scene table");
@@ -481,7 +496,7 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
     S->slots.push_back(sl);
     sl->server = S;
     const size_t idxWords = 2 * (2 * (size_t)c.maxBatchRequests + 1);
-    if ((e = cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+    if ((e = cudaStreamCreateWithPriority(&sl->stream, cudaStreamNonBlocking, greatestPriority)) != cudaSuccess ||
         (e = cudaMalloc((void**)&sl->rays, 32 * c.slotRays)) != cudaSuccess ||
         (e = cudaMalloc((void**)&sl->hits, sizeof(hrt_hit) * c.slotRays)) != cudaSuccess ||
         (e = cudaMalloc((void**)&sl->any, c.slotRays)) != cudaSuccess ||
