@@ -343,7 +343,11 @@ int hrt_server_scene_state(hrt_server* server, uint32_t sceneId, double timeoutS
 /* Frees a ready scene with no requests queued or in flight (HRT_ERR_STATE otherwise). */
 int hrt_server_remove_scene(hrt_server* server, uint32_t sceneId);
 /* Queues a request: n rays (host, 8 floats each) against one scene; kind 0
- * writes hrt_hit[n] to out, kind 1 uint8_t[n]. */
+ * writes hrt_hit[n] to out, kind 1 uint8_t[n].  Both arrays must stay valid
+ * until the request is waited for.  A request batched alone whose rays are
+ * page-locked is traced from them in place (its any-hit flags written in
+ * place when out is page-locked); otherwise the rays are copied in.  Ray
+ * batches run at the highest stream priority, scene builds at the lowest. */
 int hrt_server_submit(hrt_server* server, uint32_t sceneId, int kind, const float* rays, uint64_t n, void* out,
                       uint64_t* ticket);
 /* Waits for a request (timeoutSeconds < 0: no limit; HRT_ERR_TIMEOUT leaves the
