@@ -245,16 +245,12 @@ __global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* blockCount, uint
   if (threadIdx.x == 0) *total = s_carry;
 }
 
-// kernel_InitAORay (examples/02_rtao/rtao.cpp:147-165) for every flagged
-// traced ray: slot = its rank among the flagged rays, raysPerPixel rays at
-// slot * raysPerPixel.  dev: the tile's sample directions in the normal's
-// frame (sinT cosP, sinT sinP, cosT), one float4 per tile entry.
+// Pixel of every AO slot: the flagged traced rays, ranked in trace order
+// (block offsets from k_scan_counts, ranks inside a block by warp ballots).
 __global__ void __launch_bounds__(kThreads)
-    k_rtao_ao_rays(const uint8_t* __restrict__ flag, uint64_t n, const uint32_t* __restrict__ blockOffset,
-                   const uint32_t* __restrict__ pixel, const float4* __restrict__ positions, uint32_t width,
-                   const float4* __restrict__ dev, uint32_t raysPerPixel, float aoMaxRadius,
-                   float4* __restrict__ aoRays, uint32_t* __restrict__ aoPixel, uint64_t slotCapacity,
-                   uint32_t* errorWord)
+    k_rtao_slots(const uint8_t* __restrict__ flag, uint64_t n, const uint32_t* __restrict__ blockOffset,
+                 const uint32_t* __restrict__ pixel, uint32_t* __restrict__ aoPixel, uint64_t slotCapacity,
+                 uint32_t* errorWord)
 {
   __shared__ uint32_t s_warp[kThreads / 32 + 1];
   const uint64_t base = (uint64_t)blockIdx.x * kThreads * kChunk;
@@ -288,10 +284,26 @@ __global__ void __launch_bounds__(kThreads)
       atomicOr(errorWord, kErrLayout);
       continue;
     }
-    const uint32_t pix = pixel[k];
+    aoPixel[slot] = pixel[k];
+  }
+}
+
+// The per-pixel part of kernel_InitAORay (examples/02_rtao/rtao.cpp:147-165),
+// once per slot: the packed normal decoded (decodeNormal,
+// examples/render_common.h:126-137), CoordinateSystem's frame about it
+// (:38-54, the second branch's division in double as the renderer's
+// unqualified sqrt makes it), the offset size epsilonOfPos (:96-98) and the
+// pixel's row of the sample tile.  Record: {pos, eps}, {normal, invSign},
+// {nx, tile row}, {ny, 0}.
+__global__ void __launch_bounds__(kThreads)
+    k_rtao_frames(const uint32_t* __restrict__ aoPixel, uint64_t slots, const float4* __restrict__ positions,
+                  uint32_t width, uint32_t raysPerPixel, float4* __restrict__ frames)
+{
+  for (uint64_t s = (uint64_t)blockIdx.x * kThreads + threadIdx.x; s < slots; s += (uint64_t)gridDim.x * kThreads)
+  {
+    const uint32_t pix = aoPixel[s];
     const uint32_t x = pix % width, y = pix / width;
     const float4 pos = positions[pix];
-    // decodeNormal (examples/render_common.h:126-137)
     const uint32_t a = __float_as_uint(pos.w);
     const uint32_t ex = a & 0x0000FFFFu, ey = (a & 0xFFFF0000u) >> 16;
     const float sign = (ex & 1u) != 0 ? -1.0f : 1.0f;
@@ -301,7 +313,6 @@ __global__ void __launch_bounds__(kThreads)
     nrm[1] = __fmul_rn((float)(int16_t)(uint16_t)(ey & 0xffffu), kInv);
     const float zz = __fsub_rn(__fsub_rn(1.0f, __fmul_rn(nrm[0], nrm[0])), __fmul_rn(nrm[1], nrm[1]));
     nrm[2] = __fmul_rn(sign, __fsqrt_rn(zz < 0.0f ? 0.0f : zz));
-    // CoordinateSystem (render_common.h:38-54): nx, then ny = cross(normal, nx); nz = the normal
     float nx[3];
     if (fabsf(nrm[0]) > fabsf(nrm[1]))
     {
@@ -322,34 +333,53 @@ __global__ void __launch_bounds__(kThreads)
                          __fsub_rn(__fmul_rn(nrm[2], nx[0]), __fmul_rn(nrm[0], nx[2])),
                          __fsub_rn(__fmul_rn(nrm[0], nx[1]), __fmul_rn(nrm[1], nx[0]))};
     const float invSign = hrt::rg::dot3(nrm, nrm) > 0.0f ? 1.0f : -1.0f;
-    // epsilonOfPos / OffsRayPos (render_common.h:96-112), std::max(a, b) = a < b ? b : a
+    // std::max(a, b) = a < b ? b : a
     const float ax = fabsf(pos.x), ay = fabsf(pos.y), az = fabsf(pos.z);
     const float myz = ay < az ? az : ay;
     const float mxyz = ax < myz ? myz : ax;
     const float gEps = 2e-5f, twoGEps = __fmul_rn(2.0f, gEps);
     const float eps = __fmul_rn(mxyz < twoGEps ? twoGEps : mxyz, gEps);
-    const float4* devRow = dev + ((size_t)(y % kAoTile) * kAoTile + (x % kAoTile)) * raysPerPixel;
-    float4* out = aoRays + 2 * slot * raysPerPixel;
-    for (uint32_t z = 0; z < raysPerPixel; z++)
+    const uint32_t tileRow = ((y % kAoTile) * kAoTile + (x % kAoTile)) * raysPerPixel;
+    float4* o = frames + 4 * s;
+    o[0] = make_float4(pos.x, pos.y, pos.z, eps);
+    o[1] = make_float4(nrm[0], nrm[1], nrm[2], invSign);
+    o[2] = make_float4(nx[0], nx[1], nx[2], __uint_as_float(tileRow));
+    o[3] = make_float4(ny[0], ny[1], ny[2], 0.0f);
+  }
+}
+
+// The per-ray part of kernel_InitAORay: one thread per AO ray (slot s, sample
+// z at s * raysPerPixel + z), MapSampleToCosineDistribution with the tile
+// entry's sample direction (dev: (sinT cosP, sinT sinP, cosT) per entry) and
+// OffsRayPos (examples/render_common.h:56-112).  Consecutive threads write
+// consecutive rays.
+__global__ void __launch_bounds__(kThreads)
+    k_rtao_ao_rays(const float4* __restrict__ frames, uint64_t nRays, uint32_t raysPerPixel,
+                   const float4* __restrict__ dev, float aoMaxRadius, float4* __restrict__ aoRays)
+{
+  for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < nRays; i += (uint64_t)gridDim.x * kThreads)
+  {
+    const uint64_t s = i / raysPerPixel;
+    const uint32_t z = (uint32_t)(i - s * raysPerPixel);
+    const float4* fr = frames + 4 * s;
+    const float4 P = fr[0], N = fr[1], X = fr[2], Y = fr[3];
+    const float nrm[3] = {N.x, N.y, N.z}, nx[3] = {X.x, X.y, X.z}, ny[3] = {Y.x, Y.y, Y.z};
+    const float4 dv = dev[__float_as_uint(X.w) + z];
+    float res[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      res[c] = __fadd_rn(__fadd_rn(__fmul_rn(nx[c], dv.x), __fmul_rn(ny[c], dv.y)), __fmul_rn(nrm[c], dv.z));
+    if (__fmul_rn(N.w, hrt::rg::dot3(res, nrm)) < 0.0f)
     {
-      const float4 dv = devRow[z];
-      float res[3];
 #pragma unroll
       for (int c = 0; c < 3; c++)
-        res[c] = __fadd_rn(__fadd_rn(__fmul_rn(nx[c], dv.x), __fmul_rn(ny[c], dv.y)), __fmul_rn(nrm[c], dv.z));
-      if (__fmul_rn(invSign, hrt::rg::dot3(res, nrm)) < 0.0f)
-      {
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-          res[c] = __fsub_rn(__fadd_rn(__fmul_rn(__fmul_rn(-1.0f, nx[c]), dv.x), __fmul_rn(ny[c], dv.y)),
-                             __fmul_rn(nrm[c], dv.z));
-      }
-      const float se = __fmul_rn(hrt::rg::dot3(res, nrm) < 0.0f ? -1.0f : 1.0f, eps);
-      out[2 * z + 0] = make_float4(__fadd_rn(pos.x, __fmul_rn(se, nrm[0])), __fadd_rn(pos.y, __fmul_rn(se, nrm[1])),
-                                   __fadd_rn(pos.z, __fmul_rn(se, nrm[2])), 0.0f);
-      out[2 * z + 1] = make_float4(res[0], res[1], res[2], aoMaxRadius);
+        res[c] = __fsub_rn(__fadd_rn(__fmul_rn(__fmul_rn(-1.0f, nx[c]), dv.x), __fmul_rn(ny[c], dv.y)),
+                           __fmul_rn(nrm[c], dv.z));
     }
-    aoPixel[slot] = pix;
+    const float se = __fmul_rn(hrt::rg::dot3(res, nrm) < 0.0f ? -1.0f : 1.0f, P.w);
+    aoRays[2 * i + 0] = make_float4(__fadd_rn(P.x, __fmul_rn(se, nrm[0])), __fadd_rn(P.y, __fmul_rn(se, nrm[1])),
+                                    __fadd_rn(P.z, __fmul_rn(se, nrm[2])), 0.0f);
+    aoRays[2 * i + 1] = make_float4(res[0], res[1], res[2], aoMaxRadius);
   }
 }
 
@@ -469,6 +499,7 @@ struct hrt_frame
   // AO pass
   float4*   aoRays = nullptr;
   uint32_t* aoPixel = nullptr;
+  float4*   frames = nullptr;  // per slot: the pixel's AO frame (k_rtao_frames)
   uint8_t*  aoHit = nullptr;
   uint64_t  slotCap = 0, aoCap = 0;
   // sample tile: sample directions per entry
@@ -630,7 +661,7 @@ int hrt_frame_destroy(hrt_frame* f)
   if (!f) return HRT_ERR_INVALID_ARGUMENT;
   cudaSetDevice(f->ctx->device);
   void* dev[] = {f->rays, f->pixel, f->hits, f->positions, f->flag, f->visibility, f->blockCount, f->aoRays,
-                 f->aoPixel, f->aoHit, f->dev, f->dGeoms, f->dNormMat, f->dTotal, f->colorBuf};
+                 f->aoPixel, f->aoHit, f->dev, f->dGeoms, f->dNormMat, f->dTotal, f->colorBuf, f->frames};
   for (void* p : dev)
     if (p) cudaFree(p);
   for (float4* p : f->normals)
@@ -788,7 +819,9 @@ int hrt_frame_render_rtao(hrt_frame* f, hrt_scene* s, const hrt_rtao_params* prm
   if (nAo > 0xFFFFFFFFull) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^32-1 AO rays in one frame");
   if (slots > f->slotCap)
   {
-    if ((st = grow(ctx, (void**)&f->aoPixel, 4 * slots))) return st;
+    f->slotCap = 0;
+    if ((st = grow(ctx, (void**)&f->aoPixel, 4 * slots)) || (st = grow(ctx, (void**)&f->frames, 64 * slots)))
+      return st;
     f->slotCap = slots;
   }
   if (nAo > f->aoCap)
@@ -803,8 +836,11 @@ int hrt_frame_render_rtao(hrt_frame* f, hrt_scene* s, const hrt_rtao_params* prm
   HRT_CUDA(ctx, cudaMemsetAsync(f->visibility, 0, 4 * n, cs));
   if (slots > 0)
   {
-    k_rtao_ao_rays<<<nBlocks, kThreads, 0, cs>>>(f->flag, n, f->blockCount, f->pixel, f->positions, prm->width, f->dev,
-                                                 R, prm->aoMaxRadius, f->aoRays, f->aoPixel, f->slotCap, dErr);
+    k_rtao_slots<<<nBlocks, kThreads, 0, cs>>>(f->flag, n, f->blockCount, f->pixel, f->aoPixel, f->slotCap, dErr);
+    k_rtao_frames<<<grid_for(slots, ctx->numSMs), kThreads, 0, cs>>>(f->aoPixel, slots, f->positions, prm->width, R,
+                                                                     f->frames);
+    k_rtao_ao_rays<<<grid_for(nAo, ctx->numSMs), kThreads, 0, cs>>>(f->frames, nAo, R, f->dev, prm->aoMaxRadius,
+                                                                    f->aoRays);
     HRT_CUDA(ctx, cudaGetLastError());
     if ((st = hrt_query_any(s, reinterpret_cast<const float*>(f->aoRays), nAo, f->aoHit, stream))) return st;
     k_rtao_colors<<<grid_for(slots, ctx->numSMs), kThreads, 0, cs>>>(f->aoHit, f->aoPixel, slots, R, prm->power,
