@@ -959,18 +959,36 @@ def run_engine(args):
     L = E.lib()
     import ctypes as C
 
-    def e2e_step():
+    def e2e_step_sync():
         ctx.check(L.hrt_query_nearest_host(scene._h, C.c_void_p(pin_eye.ptr), n_eye, C.c_void_p(pin_hits.ptr)), "e2e")
         ctx.check(L.hrt_query_any_host(scene._h, C.c_void_p(pin_ao.ptr), n_ao, C.c_void_p(pin_any.ptr)), "e2e")
 
-    for _ in range(max(3, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = replicas.max_over_ranks(rk, (time.perf_counter() - t0) / args.steps, "cuda")
+    # the same two batches enqueued on two streams (reported beside the value):
+    # both streams are waited for, then the scene's device-side checks read
+    s_eye, s_ao = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def e2e_step():
+        ctx.check(L.hrt_query_nearest_host_async(scene._h, C.c_void_p(pin_eye.ptr), n_eye, C.c_void_p(pin_hits.ptr),
+                                                 C.c_void_p(s_eye.cuda_stream)), "e2e")
+        ctx.check(L.hrt_query_any_host_async(scene._h, C.c_void_p(pin_ao.ptr), n_ao, C.c_void_p(pin_any.ptr),
+                                             C.c_void_p(s_ao.cuda_stream)), "e2e")
+        s_eye.synchronize()
+        s_ao.synchronize()
+        ctx.check(L.hrt_scene_check(scene._h), "e2e")
+
+    def time_steps(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        return replicas.max_over_ranks(rk, (time.perf_counter() - t0) / args.steps, "cuda")
+
+    e2e_async_s = time_steps(e2e_step)
+    e2e_s = time_steps(e2e_step_sync)
     e2e_value = replicas.job_throughput(rk, rays_per_step, 1e3 * e2e_s) / 1e6
+    e2e_async_value = replicas.job_throughput(rk, rays_per_step, 1e3 * e2e_async_s) / 1e6
     got_any = pin_any.array(np.uint8)[:n_ao].copy()
 
     # the same frame with its rays made on the device: camera parameters in,
@@ -1082,6 +1100,8 @@ def run_engine(args):
                    "node_pairs_per_eye_ray": round(eye_pairs / n_eye, 3),
                    "node_pairs_per_ao_ray": round(ao_pairs / n_ao, 3)},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(RAY_BYTES * (n_eye + n_ao)),
+                "api": "hrt_query_nearest_host + hrt_query_any_host, page-locked arrays",
+                "async_two_streams_value": round(e2e_async_value, 3),
                 "d2h_bytes_per_step": int(32 * n_eye + n_ao)},
         "e2e_device_raygen": raygen_e2e,
         "gpu_launches": 2 * args.steps,

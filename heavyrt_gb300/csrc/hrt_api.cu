@@ -1101,6 +1101,29 @@ int hrt_query_any(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out, voi
   return launch_query(s, 1, rays, n, out, 0, (cudaStream_t)stream);
 }
 
+// Reads (after the work on `cs`) and clears the scene's device-side check
+// word: the step budget, the stack bound, index checks of the traversals.
+static int read_device_check(hrt_scene* s, cudaStream_t cs)
+{
+  hrt_context* ctx = s->ctx;
+  uint32_t ew[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  HRT_CUDA(ctx, cudaMemcpyAsync(ew, s->dError, sizeof(ew), cudaMemcpyDeviceToHost, cs));
+  HRT_CUDA(ctx, cudaStreamSynchronize(cs));
+  const uint32_t err = ew[0];
+  if (!err) return HRT_OK;
+  cudaMemsetAsync(s->dError, 0, sizeof(ew), cs);
+  cudaStreamSynchronize(cs);
+  if (err & kErrStepBudget)
+  {
+    char msg[200];
+    std::snprintf(msg, sizeof(msg), "a ray exceeded the traversal step budget (ray %u, ref 0x%08x, stack depth %d)",
+                  ew[2], ew[3], (int)ew[4]);
+    return fail(ctx, HRT_ERR_DEVICE_CHECK, msg);
+  }
+  if (err & kErrStack) return fail(ctx, HRT_ERR_DEVICE_CHECK, "traversal stack bound exceeded");
+  return fail(ctx, HRT_ERR_DEVICE_CHECK, "device-side check failed during a query");
+}
+
 static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out)
 {
   if (!s) return HRT_ERR_INVALID_ARGUMENT;
@@ -1161,26 +1184,37 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
   }
   if (nPipe > 1)
     for (int p = 0; p < nPipe; p++) HRT_CUDA(ctx, cudaStreamSynchronize(s->pipe[p]));
-  uint32_t ew[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  HRT_CUDA(ctx, cudaMemcpyAsync(ew, s->dError, sizeof(ew), cudaMemcpyDeviceToHost, cs));
-  HRT_CUDA(ctx, cudaStreamSynchronize(cs));
-  const uint32_t err = ew[0];
-  if (err)
+  return read_device_check(s, cs);
+}
+
+// Asynchronous host-pointer query: page-locked rays are read in place,
+// page-locked any-hit flags written in place; everything else goes through
+// stream-ordered device allocations and copies on `st`.
+static int query_host_async(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out, cudaStream_t st)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  if (n == 0) return HRT_OK;
+  if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
+  hrt_context* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  const float* mappedRays = static_cast<const float*>(mapped_host(rays));
+  void* mappedOut = kind == 1 ? mapped_host(out) : nullptr;
+  const size_t outSize = kind == 0 ? sizeof(hrt_hit) : 1;
+  float* dRays = nullptr;
+  void* dOut = nullptr;
+  if (!mappedRays)
   {
-    cudaMemsetAsync(s->dError, 0, sizeof(ew), cs);
-    cudaStreamSynchronize(cs);
-    if (err & kErrStepBudget)
-    {
-      char msg[200];
-      std::snprintf(msg, sizeof(msg),
-                    "a ray exceeded the traversal step budget (ray %u, ref 0x%08x, stack depth %d)", ew[2], ew[3],
-                    (int)ew[4]);
-      return fail(ctx, HRT_ERR_DEVICE_CHECK, msg);
-    }
-    if (err & kErrStack) return fail(ctx, HRT_ERR_DEVICE_CHECK, "traversal stack bound exceeded");
-    return fail(ctx, HRT_ERR_DEVICE_CHECK, "device-side check failed during a query");
+    HRT_CUDA(ctx, cudaMallocAsync((void**)&dRays, 32 * n, st));
+    HRT_CUDA(ctx, cudaMemcpyAsync(dRays, rays, 32 * n, cudaMemcpyHostToDevice, st));
   }
-  return HRT_OK;
+  if (!mappedOut) HRT_CUDA(ctx, cudaMallocAsync(&dOut, outSize * n, st));
+  int r = launch_query(s, kind, mappedRays ? mappedRays : dRays, n, mappedOut ? mappedOut : dOut, 0, st);
+  cudaError_t e = cudaSuccess;
+  if (r == HRT_OK && dOut) e = cudaMemcpyAsync(out, dOut, outSize * n, cudaMemcpyDeviceToHost, st);
+  if (dRays) cudaFreeAsync(dRays, st);
+  if (dOut) cudaFreeAsync(dOut, st);
+  if (r == HRT_OK && e != cudaSuccess) r = cuda_fail(ctx, e, "result copy");
+  return r;
 }
 
 int hrt_query_nearest_host(hrt_scene* s, const float* rays, uint64_t n, hrt_hit* hits)
@@ -1189,6 +1223,23 @@ int hrt_query_nearest_host(hrt_scene* s, const float* rays, uint64_t n, hrt_hit*
 }
 
 int hrt_query_any_host(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out) { return query_host(s, 1, rays, n, out); }
+
+int hrt_query_nearest_host_async(hrt_scene* s, const float* rays, uint64_t n, hrt_hit* hits, void* stream)
+{
+  return query_host_async(s, 0, rays, n, hits, (cudaStream_t)stream);
+}
+
+int hrt_query_any_host_async(hrt_scene* s, const float* rays, uint64_t n, uint8_t* out, void* stream)
+{
+  return query_host_async(s, 1, rays, n, out, (cudaStream_t)stream);
+}
+
+int hrt_scene_check(hrt_scene* s)
+{
+  if (!s) return HRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(s->ctx->device);
+  return read_device_check(s, s->ctx->stream);
+}
 
 int hrt_query_counters(hrt_scene* s, int kind, const float* rays, uint64_t n, uint64_t counters[2], void* stream)
 {

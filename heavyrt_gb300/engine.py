@@ -169,6 +169,9 @@ def lib() -> C.CDLL:
         "hrt_query_any": (i32, [vp, vp, u64, vp, vp]),
         "hrt_query_nearest_host": (i32, [vp, vp, u64, vp]),
         "hrt_query_any_host": (i32, [vp, vp, u64, vp]),
+        "hrt_query_nearest_host_async": (i32, [vp, vp, u64, vp, vp]),
+        "hrt_query_any_host_async": (i32, [vp, vp, u64, vp, vp]),
+        "hrt_scene_check": (i32, [vp]),
         "hrt_query_counters": (i32, [vp, i32, vp, u64, vp, vp]),
         "hrt_get_geom_num": (i32, [vp, C.POINTER(u32)]),
         "hrt_get_inst_num": (i32, [vp, C.POINTER(u32)]),

@@ -192,6 +192,20 @@ int hrt_query_any(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out,
 int hrt_query_nearest_host(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits);
 int hrt_query_any_host(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out);
 
+/* The host-pointer queries, enqueued on `stream` instead of waited for: the
+ * results are in place once the stream has reached them.  Page-locked arrays
+ * are used in place as above; other memory goes through stream-ordered device
+ * allocations (a pageable result array makes the final copy synchronous).
+ * Queries on different streams overlap, e.g. one batch's result copy with the
+ * next batch's traversal.  The arrays must stay valid until the stream is done. */
+int hrt_query_nearest_host_async(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits, void* stream);
+int hrt_query_any_host_async(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out, void* stream);
+
+/* Reads and clears the scene's device-side check word after asynchronous
+ * queries (call once their streams are synchronised): HRT_ERR_DEVICE_CHECK if
+ * a ray ran out of its step budget or the stack bound, HRT_OK otherwise. */
+int hrt_scene_check(hrt_scene* scene);
+
 /* Launch shape of the traversal kernel, per query kind (0 nearest, 1 any);
  * results never depend on it.  No reference counterpart (the reference runs
  * one ray per virtual call).  Defaults: 128 threads, persistent pool,

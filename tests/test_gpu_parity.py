@@ -220,6 +220,30 @@ def test_large_host_queries_are_pipelined_exactly(native):
     np.testing.assert_array_equal(pin_out.array(np.uint8, n).astype(bool), want_a)
     small = pinned_rays[:1000]
     np.testing.assert_array_equal(s.RayQuery_NearestHit(small).view(np.uint32).reshape(-1, 8), want_h[:1000])
+    # asynchronous forms on two streams, page-locked and pageable arrays
+    pin_hits = PinnedBuffer(32 * n)
+    pageable_hits = np.zeros((n, 8), np.uint32)
+    pageable_any = np.zeros(n, np.uint8)
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    L = E.lib()
+    pin_out.array(np.uint8, n)[:] = 7
+    assert L.hrt_query_nearest_host_async(s._h, ctypes.c_void_p(pin.ptr), n, ctypes.c_void_p(pin_hits.ptr),
+                                          ctypes.c_void_p(sa.cuda_stream)) == 0
+    assert L.hrt_query_any_host_async(s._h, ctypes.c_void_p(pin.ptr), n, ctypes.c_void_p(pin_out.ptr),
+                                      ctypes.c_void_p(sb.cuda_stream)) == 0
+    assert L.hrt_query_nearest_host_async(s._h, rays.ctypes.data_as(ctypes.c_void_p), n,
+                                          pageable_hits.ctypes.data_as(ctypes.c_void_p),
+                                          ctypes.c_void_p(sb.cuda_stream)) == 0
+    assert L.hrt_query_any_host_async(s._h, rays.ctypes.data_as(ctypes.c_void_p), n,
+                                      pageable_any.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(sa.cuda_stream)) == 0
+    sa.synchronize()
+    sb.synchronize()
+    assert L.hrt_scene_check(s._h) == 0
+    np.testing.assert_array_equal(pin_hits.array(np.uint32, 8 * n).reshape(-1, 8), want_h)
+    np.testing.assert_array_equal(pin_out.array(np.uint8, n).astype(bool), want_a)
+    np.testing.assert_array_equal(pageable_hits, want_h)
+    np.testing.assert_array_equal(pageable_any.astype(bool), want_a)
+    pin_hits.free()
     pin.free()
     pin_out.free()
     assert 0.2 < want_a.mean() < 1.0
