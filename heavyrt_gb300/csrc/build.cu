@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode
   {
     uint32_t node = L - 1 + i;
     lrCount[node] = 0;
-    __threadfence();
+    // no fences: the acquire-release add on the parent's counter publishes this
+    // thread's writes to the sibling's thread that finishes the parent
     while (node != 0)
     {
       const uint32_t p = parent[node];
@@ -240,18 +241,11 @@ __global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode
       }
       if (atomic_add_acq_rel(&visit[p], 1u) == 0u) break;  // the sibling is not finished yet
       const uint32_t l = __ldcg(&lr[p].leftOffset), r = __ldcg(&lr[p].escapeIndex);
-      BVHNode32 out;
-      out.leftOffset = l;
-      out.escapeIndex = r;
-#pragma unroll
-      for (int c = 0; c < 3; c++)
-      {
-        out.boxMin[c] = lm_min(__ldcg(&lr[l].boxMin[c]), __ldcg(&lr[r].boxMin[c]));
-        out.boxMax[c] = lm_max(__ldcg(&lr[l].boxMax[c]), __ldcg(&lr[r].boxMax[c]));
-      }
-      lr[p] = out;
+      float4 alo, ahi, blo, bhi;
+      bc::load_node_cg(lr + l, alo, ahi);
+      bc::load_node_cg(lr + r, blo, bhi);
+      bc::store_parent(lr + p, alo, ahi, blo, bhi, l, r);
       lrCount[p] = __ldcg(&lrCount[l]) + __ldcg(&lrCount[r]) + 2u;
-      __threadfence();
       node = p;
     }
   }

@@ -290,7 +290,8 @@ __global__ void __launch_bounds__(kThreads) k_seg_refit(const uint32_t* __restri
     const uint32_t L = leafOffsets[s + 1] - leafOffsets[s];
     const uint32_t nb = nodeOffsets[s], ib = intOffsets[s];
     uint32_t node = L - 1 + (g - leafOffsets[s]);
-    __threadfence();
+    // no fences: the acquire-release add on the parent's counter publishes this
+    // thread's writes to the sibling's thread that finishes the parent
     while (node != 0)
     {
       const uint32_t p = parent[nb + node];
@@ -301,18 +302,11 @@ __global__ void __launch_bounds__(kThreads) k_seg_refit(const uint32_t* __restri
       }
       if (bc::atomic_add_acq_rel(&visit[ib + p], 1u) == 0u) break;
       const uint32_t l = __ldcg(&lr[nb + p].leftOffset), r = __ldcg(&lr[nb + p].escapeIndex);
-      BVHNode32 out;
-      out.leftOffset = l;
-      out.escapeIndex = r;
-#pragma unroll
-      for (int c = 0; c < 3; c++)
-      {
-        out.boxMin[c] = lm_min(__ldcg(&lr[nb + l].boxMin[c]), __ldcg(&lr[nb + r].boxMin[c]));
-        out.boxMax[c] = lm_max(__ldcg(&lr[nb + l].boxMax[c]), __ldcg(&lr[nb + r].boxMax[c]));
-      }
-      lr[nb + p] = out;
+      float4 alo, ahi, blo, bhi;
+      bc::load_node_cg(lr + nb + l, alo, ahi);
+      bc::load_node_cg(lr + nb + r, blo, bhi);
+      bc::store_parent(lr + nb + p, alo, ahi, blo, bhi, l, r);
       lrCount[nb + p] = __ldcg(&lrCount[nb + l]) + __ldcg(&lrCount[nb + r]) + 2u;
-      __threadfence();
       node = p;
     }
   }

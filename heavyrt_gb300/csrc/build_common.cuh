@@ -34,6 +34,25 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v)
   return old;
 }
 
+// A node written by other threads of the same kernel, read through L2 in two
+// 16-byte loads: {boxMin, leftOffset}, {boxMax, escapeIndex}.
+__device__ __forceinline__ void load_node_cg(const BVHNode32* n, float4& lo, float4& hi)
+{
+  const float4* p = reinterpret_cast<const float4*>(n);
+  lo = __ldcg(p);
+  hi = __ldcg(p + 1);
+}
+
+// Parent box from its children's (lm_min / lm_max per axis), stored with the
+// child links in two 16-byte stores.
+__device__ __forceinline__ void store_parent(BVHNode32* n, const float4& alo, const float4& ahi, const float4& blo,
+                                             const float4& bhi, uint32_t l, uint32_t r)
+{
+  float4* p = reinterpret_cast<float4*>(n);
+  p[0] = make_float4(lm_min(alo.x, blo.x), lm_min(alo.y, blo.y), lm_min(alo.z, blo.z), __uint_as_float(l));
+  p[1] = make_float4(lm_max(ahi.x, bhi.x), lm_max(ahi.y, bhi.y), lm_max(ahi.z, bhi.z), __uint_as_float(r));
+}
+
 // SpreadBits / ZIndex3D, core/builders/lbvh.cpp:25-39.
 __device__ __forceinline__ uint32_t spread_bits(int x, int offset)
 {
