@@ -198,39 +198,57 @@ __global__ void __launch_bounds__(kThreads) k_leaves(const float4* __restrict__ 
 // their XOR (32 for equal codes, -1 out of range, as the reference defines).
 __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict__ codes,
                                                      const BuildParams* __restrict__ params, BVHNode32* __restrict__ lr,
-                                                     uint32_t* __restrict__ parent)
+                                                     uint32_t* __restrict__ parent, uint32_t* __restrict__ rangeEnd)
 {
   const int L = (int)params->nLeaves;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < L - 1; i += gridDim.x * kThreads)
   {
     uint32_t left, right;
-    bc::karras_node(codes, L, i, left, right);
+    int other;
+    bc::karras_node(codes, L, i, left, right, other);
     lr[i].leftOffset = left;
     lr[i].escapeIndex = right;
     parent[left] = (uint32_t)i;
     parent[right] = (uint32_t)i;
+    rangeEnd[i] = (uint32_t)other;
   }
 }
 
 // ---------------------------------------------------------------- refit
 // Bottom-up box union.  The reference runs 32 sweeps over all internal nodes
-// (core/builders/lbvh.cpp:443-489, :798-802); here each leaf walks to the root
-// and the second child to arrive at a node computes it, so every node is
+// (core/builders/lbvh.cpp:443-489, :798-802); here each leaf walks towards the
+// root and the second child to arrive at a node computes it, so every node is
 // computed once from its finished children: box = (min, max) of the children
 // in (left, right) order, count = children's counts + 2.
+//
+// A block owns the leaves [lo, hi) of one slice.  An internal node i of a
+// Karras tree has i as one end of its leaf range, so the nodes whose range
+// lies inside the slice are i in [lo, hi - 1): they are finished inside the
+// block, with arrival counters in shared memory (acquire-release at block
+// scope, children read through L1, coherent within the SM).  Only the nodes
+// whose range leaves the slice use the device-wide counters (acquire-release
+// at device scope, children read from L2).  Every node a thread reads was
+// written by the thread that released the counter it acquired.
 using bc::atomic_add_acq_rel;
+using bc::atomic_add_acq_rel_cta;
+constexpr uint32_t kRefitSlice = 4 * kThreads;  // leaves per block
 
-__global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode32* lr,
-                                                    uint32_t* lrCount, const uint32_t* __restrict__ parent,
-                                                    uint32_t* visit)
+__global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode32* lr, uint32_t* lrCount,
+                                                    const uint32_t* __restrict__ parent, uint32_t* visit,
+                                                    const uint32_t* __restrict__ rangeEnd)
 {
+  __shared__ uint32_t s_visit[kRefitSlice];
   const uint32_t L = params->nLeaves;
-  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < L; i += gridDim.x * kThreads)
+  const uint32_t lo = blockIdx.x * kRefitSlice;
+  if (lo >= L) return;
+  const uint32_t hi = min(lo + kRefitSlice, L);
+  for (uint32_t k = threadIdx.x; k < kRefitSlice; k += kThreads) s_visit[k] = 0u;
+  __syncthreads();
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += kThreads)
   {
     uint32_t node = L - 1 + i;
     lrCount[node] = 0;
-    // no fences: the acquire-release add on the parent's counter publishes this
-    // thread's writes to the sibling's thread that finishes the parent
+    bool inSlice = true;
     while (node != 0)
     {
       const uint32_t p = parent[node];
@@ -239,13 +257,41 @@ __global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode
         atomicOr(&params->error, kErrLayout);
         break;
       }
-      if (atomic_add_acq_rel(&visit[p], 1u) == 0u) break;  // the sibling is not finished yet
-      const uint32_t l = __ldcg(&lr[p].leftOffset), r = __ldcg(&lr[p].escapeIndex);
+      if (inSlice)
+      {
+        const uint32_t j = rangeEnd[p];
+        inSlice = (p < j ? p : j) >= lo && (p > j ? p : j) < hi;
+      }
+      uint32_t l, r;
       float4 alo, ahi, blo, bhi;
-      bc::load_node_cg(lr + l, alo, ahi);
-      bc::load_node_cg(lr + r, blo, bhi);
+      uint32_t cl, cr;
+      if (inSlice)
+      {
+        if (atomic_add_acq_rel_cta(&s_visit[p - lo], 1u) == 0u) break;  // the sibling is not finished yet
+        if (p == 0u) visit[0] = 2u;  // the root finished inside the slice (k_check_root reads the device counter)
+        l = lr[p].leftOffset;
+        r = lr[p].escapeIndex;
+        const float4* a = reinterpret_cast<const float4*>(lr + l);
+        const float4* b = reinterpret_cast<const float4*>(lr + r);
+        alo = a[0];
+        ahi = a[1];
+        blo = b[0];
+        bhi = b[1];
+        cl = lrCount[l];
+        cr = lrCount[r];
+      }
+      else
+      {
+        if (atomic_add_acq_rel(&visit[p], 1u) == 0u) break;
+        l = __ldcg(&lr[p].leftOffset);
+        r = __ldcg(&lr[p].escapeIndex);
+        bc::load_node_cg(lr + l, alo, ahi);
+        bc::load_node_cg(lr + r, blo, bhi);
+        cl = __ldcg(&lrCount[l]);
+        cr = __ldcg(&lrCount[r]);
+      }
       bc::store_parent(lr + p, alo, ahi, blo, bhi, l, r);
-      lrCount[p] = __ldcg(&lrCount[l]) + __ldcg(&lrCount[r]) + 2u;
+      lrCount[p] = cl + cr + 2u;
       node = p;
     }
   }
@@ -355,8 +401,9 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);
   if (e != cudaSuccess) return e;
-  k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent);
-  k_refit<<<g, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit);
+  k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent, b.visit + N);
+  k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
+                                                                   b.visit + N);
   k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
   k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
   return cudaGetLastError();
@@ -385,8 +432,9 @@ cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, c
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);
   if (e != cudaSuccess) return e;
-  k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent);
-  k_refit<<<g, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit);
+  k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent, b.visit + N);
+  k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
+                                                                   b.visit + N);
   k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
   k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
   return cudaGetLastError();

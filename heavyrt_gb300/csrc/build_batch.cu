@@ -266,7 +266,8 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
     const int L = (int)(leafOffsets[s + 1] - leafOffsets[s]);
     const int i = (int)(j - intOffsets[s]);
     uint32_t left, right;
-    bc::karras_node(compressed + leafOffsets[s], L, i, left, right);
+    int other;  // range end, unused here
+    bc::karras_node(compressed + leafOffsets[s], L, i, left, right, other);
     const uint32_t nb = nodeOffsets[s];
     lr[nb + i].leftOffset = left;
     lr[nb + i].escapeIndex = right;

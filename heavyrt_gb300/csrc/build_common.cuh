@@ -119,7 +119,7 @@ __device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ c, int 
 // (core/builders/lbvh.cpp:405-441); returns the children in the LR numbering
 // (internal 0..L-2, leaves L-1..2L-2).
 __device__ __forceinline__ void karras_node(const uint32_t* __restrict__ codes, int L, int i, uint32_t& left,
-                                            uint32_t& right)
+                                            uint32_t& right, int& other)
 {
   const int dl = karras_delta(codes, L, i, i + 1) - karras_delta(codes, L, i, i - 1);
   const int d = (dl > 0) - (dl < 0);
@@ -137,6 +137,17 @@ __device__ __forceinline__ void karras_node(const uint32_t* __restrict__ codes, 
   const int gamma = i + s * d + (d < 0 ? d : 0);
   left = ((i < j ? i : j) == gamma) ? (uint32_t)(L - 1 + gamma) : (uint32_t)gamma;
   right = ((i > j ? i : j) == gamma + 1) ? (uint32_t)(L - 1 + gamma + 1) : (uint32_t)(gamma + 1);
+  other = j;  // the node's leaf range is [min(i, j), max(i, j)]
+}
+
+__device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v)
+{
+  uint32_t old;
+  asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(v)
+               : "memory");
+  return old;
 }
 
 // Index of the segment containing position x: the largest s with

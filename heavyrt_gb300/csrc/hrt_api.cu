@@ -175,7 +175,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   HRT_CUDA(ctx, cudaMallocAsync((void**)&keysAlt, sizeof(uint32_t) * N, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&valsAlt, sizeof(uint32_t) * N, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * (2 * (size_t)N - 1), st));
-  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * N, st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * 2 * (size_t)N, st));
   HRT_CUDA(ctx, cudaMallocAsync(&scratch, build_scratch_bytes(N), st));
 
   BuildBuffers b;
@@ -628,7 +628,7 @@ int refit_geometry(hrt_scene* s, Geom& g, const float* vpos, const uint32_t* idx
   HRT_CUDA(ctx, cudaMallocAsync((void**)&dIdx, sizeof(uint32_t) * 3 * (size_t)N, st));
   HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * 3 * (size_t)N, cudaMemcpyHostToDevice, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * (2 * (size_t)N - 1), st));
-  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * N, st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * 2 * (size_t)N, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&box, sizeof(BuildParams), st));
   HRT_CUDA(ctx, cudaMallocAsync(&scratch, refit_scratch_bytes(), st));
   HRT_CUDA(ctx, cudaMemsetAsync(&g.params->error, 0, sizeof(uint32_t), st));

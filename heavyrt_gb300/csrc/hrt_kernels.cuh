@@ -45,7 +45,7 @@ struct BuildBuffers
   BVHNode32* lr;              // 2*nTris-1 (2L-1 used): Karras + refit tree
   uint32_t*  lrCount;         // 2*nTris-1
   uint32_t*  parent;          // 2*nTris-1
-  uint32_t*  visit;           // nTris
+  uint32_t*  visit;           // 2*nTris: refit counters, then each internal node's range end
   PairRec*   recs;            // max(nTris-1, 1)
   TriRec*    tris;            // nTris
   uint32_t*  sortedIdx;       // 3*nTris
