@@ -1072,6 +1072,18 @@ def run_engine(args):
             plain["coherent_eye_roofline"] = {"achieved": round(p_ach, 1), "frac": round(p_ach / pk, 4),
                                               "algorithmic_bytes_per_launch": int(p_bytes),
                                               "node_pairs_per_eye_ray": round(pp_eye / n_eye, 3)}
+            # HeavyRT's own bytes-loaded accounting (m_stats.BLB, core/BVH2CommonRT.cpp:68-70,125:
+            # 2 x 32 B per node step, 3 x 4 B + 3 x 16 B per tested triangle) on the same rays, with
+            # the BVH2 kernel's counts (the decisions of BVH2TraverseC32) and nearest-hit traversal
+            # for the AO rays too, the way the reference answers any-hit
+            pp_ao, pt_ao = ps.query_counters(0, d_ao.data_ptr(), n_ao, sh)
+            blb_eye = (64 * pp_eye + 60 * pt_eye) / n_eye
+            blb_ao = (64 * pp_ao + 60 * pt_ao) / n_ao
+            plain["reference_blb"] = {
+                "eye_bytes_per_ray": round(blb_eye, 2), "ao_bytes_per_ray": round(blb_ao, 2),
+                "eye_node_pairs_per_ray": round(pp_eye / n_eye, 3), "eye_tris_per_ray": round(pt_eye / n_eye, 3),
+                "ao_node_pairs_per_ray": round(pp_ao / n_ao, 3), "ao_tris_per_ray": round(pt_ao / n_ao, 3),
+                "at_plain_rate_gb_s": round((blb_eye * n_eye + blb_ao * n_ao) / ((pe_ms + pa_ms) * 1e-3) / 1e9, 1)}
         ps.close()
 
     # roofline of the dominant kernel
