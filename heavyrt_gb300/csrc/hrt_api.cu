@@ -46,17 +46,25 @@ void free_geom(Geom& g)
   {
     void* ptrs[] = {g.verts, g.keys, g.vals, g.keysUnsorted, g.compressed, g.runStarts, g.lr,
                     g.lrCount, g.recs, g.tris, g.sortedIdx, g.params, g.nodes4};
+    bool any = false;
+    for (void* p : ptrs) any = any || p != nullptr;
+    // the arrays come from the stream-ordered pool, whose cudaFree does not
+    // wait: finish every query that may still read them first
+    if (any) cudaDeviceSynchronize();
     for (void* p : ptrs)
       if (p) cudaFree(p);
   }
   g = Geom();
 }
 
-template <typename T> cudaError_t dalloc(T** p, size_t count, uint64_t* bytes)
+// A geometry array from the device's stream-ordered pool (no implicit
+// synchronisation, blocks reused from earlier builds); free_geom waits for the
+// device before it frees, so no query in flight loses it.
+template <typename T> cudaError_t dalloc(T** p, size_t count, uint64_t* bytes, cudaStream_t st)
 {
   const size_t b = sizeof(T) * (count ? count : 1);
   if (bytes) *bytes += b;
-  return cudaMalloc((void**)p, b);
+  return cudaMallocAsync((void**)p, b, st);
 }
 
 __global__ void k_pack_verts(const uint8_t* __restrict__ raw, uint64_t n, uint64_t stride, float4* __restrict__ out)
@@ -126,8 +134,8 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   g.nTris = N;
   g.nVerts = (uint32_t)nVert;
   uint64_t* bytes = &g.bytes;
-  HRT_CUDA(ctx, dalloc(&g.verts, nVert, bytes));
-  HRT_CUDA(ctx, dalloc(&g.params, 1, bytes));
+  HRT_CUDA(ctx, dalloc(&g.verts, nVert, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.params, 1, bytes, st));
   HRT_CUDA(ctx, cudaMemsetAsync(g.params, 0, sizeof(BuildParams), st));
   if (nVert)
   {
@@ -162,16 +170,16 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   void* scratch = nullptr;
   HRT_CUDA(ctx, cudaMallocAsync((void**)&dIdx, sizeof(uint32_t) * nIdx, st));
   HRT_CUDA(ctx, cudaMemcpyAsync(dIdx, idx, sizeof(uint32_t) * nIdx, cudaMemcpyDefault, st));
-  HRT_CUDA(ctx, dalloc(&g.keys, N, bytes));
-  HRT_CUDA(ctx, dalloc(&g.vals, N, bytes));
-  HRT_CUDA(ctx, dalloc(&g.keysUnsorted, N, bytes));
-  HRT_CUDA(ctx, dalloc(&g.compressed, N, bytes));
-  HRT_CUDA(ctx, dalloc(&g.runStarts, N, bytes));
-  HRT_CUDA(ctx, dalloc(&g.lr, 2 * (size_t)N - 1, bytes));
-  HRT_CUDA(ctx, dalloc(&g.lrCount, 2 * (size_t)N - 1, bytes));
-  HRT_CUDA(ctx, dalloc(&g.recs, N > 1 ? N - 1 : 1, bytes));
-  HRT_CUDA(ctx, dalloc(&g.tris, N, bytes));
-  HRT_CUDA(ctx, dalloc(&g.sortedIdx, 3 * (size_t)N, bytes));
+  HRT_CUDA(ctx, dalloc(&g.keys, N, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.vals, N, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.keysUnsorted, N, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.compressed, N, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.runStarts, N, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.lr, 2 * (size_t)N - 1, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.lrCount, 2 * (size_t)N - 1, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.recs, N > 1 ? N - 1 : 1, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.tris, N, bytes, st));
+  HRT_CUDA(ctx, dalloc(&g.sortedIdx, 3 * (size_t)N, bytes, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&keysAlt, sizeof(uint32_t) * N, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&valsAlt, sizeof(uint32_t) * N, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * (2 * (size_t)N - 1), st));
@@ -227,7 +235,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
     HRT_CUDA(ctx, cudaStreamSynchronize(st));
     if (count4 == 0) count4 = 1;  // a single leaf still gets a root node
     const size_t nodeBytes = (layout == HRT_LAYOUT_BVH4_F32) ? sizeof(Node4F32) : sizeof(Node4F16);
-    HRT_CUDA(ctx, cudaMalloc(&g.nodes4, nodeBytes * count4));
+    HRT_CUDA(ctx, cudaMallocAsync(&g.nodes4, nodeBytes * count4, st));
     g.bytes += nodeBytes * count4;
     g.nNodes4 = count4;
     HRT_CUDA(ctx, bvh4_emit(b4, layout - 1, g.nodes4, count4, ctx->numSMs, st));
@@ -808,6 +816,21 @@ int hrt_context_create(int device, hrt_context** out)
   hrt_context* c = new hrt_context();
   c->device = device;
   cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device);
+  // keep up to 2 GiB of freed stream-ordered memory in the device's pool, so
+  // that build scratch arrays and geometry arrays are reused instead of being
+  // returned to the driver at every synchronisation
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess)
+  {
+    uint64_t threshold = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold) == cudaSuccess &&
+        threshold < (2ull << 30))
+    {
+      threshold = 2ull << 30;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+  }
+  cudaGetLastError();
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
   {
     delete c;
