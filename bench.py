@@ -178,6 +178,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def build_bytes(n_tris: int, n_verts: int, n_leaves: int, n_nodes4: int, node4_bytes: int) -> int:
+    """Algorithmic bytes of one LBVH build (reads + writes of each stage, as the
+    build kernels touch them): scene box 16 B per vertex; Morton codes 12 B
+    indices + 48 B vertex gathers + 8 B pair out per triangle, plus the 8 B
+    copy of the unsorted codes; radix sort 4 digit passes x (8 B in + 8 B out)
+    + 4 B histogram read per pair; run compaction 4 B per code in + 8 B per run
+    out; leaves 4 + 12 + 48 + 48 + 12 B per triangle + 32 B per leaf; Karras
+    hierarchy 2 log2(L) code reads + 16 B out per internal node; refit 2 x 32 B
+    + 2 x 4 B in, 32 B + 4 B out per internal node; pair records 96 B in + 64 B
+    out per internal node; 4-wide collapse 9 B of plan arrays per internal node
+    + 4 x 32 B in + one node out per 4-wide node."""
+    import math
+
+    internal = max(n_leaves - 1, 0)
+    log_l = math.log2(max(n_leaves, 2))
+    return int(16 * n_verts + n_tris * (12 + 48 + 8 + 8) + n_tris * (4 * 16 + 4) + 4 * n_tris + 8 * n_leaves
+               + n_tris * (4 + 12 + 48 + 48 + 12) + 32 * n_leaves + internal * (8 * log_l + 16)
+               + internal * (64 + 8 + 32 + 4) + internal * (96 + 64)
+               + (internal * 9 + n_nodes4 * (4 * 32 + node4_bytes) if n_nodes4 else 0))
+
+
 def make_frame(args):
     """Scene + eye rays of the heightfield RTAO frame (host arrays)."""
     from heavyrt_gb300 import workload as wl
@@ -1094,6 +1115,14 @@ def run_engine(args):
         dom, dom_ms, dom_bytes, dom_name = "nearest", eye_avg, eye_bytes, "k_trace<nearest>"
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    node4_size = {"bvh2": 0, "bvh4": 128, "bvh4_f16": 64, "bvh4_q8": 64}[args.layout]
+    n4 = int(scene.export(gid, E.EXPORT_NODES4).nbytes // node4_size) if node4_size else 0
+    bb = build_bytes(int(w.idx.size // 3), int(w.verts.shape[0]), int(info["leaves"]), n4, node4_size)
+    build_ach = bb / (statistics.median(build_ms) * 1e-3) / 1e9
+    build_roofline = {"algorithmic_bytes": bb, "achieved_gb_s": round(build_ach, 1),
+                      "frac": round(build_ach / peak, 4), "nodes4": n4,
+                      "note": "per-stage reads + writes of the build kernels over the GPU build time; the stages are "
+                              "short launches over a few M elements, so the build is latency- and launch-bound"}
     lay = "" if args.layout == "bvh2" else f"_{args.layout}"
     traffic = profile_traffic(f"trace_{dom}{lay}_heightfield2M.txt")
     eye_achieved = eye_bytes / (eye_avg * 1e-3) / 1e9  # the coherent (eye-ray) kernel
@@ -1107,6 +1136,7 @@ def run_engine(args):
                    "l2": f"inputs larger than L2: rays {(d_eye.nbytes + d_ao.nbytes) / 1e6:.0f} MB, "
                          f"BVH+triangles {info['bytes'] / 1e6:.0f} MB",
                    "build_ms_median": round(statistics.median(build_ms), 3),
+                   "build_roofline": build_roofline,
                    "eye_ms": round(eye_avg, 4), "ao_ms": round(ao_avg, 4),
                    "eye_mrays_s": round(n_eye / eye_avg / 1e3, 2), "ao_mrays_s": round(n_ao / ao_avg / 1e3, 2),
                    "node_pairs_per_eye_ray": round(eye_pairs / n_eye, 3),
