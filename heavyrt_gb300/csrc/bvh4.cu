@@ -15,6 +15,7 @@
 // can only add visits; the triangle test is unchanged.
 #include <cuda_fp16.h>
 
+#include "build_common.cuh"
 #include "hrt_kernels.cuh"
 
 namespace hrt
@@ -24,23 +25,26 @@ namespace
 
 constexpr int kThreads = 256;
 
-// Depth of every internal node: walk up the parent chain (depth <= 30).
+// Depth of internal node i of one tree: walk up the parent chain (depth <= 30).
+__device__ __forceinline__ uint8_t node_depth(const uint32_t* __restrict__ parent, uint32_t L, uint32_t i)
+{
+  uint32_t d = 0, n = i;
+  while (n != 0 && d < 255)
+  {
+    const uint32_t p = parent[n];
+    if (p + 1u >= L) break;  // only the root lacks an internal parent
+    n = p;
+    d++;
+  }
+  return (uint8_t)d;
+}
+
 __global__ void __launch_bounds__(kThreads) k_depth(const BuildParams* __restrict__ params,
                                                     const uint32_t* __restrict__ parent, uint8_t* __restrict__ depth)
 {
   const uint32_t L = params->nLeaves;
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i + 1 < L; i += gridDim.x * kThreads)
-  {
-    uint32_t d = 0, n = i;
-    while (n != 0 && d < 255)
-    {
-      const uint32_t p = parent[n];
-      if (p + 1u >= L) break;  // only the root lacks an internal parent
-      n = p;
-      d++;
-    }
-    depth[i] = (uint8_t)d;
-  }
+    depth[i] = node_depth(parent, L, i);
 }
 
 // First sorted triangle and one-past-last of the triangles under binary node s.
@@ -56,9 +60,25 @@ __device__ __forceinline__ void node_range(const BVHNode32* __restrict__ lr, con
   end = (lb + 1 < L) ? runStarts[lb + 1] : nTris;
 }
 
-// Role of each internal node: 1 = 4-wide node, 2 = merged leaf, 0 = absorbed.
+// Role of internal node i: 1 = 4-wide node, 2 = merged leaf, 0 = absorbed.
 // mergeMode 0: merge when both children are leaves (the reference's rule);
 // mergeMode M > 0: merge when the subtree holds at most M triangles.
+__device__ __forceinline__ uint8_t node_role(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
+                                             uint32_t L, uint32_t nTris, uint8_t depth, int mergeMode, uint32_t i)
+{
+  if ((depth & 1u) != 0u) return 0;
+  bool merge;
+  if (mergeMode == 0)
+    merge = lr[i].leftOffset + 1u >= L && lr[i].escapeIndex + 1u >= L;
+  else
+  {
+    uint32_t st, en;
+    node_range(lr, runStarts, L, nTris, i, st, en);
+    merge = en - st <= (uint32_t)mergeMode;
+  }
+  return (i != 0 && merge) ? 2 : 1;
+}
+
 __global__ void __launch_bounds__(kThreads) k_roles(const BuildParams* __restrict__ params,
                                                     const BVHNode32* __restrict__ lr,
                                                     const uint32_t* __restrict__ runStarts, uint32_t nTris,
@@ -67,28 +87,15 @@ __global__ void __launch_bounds__(kThreads) k_roles(const BuildParams* __restric
 {
   const uint32_t L = params->nLeaves;
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i + 1 < L; i += gridDim.x * kThreads)
-  {
-    uint8_t r = 0;
-    if ((depth[i] & 1u) == 0u)
-    {
-      bool merge;
-      if (mergeMode == 0)
-        merge = lr[i].leftOffset + 1u >= L && lr[i].escapeIndex + 1u >= L;
-      else
-      {
-        uint32_t st, en;
-        node_range(lr, runStarts, L, nTris, i, st, en);
-        merge = en - st <= (uint32_t)mergeMode;
-      }
-      r = (i != 0 && merge) ? 2 : 1;
-    }
-    role[i] = r;
-  }
+    role[i] = node_role(lr, runStarts, L, nTris, depth[i], mergeMode, i);
 }
 
 // Exclusive scan of (role == 1) over the internal nodes: the 4-wide node index
-// of each binary node that becomes one, in Karras order (the root gets 0).
-// One block per 4096 nodes, decoupled look-back as in the run compaction.
+// of each binary node that becomes one, in Karras order (the root gets 0); the
+// prefix is written at every position.  n = L - 1 of params, or nGiven when
+// params is null (the internal nodes of a whole batch, geometry after
+// geometry).  One block per 4096 nodes, decoupled look-back as in the run
+// compaction.
 constexpr int      kScanItems  = 16;
 constexpr uint32_t kScanTile   = kThreads * kScanItems;
 constexpr uint32_t kFlagAgg    = 1u << 30;
@@ -107,15 +114,15 @@ __device__ __forceinline__ uint32_t load_relaxed(const uint32_t* p)
   return v;
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_roles(const BuildParams* __restrict__ params,
+__global__ void __launch_bounds__(kThreads) k_scan_roles(const BuildParams* __restrict__ params, uint32_t nGiven,
                                                          const uint8_t* __restrict__ role, uint32_t* __restrict__ index,
                                                          uint32_t* tileStatus, uint32_t* tileCounter, uint32_t* total,
                                                          uint32_t* errorWord)
 {
   __shared__ uint32_t s_tile, s_prefix;
   __shared__ uint32_t s_warp[kThreads / 32 + 1];
-  const uint32_t L = params->nLeaves;
-  const uint32_t n = L > 1 ? L - 1 : 0;
+  const uint32_t L = params ? params->nLeaves : 0u;
+  const uint32_t n = params ? (L > 1 ? L - 1 : 0) : nGiven;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(tileCounter, 1u);
   __syncthreads();
@@ -188,7 +195,11 @@ __global__ void __launch_bounds__(kThreads) k_scan_roles(const BuildParams* __re
   for (int k = 0; k < kScanItems; k++)
   {
     const uint32_t i = base + k;
-    if (i < n) index[i] = (flags & (1u << k)) ? pos++ : 0xFFFFFFFFu;
+    if (i < n)
+    {
+      index[i] = pos;
+      pos += (flags >> k) & 1u;
+    }
   }
 }
 
@@ -239,6 +250,153 @@ __device__ __forceinline__ uint32_t q8_hi(float origin, float v, float scale, bo
   return (uint32_t)q;
 }
 
+// One 4-wide node written in `format` (0 FP32, 1 FP16 rounded outward, 2
+// 8-bit in a per-node frame) from its ns used slots.
+__device__ __forceinline__ void write_node4(int format, void* __restrict__ nodes, uint32_t outIdx, Slot (&slot)[4],
+                                            int ns, uint32_t* errorWord)
+{
+  for (int k = ns; k < 4; k++)
+  {
+    for (int c = 0; c < 3; c++) { slot[k].lo[c] = 0.0f; slot[k].hi[c] = 0.0f; }
+    slot[k].ref = kEmptyRef;
+  }
+  if (format == 0)
+  {
+    Node4F32 o;
+    o.lox = make_float4(slot[0].lo[0], slot[1].lo[0], slot[2].lo[0], slot[3].lo[0]);
+    o.loy = make_float4(slot[0].lo[1], slot[1].lo[1], slot[2].lo[1], slot[3].lo[1]);
+    o.loz = make_float4(slot[0].lo[2], slot[1].lo[2], slot[2].lo[2], slot[3].lo[2]);
+    o.hix = make_float4(slot[0].hi[0], slot[1].hi[0], slot[2].hi[0], slot[3].hi[0]);
+    o.hiy = make_float4(slot[0].hi[1], slot[1].hi[1], slot[2].hi[1], slot[3].hi[1]);
+    o.hiz = make_float4(slot[0].hi[2], slot[1].hi[2], slot[2].hi[2], slot[3].hi[2]);
+    o.ref = make_uint4(slot[0].ref, slot[1].ref, slot[2].ref, slot[3].ref);
+    o.pad = make_uint4(0, 0, 0, 0);
+    reinterpret_cast<Node4F32*>(nodes)[outIdx] = o;
+  }
+  else if (format == 1)
+  {
+    uint32_t w[12];
+    for (int k = 0; k < 4; k++)
+    {
+      w[0 + k] = h2_bits(__float2half_rd(slot[k].lo[0]), __float2half_rd(slot[k].lo[1]));
+      w[4 + k] = h2_bits(__float2half_rd(slot[k].lo[2]), __float2half_ru(slot[k].hi[0]));
+      w[8 + k] = h2_bits(__float2half_ru(slot[k].hi[1]), __float2half_ru(slot[k].hi[2]));
+    }
+    Node4F16 o;
+    o.a = make_uint4(w[0], w[1], w[2], w[3]);
+    o.b = make_uint4(w[4], w[5], w[6], w[7]);
+    o.c = make_uint4(w[8], w[9], w[10], w[11]);
+    o.ref = make_uint4(slot[0].ref, slot[1].ref, slot[2].ref, slot[3].ref);
+    reinterpret_cast<Node4F16*>(nodes)[outIdx] = o;
+  }
+  else
+  {
+    // frame: the union of the slots' boxes; per-axis power-of-two scale
+    float org[3], scale[3];
+    int ex[3];
+    for (int c = 0; c < 3; c++)
+    {
+      float mn = slot[0].lo[c], mx = slot[0].hi[c];
+      for (int k = 1; k < ns; k++)
+      {
+        mn = fminf(mn, slot[k].lo[c]);
+        mx = fmaxf(mx, slot[k].hi[c]);
+      }
+      org[c] = mn;
+      ex[c] = q8_exponent(__fsub_rn(mx, mn));
+      // widen the scale until the frame's top is representable outward
+      for (int guard = 0; guard < 4; guard++)
+      {
+        if (q8_decode(org[c], 255u, q8_scale(ex[c])) >= mx || ex[c] >= 127) break;
+        ex[c]++;
+      }
+      scale[c] = q8_scale(ex[c]);
+    }
+    uint32_t qb[6] = {0, 0, 0, 0, 0, 0};  // lox, loy, loz, hix, hiy, hiz: 4 bytes each (one per slot)
+    for (int k = 0; k < ns; k++)
+      for (int c = 0; c < 3; c++)
+      {
+        bool ok = true;
+        const uint32_t lo = q8_lo(org[c], slot[k].lo[c], scale[c]);
+        const uint32_t hi = q8_hi(org[c], slot[k].hi[c], scale[c], ok);
+        if (!ok) atomicOr(errorWord, kErrLayout);
+        qb[c] |= lo << (8 * k);
+        qb[3 + c] |= hi << (8 * k);
+      }
+    Node4Q8 o;
+    o.frame = make_float4(org[0], org[1], org[2],
+                          __uint_as_float((uint32_t)(ex[0] + 128) | ((uint32_t)(ex[1] + 128) << 8) |
+                                          ((uint32_t)(ex[2] + 128) << 16)));
+    o.q0 = make_uint4(qb[0], qb[1], qb[2], qb[3]);
+    o.q1 = make_uint4(qb[4], qb[5], 0u, 0u);
+    o.ref = make_uint4(slot[0].ref, slot[1].ref, slot[2].ref, slot[3].ref);
+    reinterpret_cast<Node4Q8*>(nodes)[outIdx] = o;
+  }
+}
+
+// The slots of the 4-wide node that binary node i (role 1) of one tree becomes:
+// its grandchildren, or a child itself when that child is a leaf.  A slot is a
+// leaf (kLeafBit | first triangle), a merged leaf (role 2: its runs joined, the
+// 4-wide end flag cleared at the ends of the runs before the last), or the
+// 4-wide node indexOf(child) of another role-1 node.  With one leaf (L == 1)
+// the node holds that leaf alone.  Returns the number of used slots.
+template <typename IndexOf>
+__device__ __forceinline__ int node4_slots(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
+                                           uint32_t L, uint32_t nTris, const uint8_t* __restrict__ role,
+                                           IndexOf indexOf, uint32_t i, TriRec* __restrict__ tris, Slot (&slot)[4])
+{
+  if (L == 1u)
+  {
+    const BVHNode32 n = lr[0];
+    for (int c = 0; c < 3; c++) { slot[0].lo[c] = n.boxMin[c]; slot[0].hi[c] = n.boxMax[c]; }
+    slot[0].ref = kLeafBit | runStarts[0];
+    return 1;
+  }
+  const uint32_t kids[2] = {lr[i].leftOffset, lr[i].escapeIndex};
+  uint32_t cand[4];
+  int nc = 0;
+  for (int k = 0; k < 2; k++)
+  {
+    const uint32_t c = kids[k];
+    if (c + 1u >= L)
+      cand[nc++] = c;
+    else
+    {
+      cand[nc++] = lr[c].leftOffset;
+      cand[nc++] = lr[c].escapeIndex;
+    }
+  }
+  for (int k = 0; k < nc; k++)
+  {
+    const uint32_t s = cand[k];
+    const BVHNode32 n = lr[s];
+    for (int c = 0; c < 3; c++) { slot[k].lo[c] = n.boxMin[c]; slot[k].hi[c] = n.boxMax[c]; }
+    if (s + 1u >= L)
+      slot[k].ref = kLeafBit | runStarts[s - (L - 1)];
+    else if (role[s] == 2)
+    {
+      uint32_t st, en;
+      node_range(lr, runStarts, L, nTris, s, st, en);
+      slot[k].ref = kLeafBit | st;
+      uint32_t a = s, b = s;
+      while (a + 1u < L) a = lr[a].leftOffset;
+      while (b + 1u < L) b = lr[b].escapeIndex;
+      for (uint32_t leaf = a - (L - 1); leaf < b - (L - 1); leaf++)
+      {
+        const uint32_t runEnd = runStarts[leaf + 1];
+        if (runEnd > st && runEnd < en)
+        {
+          const uint32_t w = __float_as_uint(tris[runEnd - 1].a.w);
+          tris[runEnd - 1].a.w = __uint_as_float(w & ~2u);
+        }
+      }
+    }
+    else
+      slot[k].ref = indexOf(s);
+  }
+  return nc;
+}
+
 __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restrict__ params,
                                                     const BVHNode32* __restrict__ lr,
                                                     const uint32_t* __restrict__ runStarts, uint32_t nTris,
@@ -251,18 +409,8 @@ __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restric
   const uint32_t count = (L == 1u) ? 1u : L - 1u;
   for (uint32_t i = first; i < count; i += gridDim.x * kThreads)
   {
-    Slot slot[4];
-    int ns = 0;
-    uint32_t outIdx;
-    if (L == 1u)
-    {
-      outIdx = 0;
-      const BVHNode32 n = lr[0];
-      for (int c = 0; c < 3; c++) { slot[0].lo[c] = n.boxMin[c]; slot[0].hi[c] = n.boxMax[c]; }
-      slot[0].ref = kLeafBit | runStarts[0];
-      ns = 1;
-    }
-    else
+    uint32_t outIdx = 0;
+    if (L != 1u)
     {
       if (role[i] != 1) continue;
       outIdx = index[i];
@@ -271,129 +419,131 @@ __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restric
         atomicOr(errorWord, kErrLayout);
         continue;
       }
-      const uint32_t kids[2] = {lr[i].leftOffset, lr[i].escapeIndex};
-      uint32_t cand[4];
-      int nc = 0;
-      for (int k = 0; k < 2; k++)
-      {
-        const uint32_t c = kids[k];
-        if (c + 1u >= L)
-          cand[nc++] = c;
-        else
-        {
-          cand[nc++] = lr[c].leftOffset;
-          cand[nc++] = lr[c].escapeIndex;
-        }
-      }
-      for (int k = 0; k < nc; k++)
-      {
-        const uint32_t s = cand[k];
-        const BVHNode32 n = lr[s];
-        for (int c = 0; c < 3; c++) { slot[k].lo[c] = n.boxMin[c]; slot[k].hi[c] = n.boxMax[c]; }
-        if (s + 1u >= L)
-          slot[k].ref = kLeafBit | runStarts[s - (L - 1)];
-        else if (role[s] == 2)
-        {
-          uint32_t st, en;
-          node_range(lr, runStarts, L, nTris, s, st, en);
-          slot[k].ref = kLeafBit | st;
-          // the merged leaf ends at the end of its last run: clear the 4-wide
-          // end flag (bit 1) at the ends of the runs before it
-          uint32_t a = s, b = s;
-          while (a + 1u < L) a = lr[a].leftOffset;
-          while (b + 1u < L) b = lr[b].escapeIndex;
-          for (uint32_t leaf = a - (L - 1); leaf < b - (L - 1); leaf++)
-          {
-            const uint32_t runEnd = runStarts[leaf + 1];
-            if (runEnd > st && runEnd < en)
-            {
-              const uint32_t w = __float_as_uint(tris[runEnd - 1].a.w);
-              tris[runEnd - 1].a.w = __uint_as_float(w & ~2u);
-            }
-          }
-        }
-        else
-          slot[k].ref = index[s];
-      }
-      ns = nc;
     }
-    for (int k = ns; k < 4; k++)
+    Slot slot[4];
+    const int ns = node4_slots(lr, runStarts, L, nTris, role, [&](uint32_t c) { return index[c]; }, i, tris, slot);
+    write_node4(format, nodes, outIdx, slot, ns, errorWord);
+  }
+}
+
+// ---------------------------------------------------------------- batches
+// The same collapse for the geometries of a segmented build at once: internal
+// node j of the batch is node j - intOffsets[s] of geometry s; each geometry's
+// 4-wide nodes are numbered from 0 (its root) and stored at node4Off[s].
+struct SegTree
+{
+  const BVHNode32* lr;
+  const uint32_t*  runStarts;
+  const uint32_t*  parent;
+  TriRec*          tris;
+  uint32_t         L, nTris, intBase, seg;
+};
+
+__device__ __forceinline__ SegTree seg_tree(const Bvh4Batch& b, uint32_t seg)
+{
+  SegTree t;
+  t.seg = seg;
+  t.lr = b.lr + b.nodeOffsets[seg];
+  t.parent = b.parent + b.nodeOffsets[seg];
+  t.runStarts = b.runStarts + b.leafOffsets[seg];
+  t.tris = b.tris + b.triOffsets[seg];
+  t.L = b.leafOffsets[seg + 1] - b.leafOffsets[seg];
+  t.nTris = b.triOffsets[seg + 1] - b.triOffsets[seg];
+  t.intBase = b.intOffsets[seg];
+  return t;
+}
+
+__global__ void __launch_bounds__(kThreads) k_seg4_depth_roles(Bvh4Batch b, uint32_t nInt, uint8_t* __restrict__ role)
+{
+  for (uint32_t j = blockIdx.x * kThreads + threadIdx.x; j < nInt; j += gridDim.x * kThreads)
+  {
+    const SegTree t = seg_tree(b, bc::find_segment(b.intOffsets, b.G, j));
+    const uint32_t i = j - t.intBase;
+    role[j] = node_role(t.lr, t.runStarts, t.L, t.nTris, node_depth(t.parent, t.L, i), b.mergeMode, i);
+  }
+}
+
+// Per geometry: its 4-wide node count (role-1 nodes; 1 for a single leaf; 0
+// without triangles), its first node's batch-wide rank, and the exclusive sum
+// of the counts (node4Off), in one block.  out: rootRank[G], count4[G],
+// node4Off[G + 1].
+__global__ void __launch_bounds__(1024) k_seg4_counts(Bvh4Batch b, uint32_t nInt, const uint32_t* __restrict__ rank,
+                                                      const uint32_t* __restrict__ rankTotal, uint32_t* rootRank,
+                                                      uint32_t* count4, uint32_t* node4Off)
+{
+  __shared__ uint32_t s_part[1024];
+  __shared__ uint32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < b.G; base += blockDim.x)
+  {
+    const uint32_t s = base + threadIdx.x;
+    uint32_t c = 0;
+    if (s < b.G)
     {
-      for (int c = 0; c < 3; c++) { slot[k].lo[c] = 0.0f; slot[k].hi[c] = 0.0f; }
-      slot[k].ref = kEmptyRef;
+      const uint32_t L = b.leafOffsets[s + 1] - b.leafOffsets[s];
+      const uint32_t j0 = b.intOffsets[s], j1 = b.intOffsets[s + 1];
+      const uint32_t r0 = j0 < nInt ? rank[j0] : *rankTotal;
+      const uint32_t r1 = j1 < nInt ? rank[j1] : *rankTotal;
+      c = L > 1 ? r1 - r0 : (L == 1 ? 1u : 0u);
+      rootRank[s] = r0;
+      count4[s] = c;
     }
-    if (format == 0)
+    s_part[threadIdx.x] = c;
+    __syncthreads();
+    for (uint32_t o = 1; o < blockDim.x; o <<= 1)
     {
-      Node4F32 o;
-      o.lox = make_float4(slot[0].lo[0], slot[1].lo[0], slot[2].lo[0], slot[3].lo[0]);
-      o.loy = make_float4(slot[0].lo[1], slot[1].lo[1], slot[2].lo[1], slot[3].lo[1]);
-      o.loz = make_float4(slot[0].lo[2], slot[1].lo[2], slot[2].lo[2], slot[3].lo[2]);
-      o.hix = make_float4(slot[0].hi[0], slot[1].hi[0], slot[2].hi[0], slot[3].hi[0]);
-      o.hiy = make_float4(slot[0].hi[1], slot[1].hi[1], slot[2].hi[1], slot[3].hi[1]);
-      o.hiz = make_float4(slot[0].hi[2], slot[1].hi[2], slot[2].hi[2], slot[3].hi[2]);
-      o.ref = make_uint4(slot[0].ref, slot[1].ref, slot[2].ref, slot[3].ref);
-      o.pad = make_uint4(0, 0, 0, 0);
-      reinterpret_cast<Node4F32*>(nodes)[outIdx] = o;
+      const uint32_t y = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0u;
+      __syncthreads();
+      s_part[threadIdx.x] += y;
+      __syncthreads();
     }
-    else if (format == 1)
+    if (s < b.G) node4Off[s] = s_carry + s_part[threadIdx.x] - c;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_carry += s_part[blockDim.x - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) node4Off[b.G] = s_carry;
+}
+
+// Threads j < nInt emit the role-1 internal nodes; threads nInt + s emit the
+// lone-leaf node of geometry s when it has exactly one leaf.
+__global__ void __launch_bounds__(kThreads) k_seg4_emit(Bvh4Batch b, uint32_t nInt, const uint8_t* __restrict__ role,
+                                                        const uint32_t* __restrict__ rank,
+                                                        const uint32_t* __restrict__ rootRank,
+                                                        const uint32_t* __restrict__ node4Off, int format,
+                                                        void* __restrict__ nodes, uint32_t* errorWord)
+{
+  for (uint32_t j = blockIdx.x * kThreads + threadIdx.x; j < nInt + b.G; j += gridDim.x * kThreads)
+  {
+    uint32_t seg, i;
+    if (j < nInt)
     {
-      uint32_t w[12];
-      for (int k = 0; k < 4; k++)
-      {
-        w[0 + k] = h2_bits(__float2half_rd(slot[k].lo[0]), __float2half_rd(slot[k].lo[1]));
-        w[4 + k] = h2_bits(__float2half_rd(slot[k].lo[2]), __float2half_ru(slot[k].hi[0]));
-        w[8 + k] = h2_bits(__float2half_ru(slot[k].hi[1]), __float2half_ru(slot[k].hi[2]));
-      }
-      Node4F16 o;
-      o.a = make_uint4(w[0], w[1], w[2], w[3]);
-      o.b = make_uint4(w[4], w[5], w[6], w[7]);
-      o.c = make_uint4(w[8], w[9], w[10], w[11]);
-      o.ref = make_uint4(slot[0].ref, slot[1].ref, slot[2].ref, slot[3].ref);
-      reinterpret_cast<Node4F16*>(nodes)[outIdx] = o;
+      if (role[j] != 1) continue;
+      seg = bc::find_segment(b.intOffsets, b.G, j);
+      i = j - b.intOffsets[seg];
     }
     else
     {
-      // frame: the union of the slots' boxes; per-axis power-of-two scale
-      float org[3], scale[3];
-      int ex[3];
-      for (int c = 0; c < 3; c++)
-      {
-        float mn = slot[0].lo[c], mx = slot[0].hi[c];
-        for (int k = 1; k < ns; k++)
-        {
-          mn = fminf(mn, slot[k].lo[c]);
-          mx = fmaxf(mx, slot[k].hi[c]);
-        }
-        org[c] = mn;
-        ex[c] = q8_exponent(__fsub_rn(mx, mn));
-        // widen the scale until the frame's top is representable outward
-        for (int guard = 0; guard < 4; guard++)
-        {
-          if (q8_decode(org[c], 255u, q8_scale(ex[c])) >= mx || ex[c] >= 127) break;
-          ex[c]++;
-        }
-        scale[c] = q8_scale(ex[c]);
-      }
-      uint32_t qb[6] = {0, 0, 0, 0, 0, 0};  // lox, loy, loz, hix, hiy, hiz: 4 bytes each (one per slot)
-      for (int k = 0; k < ns; k++)
-        for (int c = 0; c < 3; c++)
-        {
-          bool ok = true;
-          const uint32_t lo = q8_lo(org[c], slot[k].lo[c], scale[c]);
-          const uint32_t hi = q8_hi(org[c], slot[k].hi[c], scale[c], ok);
-          if (!ok) atomicOr(errorWord, kErrLayout);
-          qb[c] |= lo << (8 * k);
-          qb[3 + c] |= hi << (8 * k);
-        }
-      Node4Q8 o;
-      o.frame = make_float4(org[0], org[1], org[2],
-                            __uint_as_float((uint32_t)(ex[0] + 128) | ((uint32_t)(ex[1] + 128) << 8) |
-                                            ((uint32_t)(ex[2] + 128) << 16)));
-      o.q0 = make_uint4(qb[0], qb[1], qb[2], qb[3]);
-      o.q1 = make_uint4(qb[4], qb[5], 0u, 0u);
-      o.ref = make_uint4(slot[0].ref, slot[1].ref, slot[2].ref, slot[3].ref);
-      reinterpret_cast<Node4Q8*>(nodes)[outIdx] = o;
+      seg = j - nInt;
+      if (b.leafOffsets[seg + 1] - b.leafOffsets[seg] != 1u) continue;
+      i = 0;
     }
+    const SegTree t = seg_tree(b, seg);
+    const uint32_t r0 = rootRank[seg];
+    const uint32_t local = t.L == 1u ? 0u : rank[j] - r0;
+    const uint32_t outIdx = node4Off[seg] + local;
+    if (outIdx >= node4Off[seg + 1])
+    {
+      atomicOr(errorWord, kErrLayout);
+      continue;
+    }
+    Slot slot[4];
+    const uint8_t* roleSeg = role + t.intBase;
+    const uint32_t* rankSeg = rank + t.intBase;
+    const int ns = node4_slots(t.lr, t.runStarts, t.L, t.nTris, roleSeg,
+                               [&](uint32_t c) { return rankSeg[c] - r0; }, i, t.tris, slot);
+    write_node4(format, nodes, outIdx, slot, ns, errorWord);
   }
 }
 
@@ -431,7 +581,7 @@ cudaError_t bvh4_plan(const Bvh4Buffers& b, int numSMs, cudaStream_t s)
   const uint32_t g = grid_for(N, numSMs);
   k_depth<<<g, kThreads, 0, s>>>(b.params, b.parent, depth);
   k_roles<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, N, depth, b.mergeMode, role);
-  k_scan_roles<<<(uint32_t)(nTiles ? nTiles : 1), kThreads, 0, s>>>(b.params, role, index, tiles + 4, tiles, total,
+  k_scan_roles<<<(uint32_t)(nTiles ? nTiles : 1), kThreads, 0, s>>>(b.params, 0u, role, index, tiles + 4, tiles, total,
                                                                       &b.params->error);
   return cudaMemcpyAsync(b.hostNodeCount, total, 4, cudaMemcpyDeviceToHost, s);
 }
@@ -445,6 +595,69 @@ cudaError_t bvh4_emit(const Bvh4Buffers& b, int format, void* nodes, uint32_t ma
   uint32_t* index = (uint32_t*)(p + 256 + ((2 * (size_t)N + 255) / 256) * 256);
   k_emit4<<<grid_for(N, numSMs), kThreads, 0, s>>>(b.params, b.lr, b.runStarts, N, role, index, format, nodes,
                                                    maxNodes, b.tris, &b.params->error);
+  return cudaGetLastError();
+}
+
+// Batch scratch: total (256 B), role (nInt B), rank (4 nInt B), per-geometry
+// rootRank, count4, node4Off (4 (3G + 1) B), scan tile status.
+size_t bvh4_batch_scratch_bytes(uint32_t nInt, uint32_t G)
+{
+  const size_t n = nInt ? nInt : 1;
+  const size_t tiles = (n + kScanTile - 1) / kScanTile;
+  return 256 + ((n + 255) / 256) * 256 + ((4 * n + 255) / 256) * 256 + ((4 * (3 * (size_t)G + 1) + 255) / 256) * 256 +
+         4 * (tiles + 8);
+}
+
+namespace
+{
+struct BatchScratch
+{
+  uint32_t *total, *rank, *rootRank, *count4, *node4Off, *tiles;
+  uint8_t* role;
+};
+BatchScratch batch_scratch(void* scratch, uint32_t nInt, uint32_t G)
+{
+  const size_t n = nInt ? nInt : 1;
+  char* p = (char*)scratch;
+  BatchScratch q;
+  q.total = (uint32_t*)p;
+  q.role = (uint8_t*)(p + 256);
+  q.rank = (uint32_t*)(p + 256 + ((n + 255) / 256) * 256);
+  q.rootRank = (uint32_t*)((char*)q.rank + ((4 * n + 255) / 256) * 256);
+  q.count4 = q.rootRank + G;
+  q.node4Off = q.count4 + G;
+  q.tiles = (uint32_t*)((char*)q.rootRank + ((4 * (3 * (size_t)G + 1) + 255) / 256) * 256);
+  return q;
+}
+}  // namespace
+
+cudaError_t bvh4_plan_batch(const Bvh4Batch& b, uint32_t nInt, void* scratch, uint32_t* hostCount4,
+                            uint32_t* hostNode4Off, uint32_t* errorWord, int numSMs, cudaStream_t s)
+{
+  const BatchScratch q = batch_scratch(scratch, nInt, b.G);
+  const size_t nTiles = ((size_t)(nInt ? nInt : 1) + kScanTile - 1) / kScanTile;
+  cudaError_t e = cudaMemsetAsync(q.total, 0, 4, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(q.tiles, 0, 4 * (nTiles + 8), s);
+  if (e != cudaSuccess) return e;
+  if (nInt)
+  {
+    k_seg4_depth_roles<<<grid_for(nInt, numSMs), kThreads, 0, s>>>(b, nInt, q.role);
+    k_scan_roles<<<(uint32_t)nTiles, kThreads, 0, s>>>(nullptr, nInt, q.role, q.rank, q.tiles + 4, q.tiles, q.total,
+                                                       errorWord);
+  }
+  k_seg4_counts<<<1, 1024, 0, s>>>(b, nInt, q.rank, q.total, q.rootRank, q.count4, q.node4Off);
+  e = cudaMemcpyAsync(hostCount4, q.count4, 4 * (size_t)b.G, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(hostNode4Off, q.node4Off, 4 * ((size_t)b.G + 1), cudaMemcpyDeviceToHost, s);
+}
+
+cudaError_t bvh4_emit_batch(const Bvh4Batch& b, uint32_t nInt, void* scratch, int format, void* nodes,
+                            uint32_t* errorWord, int numSMs, cudaStream_t s)
+{
+  const BatchScratch q = batch_scratch(scratch, nInt, b.G);
+  k_seg4_emit<<<grid_for((uint64_t)nInt + b.G, numSMs), kThreads, 0, s>>>(b, nInt, q.role, q.rank, q.rootRank,
+                                                                           q.node4Off, format, nodes, errorWord);
   return cudaGetLastError();
 }
 

@@ -379,63 +379,57 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   const uint32_t* hRec = ho.data() + 3 * (G + 1);
   uint32_t err = ho[4 * ((size_t)G + 1) + 4];
 
-  // 4-wide collapse of every geometry with triangles: plan all, one
-  // synchronisation for the node counts, then emit into one node array
+  // 4-wide collapse of every geometry at once: plan (one launch per stage over
+  // the whole batch), one synchronisation for the node counts, then emit into
+  // one node array
   std::vector<uint32_t> count4(G, 0);
   std::vector<size_t> node4Off(G, 0);
   void* nodes4 = nullptr;
   size_t nodeBytes = 0;
   void* scratch4 = nullptr;
-  std::vector<Bvh4Buffers> b4(G);
   if (s->layout != HRT_LAYOUT_BVH2 && N > 0 && err == 0)
   {
     nodeBytes = (s->layout == HRT_LAYOUT_BVH4_F32) ? sizeof(Node4F32) : sizeof(Node4F16);
-    std::vector<size_t> scrOff(G + 1, 0);
-    for (uint32_t i = 0; i < G; i++)
-      scrOff[i + 1] = scrOff[i] + (ht[i + 1] > ht[i] ? align_up(bvh4_scratch_bytes(ht[i + 1] - ht[i]), 256) : 0);
-    HRT_CUDA(ctx, cudaMallocAsync(&scratch4, scrOff[G] ? scrOff[G] : 256, st));
+    const uint32_t* hInt = ho.data() + (G + 1);
+    const uint32_t nInt = hInt[G];
+    Bvh4Batch q;
+    q.G = G;
+    q.lr = b.lr;
+    q.runStarts = b.runStarts;
+    q.parent = parent;
+    q.tris = b.tris;
+    q.leafOffsets = b.leafOffsets;
+    q.intOffsets = b.intOffsets;
+    q.nodeOffsets = b.nodeOffsets;
+    q.triOffsets = b.triOffsets;
+    q.mergeMode = s->bvh4Merge;
+    HRT_CUDA(ctx, cudaMallocAsync(&scratch4, bvh4_batch_scratch_bytes(nInt, G), st));
     uint32_t* hostCounts = nullptr;
-    HRT_CUDA(ctx, cudaMallocHost((void**)&hostCounts, sizeof(uint32_t) * G));
+    HRT_CUDA(ctx, cudaMallocHost((void**)&hostCounts, sizeof(uint32_t) * (2 * (size_t)G + 1)));
+    cudaError_t pe = bvh4_plan_batch(q, nInt, scratch4, hostCounts, hostCounts + G, b.errorWord, ctx->numSMs, st);
+    if (pe == cudaSuccess) pe = cudaStreamSynchronize(st);
+    if (pe != cudaSuccess)
+    {
+      cudaFreeHost(hostCounts);
+      return cuda_fail(ctx, pe, "bvh4_plan_batch");
+    }
     for (uint32_t i = 0; i < G; i++)
     {
-      hostCounts[i] = 0;
-      const uint32_t Ni = ht[i + 1] - ht[i];
-      if (Ni == 0) continue;
-      Bvh4Buffers& q = b4[i];
-      q.nTris = Ni;
-      q.params = b.params + i;
-      q.lr = b.lr + hNode[i];
-      q.runStarts = b.runStarts + hLeaf[i];
-      q.parent = parent + hNode[i];
-      q.tris = b.tris + ht[i];
-      q.mergeMode = s->bvh4Merge;
-      q.scratch = (char*)scratch4 + scrOff[i];
-      q.hostNodeCount = hostCounts + i;
-      cudaError_t pe = bvh4_plan(q, ctx->numSMs, st);
-      if (pe != cudaSuccess)
-      {
-        cudaFreeHost(hostCounts);
-        return cuda_fail(ctx, pe, "bvh4_plan");
-      }
+      count4[i] = hostCounts[i];
+      node4Off[i] = hostCounts[G + i];
     }
-    cudaError_t se = cudaStreamSynchronize(st);
-    size_t total = 0;
-    for (uint32_t i = 0; i < G; i++)
-    {
-      count4[i] = (ht[i + 1] > ht[i]) ? (hostCounts[i] ? hostCounts[i] : 1u) : 0u;
-      node4Off[i] = total;
-      total += count4[i];
-    }
+    const size_t total = hostCounts[2 * (size_t)G];
     cudaFreeHost(hostCounts);
-    if (se != cudaSuccess) return cuda_fail(ctx, se, "bvh4_plan sync");
     HRT_CUDA(ctx, balloc((char**)&nodes4, nodeBytes * (total ? total : 1), owned));
-    for (uint32_t i = 0; i < G; i++)
-      if (count4[i])
-        HRT_CUDA(ctx, bvh4_emit(b4[i], s->layout - 1, (char*)nodes4 + nodeBytes * node4Off[i], count4[i],
-                                ctx->numSMs, st));
+    HRT_CUDA(ctx, bvh4_emit_batch(q, nInt, scratch4, s->layout - 1, nodes4, b.errorWord, ctx->numSMs, st));
   }
   HRT_CUDA(ctx, cudaEventRecord(e1, st));
-  if (nodes4) HRT_CUDA(ctx, cudaMemcpyAsync(hp.data(), b.params, sizeof(BuildParams) * G, cudaMemcpyDeviceToHost, st));
+  uint32_t collapseErr = 0;
+  if (nodes4)
+  {
+    HRT_CUDA(ctx, cudaMemcpyAsync(hp.data(), b.params, sizeof(BuildParams) * G, cudaMemcpyDeviceToHost, st));
+    HRT_CUDA(ctx, cudaMemcpyAsync(&collapseErr, b.errorWord, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  }
   HRT_CUDA(ctx, cudaFreeAsync(dIdx, st));
   HRT_CUDA(ctx, cudaFreeAsync(keysAlt, st));
   HRT_CUDA(ctx, cudaFreeAsync(valsAlt, st));
@@ -450,6 +444,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  err |= collapseErr;
   for (uint32_t i = 0; i < G; i++) err |= hp[i].error;
   if (err & kErrIndexRange) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "triangle index >= vertex count of its geometry");
   if (err & kErrLeafCount)

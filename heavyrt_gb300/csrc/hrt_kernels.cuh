@@ -131,6 +131,31 @@ cudaError_t bvh4_plan(const Bvh4Buffers& b, int numSMs, cudaStream_t stream);
 cudaError_t bvh4_emit(const Bvh4Buffers& b, int format, void* nodes, uint32_t maxNodes, int numSMs,
                       cudaStream_t stream);
 
+// The collapse of every geometry of a segmented build at once (device arrays
+// as in BatchBuffers; runStarts local to each geometry).  bvh4_plan_batch
+// copies each geometry's 4-wide node count (G words) and node offset in the
+// batch's node array (G + 1 words; the last is the total) to host memory
+// (asynchronously: synchronise before reading); bvh4_emit_batch writes all
+// nodes, geometry s from node node4Off[s] on, numbered from its root.
+struct Bvh4Batch
+{
+  uint32_t         G;
+  const BVHNode32* lr;
+  const uint32_t*  runStarts;
+  const uint32_t*  parent;
+  TriRec*          tris;
+  const uint32_t*  leafOffsets;
+  const uint32_t*  intOffsets;
+  const uint32_t*  nodeOffsets;
+  const uint32_t*  triOffsets;
+  int              mergeMode;
+};
+size_t bvh4_batch_scratch_bytes(uint32_t nInt, uint32_t G);
+cudaError_t bvh4_plan_batch(const Bvh4Batch& b, uint32_t nInt, void* scratch, uint32_t* hostCount4,
+                            uint32_t* hostNode4Off, uint32_t* errorWord, int numSMs, cudaStream_t stream);
+cudaError_t bvh4_emit_batch(const Bvh4Batch& b, uint32_t nInt, void* scratch, int format, void* nodes,
+                            uint32_t* errorWord, int numSMs, cudaStream_t stream);
+
 // ---------------------------------------------------------------- trace.cu
 // One instance of a geometry as the traversal sees it.
 struct InstanceDesc
