@@ -420,11 +420,13 @@ class SceneRT:
         vs = []
         for v in verts_list:
             a = np.asarray(v, dtype=np.float32)
-            a = a.reshape(len(a), -1) if a.size else np.zeros((0, 3), np.float32)
-            p4 = np.ones((len(a), 4), np.float32)
-            p4[:, :3] = a[:, :3]
-            vs.append(p4)
-        v = np.ascontiguousarray(np.concatenate(vs, axis=0))
+            a = a.reshape(len(a), -1) if a.size else np.zeros((0, 4), np.float32)
+            if a.shape[1] != 4:  # the engine reads xyz at a 16-byte stride; w is not used
+                p4 = np.ones((len(a), 4), np.float32)
+                p4[:, :3] = a[:, :3]
+                a = p4
+            vs.append(a)
+        v = np.concatenate(vs, axis=0) if len(vs) > 1 else np.ascontiguousarray(vs[0])
         ids = [np.asarray(i, dtype=np.uint32).reshape(-1) for i in idx_list]
         idx = np.ascontiguousarray(np.concatenate(ids))
         voff = np.zeros(len(vs) + 1, dtype=np.uint64)
