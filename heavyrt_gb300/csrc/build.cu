@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict_
 // written by the thread that released the counter it acquired.
 using bc::atomic_add_acq_rel;
 using bc::atomic_add_acq_rel_cta;
-constexpr uint32_t kRefitSlice = 4 * kThreads;  // leaves per block
+using bc::kRefitSlice;
 
 __global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode32* lr, uint32_t* lrCount,
                                                     const uint32_t* __restrict__ parent, uint32_t* visit,

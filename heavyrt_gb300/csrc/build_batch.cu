@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
                                                          const uint32_t* __restrict__ intOffsets,
                                                          const uint32_t* __restrict__ nodeOffsets, uint32_t G,
                                                          const uint32_t* __restrict__ counts, BVHNode32* __restrict__ lr,
-                                                         uint32_t* __restrict__ parent)
+                                                         uint32_t* __restrict__ parent, uint32_t* __restrict__ rangeEnd)
 {
   const uint32_t Itot = counts[1];
   for (uint32_t j = blockIdx.x * kThreads + threadIdx.x; j < Itot; j += gridDim.x * kThreads)
@@ -266,13 +266,14 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
     const int L = (int)(leafOffsets[s + 1] - leafOffsets[s]);
     const int i = (int)(j - intOffsets[s]);
     uint32_t left, right;
-    int other;  // range end, unused here
+    int other;
     bc::karras_node(compressed + leafOffsets[s], L, i, left, right, other);
     const uint32_t nb = nodeOffsets[s];
     lr[nb + i].leftOffset = left;
     lr[nb + i].escapeIndex = right;
     parent[nb + left] = (uint32_t)i;
     parent[nb + right] = (uint32_t)i;
+    rangeEnd[j] = (uint32_t)other;
   }
 }
 
@@ -282,17 +283,29 @@ __global__ void __launch_bounds__(kThreads) k_seg_refit(const uint32_t* __restri
                                                         const uint32_t* __restrict__ nodeOffsets, uint32_t G,
                                                         const uint32_t* __restrict__ counts, BVHNode32* lr,
                                                         uint32_t* lrCount, const uint32_t* __restrict__ parent,
-                                                        uint32_t* visit, uint32_t* errorWord)
+                                                        uint32_t* visit, const uint32_t* __restrict__ rangeEnd,
+                                                        uint32_t* errorWord)
 {
+  // A block owns the global leaves [lo, hi).  Internal node p of geometry s
+  // (leaf base lb) with range [a, b] lies in the slice when lb + a >= lo and
+  // lb + b < hi; such nodes finish with shared-memory counters indexed by
+  // lb + p (unique across geometries, inside the slice), the others with the
+  // device-wide counters, as in the single-geometry refit.
+  __shared__ uint32_t s_visit[bc::kRefitSlice];
   const uint32_t Ltot = counts[0];
-  for (uint32_t g = blockIdx.x * kThreads + threadIdx.x; g < Ltot; g += gridDim.x * kThreads)
+  const uint32_t lo = blockIdx.x * bc::kRefitSlice;
+  if (lo >= Ltot) return;
+  const uint32_t hi = min(lo + bc::kRefitSlice, Ltot);
+  for (uint32_t k = threadIdx.x; k < bc::kRefitSlice; k += kThreads) s_visit[k] = 0u;
+  __syncthreads();
+  for (uint32_t g = lo + threadIdx.x; g < hi; g += kThreads)
   {
     const uint32_t s = find_segment(leafOffsets, G, g);
-    const uint32_t L = leafOffsets[s + 1] - leafOffsets[s];
+    const uint32_t lb = leafOffsets[s];
+    const uint32_t L = leafOffsets[s + 1] - lb;
     const uint32_t nb = nodeOffsets[s], ib = intOffsets[s];
-    uint32_t node = L - 1 + (g - leafOffsets[s]);
-    // no fences: the acquire-release add on the parent's counter publishes this
-    // thread's writes to the sibling's thread that finishes the parent
+    uint32_t node = L - 1 + (g - lb);
+    bool inSlice = true;
     while (node != 0)
     {
       const uint32_t p = parent[nb + node];
@@ -301,13 +314,41 @@ __global__ void __launch_bounds__(kThreads) k_seg_refit(const uint32_t* __restri
         atomicOr(errorWord, kErrLayout);
         break;
       }
-      if (bc::atomic_add_acq_rel(&visit[ib + p], 1u) == 0u) break;
-      const uint32_t l = __ldcg(&lr[nb + p].leftOffset), r = __ldcg(&lr[nb + p].escapeIndex);
+      if (inSlice)
+      {
+        const uint32_t j = rangeEnd[ib + p];
+        inSlice = lb + (p < j ? p : j) >= lo && lb + (p > j ? p : j) < hi;
+      }
+      uint32_t l, r;
       float4 alo, ahi, blo, bhi;
-      bc::load_node_cg(lr + nb + l, alo, ahi);
-      bc::load_node_cg(lr + nb + r, blo, bhi);
+      uint32_t cl, cr;
+      if (inSlice)
+      {
+        if (bc::atomic_add_acq_rel_cta(&s_visit[lb + p - lo], 1u) == 0u) break;
+        if (p == 0u) visit[ib] = 2u;  // the root finished inside the slice (k_seg_records checks the counter)
+        l = lr[nb + p].leftOffset;
+        r = lr[nb + p].escapeIndex;
+        const float4* a = reinterpret_cast<const float4*>(lr + nb + l);
+        const float4* b = reinterpret_cast<const float4*>(lr + nb + r);
+        alo = a[0];
+        ahi = a[1];
+        blo = b[0];
+        bhi = b[1];
+        cl = lrCount[nb + l];
+        cr = lrCount[nb + r];
+      }
+      else
+      {
+        if (bc::atomic_add_acq_rel(&visit[ib + p], 1u) == 0u) break;
+        l = __ldcg(&lr[nb + p].leftOffset);
+        r = __ldcg(&lr[nb + p].escapeIndex);
+        bc::load_node_cg(lr + nb + l, alo, ahi);
+        bc::load_node_cg(lr + nb + r, blo, bhi);
+        cl = __ldcg(&lrCount[nb + l]);
+        cr = __ldcg(&lrCount[nb + r]);
+      }
       bc::store_parent(lr + nb + p, alo, ahi, blo, bhi, l, r);
-      lrCount[nb + p] = __ldcg(&lrCount[nb + l]) + __ldcg(&lrCount[nb + r]) + 2u;
+      lrCount[nb + p] = cl + cr + 2u;
       node = p;
     }
   }
@@ -419,9 +460,10 @@ cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t s)
                                       b.recOffsets, G, b.counts, b.vals, b.runStarts, b.lr, b.lrCount, b.tris,
                                       b.sortedIdx, b.recs, b.errorWord);
   k_seg_karras<<<g, kThreads, 0, s>>>(b.compressed, b.leafOffsets, b.intOffsets, b.nodeOffsets, G, b.counts, b.lr,
-                                      b.parent);
-  k_seg_refit<<<g, kThreads, 0, s>>>(b.leafOffsets, b.intOffsets, b.nodeOffsets, G, b.counts, b.lr, b.lrCount, b.parent,
-                                     b.visit, b.errorWord);
+                                      b.parent, b.visit + N);
+  k_seg_refit<<<(N + bc::kRefitSlice - 1) / bc::kRefitSlice, kThreads, 0, s>>>(
+      b.leafOffsets, b.intOffsets, b.nodeOffsets, G, b.counts, b.lr, b.lrCount, b.parent, b.visit, b.visit + N,
+      b.errorWord);
   k_seg_records<<<g, kThreads, 0, s>>>(b.triOffsets, b.leafOffsets, b.intOffsets, b.nodeOffsets, b.recOffsets, G,
                                        b.counts, b.lr, b.runStarts, b.visit, b.recs, b.errorWord);
   k_seg_localize<<<g, kThreads, 0, s>>>(b.triOffsets, b.leafOffsets, G, N, b.counts, b.runStarts, b.vals);

@@ -140,6 +140,10 @@ __device__ __forceinline__ void karras_node(const uint32_t* __restrict__ codes, 
   other = j;  // the node's leaf range is [min(i, j), max(i, j)]
 }
 
+// Leaves per block of the bottom-up refit: the nodes whose leaf range lies in
+// a block's slice finish with counters in shared memory.
+constexpr uint32_t kRefitSlice = 1024;
+
 __device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v)
 {
   uint32_t old;

@@ -354,7 +354,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   HRT_CUDA(ctx, cudaMallocAsync((void**)&keysAlt, sizeof(uint32_t) * (N ? N : 1), st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&valsAlt, sizeof(uint32_t) * (N ? N : 1), st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&parent, sizeof(uint32_t) * 2 * (N ? N : 1), st));
-  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * (N ? N : 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&visit, sizeof(uint32_t) * 2 * (N ? N : 1), st));
   HRT_CUDA(ctx, cudaMallocAsync(&scratch, build_batch_scratch_bytes((uint32_t)N, G), st));
   b.keysAlt = keysAlt;
   b.valsAlt = valsAlt;

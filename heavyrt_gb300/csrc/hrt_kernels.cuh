@@ -92,7 +92,7 @@ struct BatchBuffers
   BVHNode32* lr;                // 2*nTris
   uint32_t*  lrCount;           // 2*nTris
   uint32_t*  parent;            // 2*nTris
-  uint32_t*  visit;             // nTris
+  uint32_t*  visit;             // 2*nTris: refit counters, then each internal node's range end
   PairRec*   recs;              // nTris
   TriRec*    tris;              // nTris; e1.w = triangle id local to the geometry
   uint32_t*  sortedIdx;         // 3*nTris, local vertex ids
