@@ -98,6 +98,51 @@ def test_results_same_alone_and_in_the_mix(native):
     srv.close()
 
 
+def test_page_locked_requests_are_traced_in_place(native):
+    """Requests whose rays (and any-hit flags) sit in page-locked memory: a
+    request batched alone is traced from them in place; results equal the
+    same requests from pageable memory, alone and mixed into batches."""
+    from heavyrt_gb300 import PinnedBuffer
+    from heavyrt_gb300 import engine as E
+
+    scenes = _scenes()
+    srv = E.Server(slot_rays=1 << 20, slots=2)
+    ids = [srv.add_scene(v, idx, evictable=False) for v, idx in scenes]
+    assert all(srv.scene_state(i, timeout=120) == E.SCENE_READY for i in ids)
+    reqs = _requests(scenes, 24, 29)
+    want = []
+    for s, kind, rays in reqs:
+        out = _out(kind, len(rays))
+        assert srv.wait(srv.submit_array(ids[s], kind, rays, out))[0] == 0
+        want.append(out)
+    bufs = []
+    for s, kind, rays in reqs:
+        pr, po = PinnedBuffer(rays.nbytes), PinnedBuffer(_out(kind, len(rays)).nbytes)
+        pr.array(np.float32, rays.size)[:] = rays.reshape(-1)
+        bufs.append((pr, po))
+    # one at a time (each batched alone: read in place), then all at once (batched together)
+    for rounds in range(2):
+        tickets = []
+        for j, (s, kind, rays) in enumerate(reqs):
+            pr, po = bufs[j]
+            po.array(np.uint8)[:] = 0xAB
+            t = srv.submit(ids[s], kind, pr.ptr, len(rays), po.ptr)
+            if rounds == 0:
+                st, info = srv.wait(t)
+                assert st == 0 and info["batchRequests"] == 1
+            else:
+                tickets.append(t)
+        for t in tickets:
+            assert srv.wait(t)[0] == 0
+        for j, (s, kind, rays) in enumerate(reqs):
+            got = bufs[j][1].array(np.uint32 if kind == 0 else np.uint8)
+            np.testing.assert_array_equal(got.reshape(want[j].shape), want[j], err_msg=f"round {rounds} request {j}")
+    for pr, po in bufs:
+        pr.free()
+        po.free()
+    srv.close()
+
+
 def test_upload_on_arrival(native):
     from heavyrt_gb300 import engine as E
     from heavyrt_gb300 import workload as wl
