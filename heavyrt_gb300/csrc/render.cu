@@ -556,14 +556,14 @@ int ensure_pixels(hrt_frame* f, uint64_t n)
   return HRT_OK;
 }
 
-// Where the kernels write a frame's colours: device-accessible memory
-// (device, managed, pinned host) directly; pageable host memory through the
-// frame's own buffer and one copy at the end of the frame.
+// Where the kernels write a frame's colours: device or managed memory
+// directly; host memory (page-locked or not) through the frame's own buffer
+// and one copy at the end of the frame.
 int color_target(hrt_frame* f, uint32_t* colors, uint64_t n, uint32_t** target)
 {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, colors) == cudaSuccess &&
-      (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost))
+      (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
   {
     *target = colors;
     return HRT_OK;

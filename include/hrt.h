@@ -413,9 +413,8 @@ int hrt_gen_ao_rays(hrt_scene* scene, uint64_t seed, const float* eyeRays, const
  * for bit to the renderers' own kernels run on the same hits.  A frame object
  * owns its buffers (grown on demand) and is used by one thread at a time.
  * Colours: width * height uint32 RGBA, row-major pixels (x, y at
- * y * width + x), in device-accessible memory (written by the kernels) or in
- * pageable host memory (copied there at the end of the frame, which then
- * synchronises `stream`).  Rays are traced in EyeRayCaster's packed order
+ * y * width + x), in device memory (written by the kernels) or in host memory
+ * (copied there at the end of the frame, which then synchronises `stream`).  Rays are traced in EyeRayCaster's packed order
  * (kernel_PackXY, eye_ray.cpp:106-134: 4x4 blocks in 2x2 super-blocks) when
  * both sides are multiples of 8, row by row otherwise; the images are the same. */
 typedef struct hrt_frame hrt_frame;

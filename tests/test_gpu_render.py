@@ -59,7 +59,7 @@ def test_rtao_frame_matches_reference_fixture(native):
     visibility and colours equal the reference RTAO kernels bit for bit."""
     import torch
 
-    from heavyrt_gb300 import Frame, rtao_qmc_tile
+    from heavyrt_gb300 import Frame, PinnedBuffer, rtao_qmc_tile
 
     z = _fixture()
     s, g = _scene(z["verts"], z["idx"])
@@ -70,6 +70,12 @@ def test_rtao_frame_matches_reference_fixture(native):
         f.set_ao_tile(rtao_qmc_tile(c["rays_per_pixel"]), c["rays_per_pixel"])
         colors = torch.empty(c["width"] * c["height"], dtype=torch.int32, device="cuda")
         o = _render_rtao(f, s, c, colors)
+        # the same frame into page-locked host memory
+        pin = PinnedBuffer(4 * c["width"] * c["height"])
+        f.render_rtao(s, c["proj_inv"], c["world_view_inv"], c["width"], c["height"], pin.ptr, c["z_near"],
+                      c["z_far"], c["radius"], c["power"], c["norm_matrix"][None])
+        np.testing.assert_array_equal(pin.array(np.uint32), z[f"{k}_colors"])
+        pin.free()
         hit = z[f"{k}_positions"][:, 1] < 1e7
         np.testing.assert_array_equal(o["positions"].view(np.uint32), z[f"{k}_positions"].view(np.uint32))
         np.testing.assert_array_equal(np.sort(o["ao_pixel"]), np.nonzero(hit)[0])
@@ -99,6 +105,16 @@ def test_eye_frame_matches_reference_fixture(native):
     f.render_eye(s, c["proj_inv"], c["world_view_inv"], c["width"], c["height"], colors.data_ptr())
     torch.cuda.synchronize()
     np.testing.assert_array_equal(colors.cpu().numpy().view(np.uint32), z["a_eye_colors"])
+    # colours into page-locked and into pageable host memory
+    from heavyrt_gb300 import PinnedBuffer
+
+    pin = PinnedBuffer(4 * c["width"] * c["height"])
+    f.render_eye(s, c["proj_inv"], c["world_view_inv"], c["width"], c["height"], pin.ptr)
+    np.testing.assert_array_equal(pin.array(np.uint32), z["a_eye_colors"])
+    host = np.zeros(c["width"] * c["height"], np.uint32)
+    f.render_eye(s, c["proj_inv"], c["world_view_inv"], c["width"], c["height"], host.ctypes.data)
+    np.testing.assert_array_equal(host, z["a_eye_colors"])
+    pin.free()
     # a size that is no multiple of 8 (row order) against the restatement
     b = orc.OracleBVH(z["verts"], z["idx"])
     colors = torch.empty(45 * 23, dtype=torch.int32, device="cuda")
