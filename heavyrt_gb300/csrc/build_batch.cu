@@ -22,12 +22,23 @@ namespace
 constexpr int kThreads = 256;
 using bc::find_segment;
 
-// Scene box and Morton scale of each geometry: one block per geometry.
-__global__ void __launch_bounds__(kThreads) k_seg_box(const float4* __restrict__ v,
-                                                      const uint32_t* __restrict__ vertOffsets, BuildParams* params)
+// Scene box and Morton scale of each geometry, in two passes: every geometry's
+// vertices in chunks of kBoxChunk, one block per chunk (geometry s owns chunks
+// [chunkOffsets[s], chunkOffsets[s + 1])), then the chunks of each geometry
+// combined in order.  Min / max are exact, so the box is the reference's
+// (core/builders/lbvh.cpp:228-239; init +-1e10, :53).
+constexpr uint32_t kBoxChunk = kBatchBoxChunk;
+
+__global__ void __launch_bounds__(kThreads) k_seg_box_partial(const float4* __restrict__ v,
+                                                              const uint32_t* __restrict__ vertOffsets,
+                                                              const uint32_t* __restrict__ chunkOffsets, uint32_t G,
+                                                              float4* __restrict__ partial)
 {
-  const uint32_t s = blockIdx.x;
-  const uint32_t b = vertOffsets[s], e = vertOffsets[s + 1];
+  const uint32_t k = blockIdx.x;
+  const uint32_t s = find_segment(chunkOffsets, G, k);
+  const uint32_t c = k - chunkOffsets[s];
+  const uint32_t b = vertOffsets[s] + c * kBoxChunk;
+  const uint32_t e = min(b + kBoxChunk, vertOffsets[s + 1]);
   float mn[4] = {1e10f, 1e10f, 1e10f, 1e10f}, mx[4] = {-1e10f, -1e10f, -1e10f, -1e10f};
   for (uint32_t i = b + threadIdx.x; i < e; i += kThreads)
   {
@@ -38,20 +49,37 @@ __global__ void __launch_bounds__(kThreads) k_seg_box(const float4* __restrict__
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-    for (int c = 0; c < 4; c++)
+    for (int q = 0; q < 4; q++)
     {
-      mn[c] = lm_min(mn[c], __shfl_down_sync(0xFFFFFFFFu, mn[c], o));
-      mx[c] = lm_max(mx[c], __shfl_down_sync(0xFFFFFFFFu, mx[c], o));
+      mn[q] = lm_min(mn[q], __shfl_down_sync(0xFFFFFFFFu, mn[q], o));
+      mx[q] = lm_max(mx[q], __shfl_down_sync(0xFFFFFFFFu, mx[q], o));
     }
   __shared__ float smn[kThreads / 32][4], smx[kThreads / 32][4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
-    for (int c = 0; c < 4; c++) { smn[warp][c] = mn[c]; smx[warp][c] = mx[c]; }
+    for (int q = 0; q < 4; q++) { smn[warp][q] = mn[q]; smx[warp][q] = mx[q]; }
   __syncthreads();
   if (threadIdx.x == 0)
   {
     for (int w = 1; w < kThreads / 32; w++)
-      for (int c = 0; c < 4; c++) { mn[c] = lm_min(mn[c], smn[w][c]); mx[c] = lm_max(mx[c], smx[w][c]); }
+      for (int q = 0; q < 4; q++) { mn[q] = lm_min(mn[q], smn[w][q]); mx[q] = lm_max(mx[q], smx[w][q]); }
+    partial[2 * k] = make_float4(mn[0], mn[1], mn[2], mn[3]);
+    partial[2 * k + 1] = make_float4(mx[0], mx[1], mx[2], mx[3]);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_seg_box_final(const uint32_t* __restrict__ chunkOffsets, uint32_t G,
+                                                            const float4* __restrict__ partial, BuildParams* params)
+{
+  for (uint32_t s = blockIdx.x * kThreads + threadIdx.x; s < G; s += gridDim.x * kThreads)
+  {
+    float mn[4] = {1e10f, 1e10f, 1e10f, 1e10f}, mx[4] = {-1e10f, -1e10f, -1e10f, -1e10f};
+    for (uint32_t k = chunkOffsets[s]; k < chunkOffsets[s + 1]; k++)
+    {
+      const float4 a = partial[2 * k], b = partial[2 * k + 1];
+      mn[0] = lm_min(mn[0], a.x); mn[1] = lm_min(mn[1], a.y); mn[2] = lm_min(mn[2], a.z); mn[3] = lm_min(mn[3], a.w);
+      mx[0] = lm_max(mx[0], b.x); mx[1] = lm_max(mx[1], b.y); mx[2] = lm_max(mx[2], b.z); mx[3] = lm_max(mx[3], b.w);
+    }
     bc::zindex_scale(mn, mx, &params[s]);
     params[s].nLeaves = 0;
     params[s].error = 0;
@@ -435,7 +463,9 @@ cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t s)
   uint32_t* scanStatus = scanCounter + 4;
   void* sortScratch = scratch + scanBytes;
 
-  k_seg_box<<<G, kThreads, 0, s>>>(b.verts, b.vertOffsets, b.params);
+  if (b.nBoxChunks) k_seg_box_partial<<<b.nBoxChunks, kThreads, 0, s>>>(b.verts, b.vertOffsets, b.boxChunkOffsets, G,
+                                                                         b.boxPartial);
+  k_seg_box_final<<<(G + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.boxChunkOffsets, G, b.boxPartial, b.params);
   k_seg_morton<<<(N + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.verts, b.idx, b.vertOffsets, b.triOffsets, G, N,
                                                                    b.params, b.keys, b.vals, b.errorWord);
   cudaError_t e = cudaMemcpyAsync(b.keysUnsorted, b.keys, sizeof(uint32_t) * N, cudaMemcpyDeviceToDevice, s);

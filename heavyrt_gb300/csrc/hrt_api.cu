@@ -325,6 +325,17 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   b.triOffsets = dTOff;
   b.G = G;
   b.nTris = (uint32_t)N;
+  // scene-box chunks of each geometry's vertices
+  std::vector<uint32_t> hChunk(G + 1, 0);
+  for (uint32_t i = 0; i < G; i++) hChunk[i + 1] = hChunk[i] + (hv[i + 1] - hv[i] + kBatchBoxChunk - 1) / kBatchBoxChunk;
+  uint32_t* dChunk = nullptr;
+  float4* boxPartial = nullptr;
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&dChunk, sizeof(uint32_t) * (G + 1), st));
+  HRT_CUDA(ctx, cudaMallocAsync((void**)&boxPartial, 2 * sizeof(float4) * (hChunk[G] ? hChunk[G] : 1), st));
+  HRT_CUDA(ctx, cudaMemcpyAsync(dChunk, hChunk.data(), sizeof(uint32_t) * (G + 1), cudaMemcpyHostToDevice, st));
+  b.boxChunkOffsets = dChunk;
+  b.nBoxChunks = hChunk[G];
+  b.boxPartial = boxPartial;
   uint32_t *keysAlt = nullptr, *valsAlt = nullptr, *parent = nullptr, *visit = nullptr;
   void* scratch = nullptr;
   HRT_CUDA(ctx, balloc(&b.keys, N, owned));
@@ -438,6 +449,8 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   HRT_CUDA(ctx, cudaFreeAsync(scratch, st));
   HRT_CUDA(ctx, cudaFreeAsync(dVOff, st));
   HRT_CUDA(ctx, cudaFreeAsync(dTOff, st));
+  HRT_CUDA(ctx, cudaFreeAsync(dChunk, st));
+  HRT_CUDA(ctx, cudaFreeAsync(boxPartial, st));
   if (scratch4) HRT_CUDA(ctx, cudaFreeAsync(scratch4, st));
   HRT_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.0f;

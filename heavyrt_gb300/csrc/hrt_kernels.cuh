@@ -104,7 +104,13 @@ struct BatchBuffers
   uint32_t*  counts;            // 4
   uint32_t*  errorWord;         // device word shared by the batch
   void*      scratch;           // build_batch_scratch_bytes(nTris, G)
+  // scene boxes: geometry s's vertices in chunks [boxChunkOffsets[s], boxChunkOffsets[s+1])
+  // of kBatchBoxChunk vertices, one (min, max) float4 pair per chunk in boxPartial
+  const uint32_t* boxChunkOffsets;  // G+1 (device)
+  uint32_t        nBoxChunks;
+  float4*         boxPartial;       // 2 * nBoxChunks
 };
+constexpr uint32_t kBatchBoxChunk = 8192;
 size_t build_batch_scratch_bytes(uint32_t nTris, uint32_t G);
 cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t stream);
 
