@@ -246,6 +246,25 @@ def cpu_trace_rate(o, eye, ao, seconds: float, threads: int = 0):
                                f"(every {step}th)) of the frame, {dt:.1f} s"
 
 
+def host_cpu() -> str:
+    """The host CPU's model name and logical core count (for the CPU-baseline record)."""
+    name = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    name = line.split(":", 1)[1].strip()
+                    break
+                if key == "cpu part" and not name and ":" in line:
+                    name = "Arm CPU part " + line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return f"{name or platform.processor() or platform.machine()} ({os.cpu_count()} logical cores)"
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -282,7 +301,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w.name, "tris": int(w.idx.size // 3), "eye_rays": int(n_eye), "ao_rays": int(n_ao),
                    "parallelism": "cpu", "l2": "n/a (host)"},
-        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": int(used), "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": int(used), "kind": "port", "sample": sample,
+                         "cpu": host_cpu()},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -1178,7 +1198,7 @@ def run_engine(args):
         o = orc.OracleBVH(w.verts, w.idx)
         rate, used, sample = cpu_trace_rate(o, w.eye_rays, ao, args.cpu_seconds)
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": UNIT, "cores": int(used), "kind": "port",
-                                "sample": sample}
+                                "sample": sample, "cpu": host_cpu()}
         # the frame's any-hit flags from the e2e leg agree with the oracle on the sample rows
         step_ao = max(1, n_ao // 20000)
         want = o.trace(ao[::step_ao], any_hit=True)
