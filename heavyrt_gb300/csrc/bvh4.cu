@@ -70,6 +70,8 @@ __device__ __forceinline__ uint8_t node_role(const BVHNode32* __restrict__ lr, c
   bool merge;
   if (mergeMode == 0)
     merge = lr[i].leftOffset + 1u >= L && lr[i].escapeIndex + 1u >= L;
+  else if (mergeMode == 1)
+    merge = false;  // an internal node holds two leaves at least, so two triangles
   else
   {
     uint32_t st, en;
