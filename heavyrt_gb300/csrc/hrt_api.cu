@@ -783,6 +783,7 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
     a.tlasRecs = s->tlas.recs;
     a.tlasTris = s->tlas.tris;
   }
+  if (s->single && !q.rayOffsets) a.one = &s->singleDesc;
   cudaError_t e = trace(a, kind, counting, s->layout, s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
@@ -1111,6 +1112,8 @@ int hrt_commit_scene(hrt_scene* s, int quality)
   if (s->dInst) cudaFree(s->dInst);
   s->dInst = nullptr;
   s->nInstDev = (uint32_t)d.size();
+  s->single = d.size() == 1 && d[0].identity && d[0].valid && s->tlas.nTris == 0;
+  if (s->single) s->singleDesc = d[0];
   if (!d.empty())
   {
     HRT_CUDA(ctx, cudaMalloc((void**)&s->dInst, sizeof(InstanceDesc) * d.size()));

@@ -80,6 +80,10 @@ struct hrt_scene
   Geom                  tlas;           // instance tree of the committed scene (nTris = 0: none)
   InstanceDesc*         dInst = nullptr;
   uint32_t              nInstDev = 0;
+  // the committed scene is one valid instance under the identity transform
+  // (no instance tree): its descriptor, for the single-instance kernel
+  bool                  single = false;
+  InstanceDesc          singleDesc{};
   uint32_t*             dError = nullptr;
   unsigned long long*   dCounters = nullptr;
   // work counters of the persistent traversal pool: one slot per launch, taken

@@ -195,6 +195,9 @@ struct TraceArgs
   // its triangle records' e1.w hold instance ids
   const PairRec*      tlasRecs = nullptr;
   const TriRec*       tlasTris = nullptr;
+  // host copy of the descriptor when the scene is one valid instance under the
+  // identity transform (the single-instance kernel), else null
+  const InstanceDesc* one = nullptr;
 };
 
 // Launch shape of the traversal (tuned per workload).

@@ -275,7 +275,8 @@ constexpr uint32_t kStepBudget = 1u << 24;
 
 // The first lane to run out of budget records its state after the error word:
 // [1] = 1 (taken), [2] ray, [3] current ref, [4] stack depth.
-__device__ __forceinline__ bool out_of_budget(Lane& L, uint32_t* errorWord)
+template <typename LaneT>
+__device__ __forceinline__ bool out_of_budget(LaneT& L, uint32_t* errorWord)
 {
   if (L.budget-- != 0u) return false;
   atomicOr(errorWord, kErrStepBudget);
@@ -329,8 +330,8 @@ template <int LAYOUT> struct EndBit
 // otherwise, -1 when the stack bound would be exceeded (reported).
 // One child pair of a binary tree: BVH2TraverseC32's decisions
 // (core/BVH2CommonRT.cpp:88-113).
-template <bool COUNT, int THREADS, int DEPTH>
-__device__ __forceinline__ int visit_pair(Lane& L, const PairRec* __restrict__ recs, uint32_t* __restrict__ stack,
+template <bool COUNT, int THREADS, int DEPTH, typename LaneT>
+__device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ recs, uint32_t* __restrict__ stack,
                                           uint64_t& nPairs, uint32_t* errorWord)
 {
   const float4* p = reinterpret_cast<const float4*>(recs + L.cur);
@@ -361,8 +362,8 @@ __device__ __forceinline__ int visit_pair(Lane& L, const PairRec* __restrict__ r
   return 0;
 }
 
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS, int DEPTH>
-__device__ __forceinline__ int visit_node(Lane& L, uint32_t* __restrict__ stack, uint64_t& nPairs, uint32_t* errorWord)
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, int DEPTH, typename LaneT>
+__device__ __forceinline__ int visit_node(LaneT& L, uint32_t* __restrict__ stack, uint64_t& nPairs, uint32_t* errorWord)
 {
   if constexpr (LAYOUT != 0)
   {
@@ -700,6 +701,172 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
   flush_counters<COUNT>(nPairs, nTris, counters);
 }
 
+// ------------------------------------------------ one instance, no transform
+// A scene of one geometry under the identity transform (no instance tree, no
+// segments) needs none of the instance state: the ray is used as given, the
+// node and triangle arrays are kernel parameters, and the ray leaves after its
+// last pop.  The lane keeps less state, so the kernel holds fewer registers
+// and more warps fit on an SM; each ray's decisions are those of the general
+// kernel.
+struct Lane1
+{
+  Ray           r;
+  Hit           h;
+  uint32_t      ray;     // ray index or kNoRay
+  uint32_t      cur;     // current node / leaf reference
+  int           top;     // stack depth
+  uint32_t      budget;  // steps left for this ray
+  const void*   nodes;   // the geometry's binary records or 4-wide nodes
+  const TriRec* tris;
+};
+
+__device__ __forceinline__ void start_ray_one(Lane1& L, uint32_t i, const float4* __restrict__ rays)
+{
+  const float4 po = __ldg(rays + 2 * (size_t)i + 0);
+  const float4 di = __ldg(rays + 2 * (size_t)i + 1);
+  L.ray = i;
+  L.r.ox = po.x; L.r.oy = po.y; L.r.oz = po.z; L.r.tNear = po.w;
+  L.r.dx = di.x; L.r.dy = di.y; L.r.dz = di.z;
+  L.r.ix = safe_inv(di.x);
+  L.r.iy = safe_inv(di.y);
+  L.r.iz = safe_inv(di.z);
+  L.h.t = di.w;
+  L.h.u = L.h.v = 0.0f;
+  L.h.prim = L.h.inst = 0xFFFFFFFFu;
+  L.cur = 0;
+  L.top = 0;
+  L.budget = kStepBudget;
+}
+
+// One step of the single-instance kernel; true when the ray is finished.
+template <int LAYOUT, bool ANY, int THREADS>
+__device__ __forceinline__ bool step_one(Lane1& L, uint32_t* __restrict__ stack, uint32_t* errorWord)
+{
+  constexpr int DEPTH = StackDepth<LAYOUT, false>::value;
+  uint64_t none = 0;
+  if ((L.cur & kLeafBit) == 0u)
+  {
+    const int r = visit_node<LAYOUT, ANY, false, THREADS, DEPTH>(L, stack, none, errorWord);
+    if (r < 0) return true;
+    if (r == 0) return false;
+  }
+  else if (L.cur != kEmptyRef &&
+           leaf_test<ANY, false, EndBit<LAYOUT>::value>(L.tris, L.cur & ~kLeafBit, L.r, L.h, 0u, none))
+    return true;  // any-hit found
+  if (L.top == 0) return true;
+  L.top--;
+  L.cur = stack[L.top * THREADS];
+  return false;
+}
+
+template <bool ANY>
+__device__ __forceinline__ void write_result_one(const Lane1& L, uint32_t instId, uint32_t geomId, void* out)
+{
+  const bool hit = L.h.prim != 0xFFFFFFFFu;
+  if (ANY)
+    reinterpret_cast<uint8_t*>(out)[L.ray] = hit ? 1 : 0;
+  else
+  {
+    float4* o = reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray);
+    o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(hit ? instId : 0xFFFFFFFFu),
+                       __uint_as_float(hit ? geomId : 0xFFFFFFFFu));
+    o[1] = make_float4(L.h.u, L.h.v, 0.0f, 0.0f);
+  }
+}
+
+// Persistent warp pool over one instance (the refill rule of k_trace_pool).
+template <int LAYOUT, bool ANY, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict__ rays, uint32_t n,
+                                                       const void* __restrict__ nodes, const TriRec* __restrict__ tris,
+                                                       uint32_t instId, uint32_t geomId, void* out,
+                                                       uint32_t* errorWord, unsigned int* rayCounter, int steps,
+                                                       int refill)
+{
+  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT>::value * THREADS entries
+  uint32_t* stack = s_stack + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t ltMask = (1u << lane) - 1u;
+  Lane1 L;
+  L.ray = kNoRay;
+  L.nodes = nodes;
+  L.tris = tris;
+  bool exhausted = false;
+  while (true)
+  {
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, L.ray == kNoRay);
+    if (exhausted && idle == 0xFFFFFFFFu) break;
+    if (!exhausted && (__popc(idle) >= refill || idle == 0xFFFFFFFFu))
+    {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(rayCounter, (unsigned int)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+      if (L.ray == kNoRay)
+      {
+        const uint32_t i = base + __popc(idle & ltMask);
+        if (i < n) start_ray_one(L, i, rays);
+      }
+    }
+    if (L.ray != kNoRay)
+    {
+      for (int s = 0; s < steps; s++)
+      {
+        if (out_of_budget(L, errorWord) || step_one<LAYOUT, ANY, THREADS>(L, stack, errorWord))
+        {
+          write_result_one<ANY>(L, instId, geomId, out);
+          L.ray = kNoRay;
+          break;
+        }
+      }
+    }
+  }
+}
+
+template <int LAYOUT, bool ANY, int THREADS>
+cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  const uint32_t n = (uint32_t)a.n;
+  constexpr size_t smem = sizeof(uint32_t) * StackDepth<LAYOUT, false>::value * THREADS;
+  if (smem > 48 * 1024)
+  {
+    cudaError_t e = cudaFuncSetAttribute(k_trace_one<LAYOUT, ANY, THREADS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int perSM = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_one<LAYOUT, ANY, THREADS>, THREADS,
+                                                                smem);
+  if (e != cudaSuccess) return e;
+  if (perSM < 1) perSM = 1;
+  uint64_t blocks = (uint64_t)numSMs * perSM;
+  const uint64_t need = ((uint64_t)n + THREADS - 1) / THREADS;
+  if (blocks > need) blocks = need;
+  e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  const InstanceDesc& d = *a.one;
+  const void* nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
+  k_trace_one<LAYOUT, ANY, THREADS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+      a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill,
+      c.refillLanes);
+  return cudaGetLastError();
+}
+
+template <int LAYOUT>
+cudaError_t trace_one(const TraceArgs& a, int kind, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  switch (c.threadsPerBlock)
+  {
+    case 64:
+      return kind == 0 ? launch_one<LAYOUT, false, 64>(a, c, numSMs, s) : launch_one<LAYOUT, true, 64>(a, c, numSMs, s);
+    case 256:
+      return kind == 0 ? launch_one<LAYOUT, false, 256>(a, c, numSMs, s)
+                       : launch_one<LAYOUT, true, 256>(a, c, numSMs, s);
+    default:
+      return kind == 0 ? launch_one<LAYOUT, false, 128>(a, c, numSMs, s)
+                       : launch_one<LAYOUT, true, 128>(a, c, numSMs, s);
+  }
+}
+
 template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
 cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
@@ -763,10 +930,13 @@ cudaError_t trace_tlas(const TraceArgs& a, int kind, int counting, const TraceCo
 
 // Counting runs use the one-thread-per-ray grid at 128 threads: the counts do
 // not depend on the schedule.  A scene with an instance tree uses the
-// two-level kernels, except in segmented queries (one instance per ray).
+// two-level kernels, except in segmented queries (one instance per ray).  A
+// scene of one untransformed instance uses the single-instance pool.
 template <int LAYOUT>
 cudaError_t trace_layout(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
+  if (a.one != nullptr && !counting && c.persistent && a.rayOffsets == nullptr && a.tlasRecs == nullptr)
+    return trace_one<LAYOUT>(a, kind, c, numSMs, s);
   if (a.tlasRecs != nullptr && a.rayOffsets == nullptr)
     return trace_tlas<LAYOUT, true>(a, kind, counting, c, numSMs, s);
   return trace_tlas<LAYOUT, false>(a, kind, counting, c, numSMs, s);
