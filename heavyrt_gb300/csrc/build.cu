@@ -233,18 +233,21 @@ using bc::atomic_add_acq_rel;
 using bc::atomic_add_acq_rel_cta;
 using bc::kRefitSlice;
 
-__global__ void __launch_bounds__(kThreads) k_refit(BuildParams* params, BVHNode32* lr, uint32_t* lrCount,
-                                                    const uint32_t* __restrict__ parent, uint32_t* visit,
-                                                    const uint32_t* __restrict__ rangeEnd)
+using bc::kRefitMinBlocks;
+using bc::kRefitThreads;
+
+__global__ void __launch_bounds__(kRefitThreads, kRefitMinBlocks)
+    k_refit(BuildParams* params, BVHNode32* lr, uint32_t* lrCount, const uint32_t* __restrict__ parent,
+            uint32_t* visit, const uint32_t* __restrict__ rangeEnd)
 {
   __shared__ uint32_t s_visit[kRefitSlice];
   const uint32_t L = params->nLeaves;
   const uint32_t lo = blockIdx.x * kRefitSlice;
   if (lo >= L) return;
   const uint32_t hi = min(lo + kRefitSlice, L);
-  for (uint32_t k = threadIdx.x; k < kRefitSlice; k += kThreads) s_visit[k] = 0u;
+  for (uint32_t k = threadIdx.x; k < kRefitSlice; k += kRefitThreads) s_visit[k] = 0u;
   __syncthreads();
-  for (uint32_t i = lo + threadIdx.x; i < hi; i += kThreads)
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += kRefitThreads)
   {
     uint32_t node = L - 1 + i;
     lrCount[node] = 0;
@@ -402,7 +405,7 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
   e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);
   if (e != cudaSuccess) return e;
   k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent, b.visit + N);
-  k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
+  k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kRefitThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
                                                                    b.visit + N);
   k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
   k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
@@ -433,7 +436,7 @@ cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, c
   e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);
   if (e != cudaSuccess) return e;
   k_karras<<<g, kThreads, 0, s>>>(b.compressed, b.params, b.lr, b.parent, b.visit + N);
-  k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
+  k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kRefitThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
                                                                    b.visit + N);
   k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
   k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);

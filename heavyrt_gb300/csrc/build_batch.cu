@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
 }
 
 // Bottom-up refit per geometry (as k_refit in build.cu, local numbering).
-__global__ void __launch_bounds__(kThreads) k_seg_refit(const uint32_t* __restrict__ leafOffsets,
+__global__ void __launch_bounds__(bc::kRefitThreads, bc::kRefitMinBlocks) k_seg_refit(const uint32_t* __restrict__ leafOffsets,
                                                         const uint32_t* __restrict__ intOffsets,
                                                         const uint32_t* __restrict__ nodeOffsets, uint32_t G,
                                                         const uint32_t* __restrict__ counts, BVHNode32* lr,
@@ -324,9 +324,9 @@ __global__ void __launch_bounds__(kThreads) k_seg_refit(const uint32_t* __restri
   const uint32_t lo = blockIdx.x * bc::kRefitSlice;
   if (lo >= Ltot) return;
   const uint32_t hi = min(lo + bc::kRefitSlice, Ltot);
-  for (uint32_t k = threadIdx.x; k < bc::kRefitSlice; k += kThreads) s_visit[k] = 0u;
+  for (uint32_t k = threadIdx.x; k < bc::kRefitSlice; k += bc::kRefitThreads) s_visit[k] = 0u;
   __syncthreads();
-  for (uint32_t g = lo + threadIdx.x; g < hi; g += kThreads)
+  for (uint32_t g = lo + threadIdx.x; g < hi; g += bc::kRefitThreads)
   {
     const uint32_t s = find_segment(leafOffsets, G, g);
     const uint32_t lb = leafOffsets[s];
@@ -491,7 +491,7 @@ cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t s)
                                       b.sortedIdx, b.recs, b.errorWord);
   k_seg_karras<<<g, kThreads, 0, s>>>(b.compressed, b.leafOffsets, b.intOffsets, b.nodeOffsets, G, b.counts, b.lr,
                                       b.parent, b.visit + N);
-  k_seg_refit<<<(N + bc::kRefitSlice - 1) / bc::kRefitSlice, kThreads, 0, s>>>(
+  k_seg_refit<<<(N + bc::kRefitSlice - 1) / bc::kRefitSlice, bc::kRefitThreads, 0, s>>>(
       b.leafOffsets, b.intOffsets, b.nodeOffsets, G, b.counts, b.lr, b.lrCount, b.parent, b.visit, b.visit + N,
       b.errorWord);
   k_seg_records<<<g, kThreads, 0, s>>>(b.triOffsets, b.leafOffsets, b.intOffsets, b.nodeOffsets, b.recOffsets, G,

@@ -142,7 +142,12 @@ __device__ __forceinline__ void karras_node(const uint32_t* __restrict__ codes, 
 
 // Leaves per block of the bottom-up refit: the nodes whose leaf range lies in
 // a block's slice finish with counters in shared memory.
-constexpr uint32_t kRefitSlice = 1024;
+constexpr uint32_t kRefitSlice = 512;
+// One refit thread per leaf of the slice, so a slice's walks run side by side,
+// at 32 registers so that four blocks (64 warps) fit on an SM: the walks are
+// chains of dependent loads and atomics, and the warps in flight hide them.
+constexpr int kRefitThreads = 512;
+constexpr int kRefitMinBlocks = 4;
 
 __device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v)
 {
