@@ -83,6 +83,8 @@ def parse():
     p.add_argument("--only-precision", action="store_true",
                    help="run only the quantised-node precision measurement (prints its JSON object)")
     p.add_argument("--soup-tris", type=int, default=8388608, help="soup size of the precision measurement")
+    p.add_argument("--only-build", type=int, default=0, metavar="K",
+                   help="only K builds of the headline scene (the launch list of the build)")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     p.add_argument("--only-served", action="store_true",
                    help="run only the served-stream measurement (prints its JSON object)")
@@ -797,6 +799,25 @@ def run_served(ctx, args) -> dict:
 
 # ---------------------------------------------------------------- GPU engine
 
+def run_builds(ctx, args, w):
+    """K builds of the headline scene; GPU build time of each (CUDA events around the build's launches)."""
+    from heavyrt_gb300 import SceneRT
+
+    ms = []
+    for _ in range(args.only_build):
+        s = SceneRT(ctx, layout=args.layout)
+        if args.layout != "bvh2":
+            s.set_bvh4_merge(args.merge)
+        g = s.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+        s.AddInstance(g)
+        s.CommitScene()
+        ms.append(s.geom_info(g)["build_ms"])
+        s.close()
+    return {"workload": f"heightfield{args.nx}x{args.nx} ({w.idx.size // 3} tris), {args.layout} (merge {args.merge})",
+            "builds": len(ms), "build_ms": [round(x, 4) for x in ms],
+            "median_ms": round(statistics.median(ms), 4) if ms else None}
+
+
 def run_frames(ctx, args, w, trace_configs=None) -> dict:
     """Whole frames of HeavyRT's two example renderers on the device (hrt_frame):
     RTAO (examples/02_rtao: eye rays, nearest hit, hit shading, 16 AO rays per
@@ -894,6 +915,10 @@ def run_engine(args):
             print(json.dumps({"precision": run_precision(ctx, args)}), flush=True)
         return 0
     w = make_frame(args)
+    if args.only_build:
+        if rank == 0:
+            print(json.dumps({"build": run_builds(ctx, args, w)}), flush=True)
+        return 0
     if args.only_frames:
         if rank == 0:
             print(json.dumps({"frames": run_frames(ctx, args, w)}), flush=True)
