@@ -751,16 +751,19 @@ int ensure_stage(hrt_scene* s, uint64_t n)
 // null, the work counter the launch uses instead of a slot of the scene's ring.
 struct QuerySegments
 {
-  const uint32_t* rayOffsets = nullptr;
-  const uint32_t* segInst = nullptr;
-  uint32_t        nSeg = 0;
-  unsigned int*   counter = nullptr;
+  const uint32_t*    rayOffsets = nullptr;
+  const uint32_t*    segInst = nullptr;
+  uint32_t           nSeg = 0;
+  unsigned int*      counter = nullptr;
+  const TraceConfig* config = nullptr;  // launch shape for this launch instead of the scene's
 };
 
 int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out, int counting, cudaStream_t st,
                  const QuerySegments& q = QuerySegments())
 {
   if (!s->committed) return fail(s->ctx, HRT_ERR_STATE, "query before hrt_commit_scene");
+  if ((rays && !aligned_to(rays, 16)) || (kind == 0 && out && !aligned_to(out, 16)))
+    return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "ray and hit arrays must be 16-byte aligned");
   if (n == 0) return HRT_OK;
   if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
   if (n > 0xFFFFFFFFull) return fail(s->ctx, HRT_ERR_CAPACITY, "more than 2^32-1 rays in one query");
@@ -784,7 +787,7 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
     a.tlasTris = s->tlas.tris;
   }
   if (s->single && !q.rayOffsets) a.one = &s->singleDesc;
-  cudaError_t e = trace(a, kind, counting, s->layout, s->cfg[kind], s->ctx->numSMs, st);
+  cudaError_t e = trace(a, kind, counting, s->layout, q.config ? *q.config : s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
 }
@@ -1169,15 +1172,26 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
   cudaStream_t cs = ctx->stream;
   int st = HRT_OK;
   // Page-locked host arrays are mapped into the GPU's address space: the
-  // traversal reads such rays in place over the host link, and writes any-hit
-  // flags (1 byte per ray) in place too.  Nearest hits (32 bytes per ray) go
-  // to the device and come back by copy.  Other host memory is copied in.
-  const float* mappedRays = static_cast<const float*>(mapped_host(rays));
-  void* mappedOut = kind == 1 ? mapped_host(out) : nullptr;
+  // traversal reads such rays in place over the host link and writes the
+  // results in place too.  Nearest hits in place come from the one-thread-per-
+  // ray kernel, whose warps write 32 consecutive hits at once (the persistent
+  // pool writes each hit when its ray ends, scattered 32-byte writes that the
+  // link serves poorly).  Other host memory (or arrays that are not 16-byte
+  // aligned) goes through the staging buffers.
+  const float* mappedRays = aligned_to(rays, 16) ? static_cast<const float*>(mapped_host(rays)) : nullptr;
+  void* mappedOut = kind == 1 || aligned_to(out, 16) ? mapped_host(out) : nullptr;
   const bool inPlace = mappedRays && mappedOut;
   if (inPlace)
   {
-    st = launch_query(s, kind, mappedRays, n, mappedOut, 0, cs);
+    QuerySegments q;
+    TraceConfig grid = s->cfg[kind];
+    if (kind == 0)
+    {
+      grid.persistent = 0;
+      grid.threadsPerBlock = 256;
+      q.config = &grid;
+    }
+    st = launch_query(s, kind, mappedRays, n, mappedOut, 0, cs, q);
     if (st != HRT_OK) return st;
   }
   else if ((st = ensure_stage(s, n)) != HRT_OK)
@@ -1221,9 +1235,9 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
   return read_device_check(s, cs);
 }
 
-// Asynchronous host-pointer query: page-locked rays are read in place,
-// page-locked any-hit flags written in place; everything else goes through
-// stream-ordered device allocations and copies on `st`.
+// Asynchronous host-pointer query: page-locked (16-byte aligned) rays are read
+// in place and page-locked results written in place; everything else goes
+// through stream-ordered device allocations and copies on `st`.
 static int query_host_async(hrt_scene* s, int kind, const float* rays, uint64_t n, void* out, cudaStream_t st)
 {
   if (!s) return HRT_ERR_INVALID_ARGUMENT;
@@ -1231,8 +1245,8 @@ static int query_host_async(hrt_scene* s, int kind, const float* rays, uint64_t 
   if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
   hrt_context* ctx = s->ctx;
   cudaSetDevice(ctx->device);
-  const float* mappedRays = static_cast<const float*>(mapped_host(rays));
-  void* mappedOut = kind == 1 ? mapped_host(out) : nullptr;
+  const float* mappedRays = aligned_to(rays, 16) ? static_cast<const float*>(mapped_host(rays)) : nullptr;
+  void* mappedOut = kind == 1 || aligned_to(out, 16) ? mapped_host(out) : nullptr;
   const size_t outSize = kind == 0 ? sizeof(hrt_hit) : 1;
   float* dRays = nullptr;
   void* dOut = nullptr;
@@ -1242,7 +1256,15 @@ static int query_host_async(hrt_scene* s, int kind, const float* rays, uint64_t 
     HRT_CUDA(ctx, cudaMemcpyAsync(dRays, rays, 32 * n, cudaMemcpyHostToDevice, st));
   }
   if (!mappedOut) HRT_CUDA(ctx, cudaMallocAsync(&dOut, outSize * n, st));
-  int r = launch_query(s, kind, mappedRays ? mappedRays : dRays, n, mappedOut ? mappedOut : dOut, 0, st);
+  QuerySegments q;
+  TraceConfig grid = s->cfg[kind];
+  if (kind == 0 && mappedOut)
+  {
+    grid.persistent = 0;  // hits written in place: see query_host
+    grid.threadsPerBlock = 256;
+    q.config = &grid;
+  }
+  int r = launch_query(s, kind, mappedRays ? mappedRays : dRays, n, mappedOut ? mappedOut : dOut, 0, st, q);
   cudaError_t e = cudaSuccess;
   if (r == HRT_OK && dOut) e = cudaMemcpyAsync(out, dOut, outSize * n, cudaMemcpyDeviceToHost, st);
   if (dRays) cudaFreeAsync(dRays, st);

@@ -124,6 +124,10 @@ bool is_identity(const float* m);
 // The device address of page-locked host memory (mapped into the GPU's
 // address space), or null for pageable memory.
 void* mapped_host(const void* p);
+// True when p is a multiple of `bytes` (a power of two).  Kernels read rays
+// and write hits as 16-byte vectors, so arrays they access in place must be
+// 16-byte aligned; the entry points check this before any launch.
+inline bool aligned_to(const void* p, uintptr_t bytes) { return (reinterpret_cast<uintptr_t>(p) & (bytes - 1)) == 0; }
 
 }  // namespace api
 }  // namespace hrt

@@ -314,6 +314,7 @@ int hrt_gen_eye_rays(hrt_context* ctx, const float projInv[16], const float worl
                      uint32_t height, float tNear, float tFar, float* rays, void* stream)
 {
   if (!ctx || !projInv || !worldViewInv || (!rays && width && height)) return HRT_ERR_INVALID_ARGUMENT;
+  if (!aligned_to(rays, 16)) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "ray array must be 16-byte aligned");
   if ((uint64_t)width * height == 0) return HRT_OK;
   cudaSetDevice(ctx->device);
   Mat4 p, v;
@@ -329,6 +330,7 @@ int hrt_gen_pinhole_rays(hrt_context* ctx, const float eye[3], const float targe
                          uint32_t width, uint32_t height, float tmin, float tmax, float* rays, void* stream)
 {
   if (!ctx || !eye || !target || !up || (!rays && width && height)) return HRT_ERR_INVALID_ARGUMENT;
+  if (!aligned_to(rays, 16)) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "ray array must be 16-byte aligned");
   if ((uint64_t)width * height == 0) return HRT_OK;
   cudaSetDevice(ctx->device);
   // the frame, as the host generator sets it up (heavyrt_gb300/csrc/workload.c)
@@ -362,6 +364,8 @@ int hrt_gen_ao_rays(hrt_scene* s, uint64_t seed, const float* eyeRays, const hrt
   if (!s || !count) return HRT_ERR_INVALID_ARGUMENT;
   hrt_context* ctx = s->ctx;
   *count = 0;
+  if (!aligned_to(eyeRays, 16) || !aligned_to(hits, 16) || !aligned_to(aoRays, 16) || !aligned_to(owner, 4))
+    return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "ray and hit arrays must be 16-byte aligned, owners 4-byte aligned");
   if (nEye == 0 || perHit == 0) return HRT_OK;
   if (!eyeRays || !hits || !aoRays) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "null ray, hit or output pointer");
   if (nEye > 0xFFFFFFFFull) return fail(ctx, HRT_ERR_CAPACITY, "more than 2^32-1 eye rays");

@@ -557,12 +557,12 @@ int ensure_pixels(hrt_frame* f, uint64_t n)
 }
 
 // Where the kernels write a frame's colours: device or managed memory
-// directly; host memory (page-locked or not) through the frame's own buffer
-// and one copy at the end of the frame.
+// directly (4-byte aligned); host memory (page-locked or not) and unaligned
+// arrays through the frame's own buffer and one copy at the end of the frame.
 int color_target(hrt_frame* f, uint32_t* colors, uint64_t n, uint32_t** target)
 {
   cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, colors) == cudaSuccess &&
+  if (aligned_to(colors, 4) && cudaPointerGetAttributes(&a, colors) == cudaSuccess &&
       (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
   {
     *target = colors;
@@ -583,7 +583,7 @@ int color_target(hrt_frame* f, uint32_t* colors, uint64_t n, uint32_t** target)
 int finish_colors(hrt_frame* f, uint32_t* colors, const uint32_t* target, uint64_t n, cudaStream_t cs)
 {
   if (target == colors) return HRT_OK;
-  HRT_CUDA(f->ctx, cudaMemcpyAsync(colors, target, 4 * n, cudaMemcpyDeviceToHost, cs));
+  HRT_CUDA(f->ctx, cudaMemcpyAsync(colors, target, 4 * n, cudaMemcpyDefault, cs));
   HRT_CUDA(f->ctx, cudaStreamSynchronize(cs));
   return HRT_OK;
 }

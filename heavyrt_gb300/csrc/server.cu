@@ -172,11 +172,12 @@ void CUDART_CB on_slot_done(void* p)
 cudaError_t issue(hrt_server* S, Slot* sl)
 {
   const uint32_t maxReq = S->cfg.maxBatchRequests;
-  // A batch of one request whose rays are page-locked reads them in place over
-  // the host link (no copy in); its any-hit flags are written in place too
-  // when the output is page-locked.
+  // A batch of one request whose rays are page-locked (and 16-byte aligned)
+  // reads them in place over the host link (no copy in); its any-hit flags are
+  // written in place too when the output is page-locked.
   const Request* only = sl->reqs.size() == 1 ? sl->reqs[0] : nullptr;
-  const float4* inPlaceRays = only ? static_cast<const float4*>(mapped_host(only->rays)) : nullptr;
+  const float4* inPlaceRays =
+      only && aligned_to(only->rays, 16) ? static_cast<const float4*>(mapped_host(only->rays)) : nullptr;
   void* inPlaceOut = only && only->kind == 1 ? mapped_host(only->out) : nullptr;
   uint32_t* hOff[2] = {sl->hIdx, sl->hIdx + (2 * maxReq + 1)};
   uint32_t* dOff[2] = {sl->dIdx, sl->dIdx + (2 * maxReq + 1)};

@@ -92,6 +92,36 @@ __device__ __forceinline__ void slab(const Ray& r, float bx0, float by0, float b
   tf = fminf(fminf(fmaxf(lo, hi), fmaxf(lo1, hi1)), fmaxf(lo2, hi2));
 }
 
+// A 32-byte ray or hit record: one 256-bit access when the record is 32-byte
+// aligned (sm_100 and later), else two 128-bit ones.  A warp's 32 records are
+// then one contiguous kilobyte per instruction, which matters most for arrays
+// read and written in place over the host link.
+__device__ __forceinline__ void load_record(const float4* __restrict__ p, float4& a, float4& b)
+{
+  if ((reinterpret_cast<uintptr_t>(p) & 31u) == 0u)
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+  else
+  {
+    a = __ldg(p);
+    b = __ldg(p + 1);
+  }
+}
+
+__device__ __forceinline__ void store_record(float4* p, const float4& a, const float4& b)
+{
+  if ((reinterpret_cast<uintptr_t>(p) & 31u) == 0u)
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+                 "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+                 : "memory");
+  else
+  {
+    p[0] = a;
+    p[1] = b;
+  }
+}
+
 struct Hit
 {
   float    t, u, v;
@@ -551,9 +581,9 @@ __device__ __forceinline__ void write_result(const Lane& L, const InstanceDesc* 
   {
     const uint32_t instId = hit ? inst[L.h.inst].instId : 0xFFFFFFFFu;
     const uint32_t geomId = hit ? inst[L.h.inst].geomId : 0xFFFFFFFFu;
-    float4* o = reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray);
-    o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(instId), __uint_as_float(geomId));
-    o[1] = make_float4(L.h.u, L.h.v, 0.0f, 0.0f);
+    store_record(reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray),
+                 make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(instId), __uint_as_float(geomId)),
+                 make_float4(L.h.u, L.h.v, 0.0f, 0.0f));
   }
 }
 
@@ -591,8 +621,7 @@ __device__ __forceinline__ uint32_t first_instance(Lane& L, uint32_t i, const Se
 __device__ __forceinline__ void start_ray(Lane& L, uint32_t i, const float4* __restrict__ rays)
 {
   L.ray = i;
-  L.po = __ldg(rays + 2 * (size_t)i + 0);
-  L.di = __ldg(rays + 2 * (size_t)i + 1);
+  load_record(rays + 2 * (size_t)i, L.po, L.di);
   L.h.t = L.di.w;
   L.h.u = L.h.v = 0.0f;
   L.h.prim = L.h.inst = 0xFFFFFFFFu;
@@ -722,8 +751,8 @@ struct Lane1
 
 __device__ __forceinline__ void start_ray_one(Lane1& L, uint32_t i, const float4* __restrict__ rays)
 {
-  const float4 po = __ldg(rays + 2 * (size_t)i + 0);
-  const float4 di = __ldg(rays + 2 * (size_t)i + 1);
+  float4 po, di;
+  load_record(rays + 2 * (size_t)i, po, di);
   L.ray = i;
   L.r.ox = po.x; L.r.oy = po.y; L.r.oz = po.z; L.r.tNear = po.w;
   L.r.dx = di.x; L.r.dy = di.y; L.r.dz = di.z;
@@ -767,10 +796,10 @@ __device__ __forceinline__ void write_result_one(const Lane1& L, uint32_t instId
     reinterpret_cast<uint8_t*>(out)[L.ray] = hit ? 1 : 0;
   else
   {
-    float4* o = reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray);
-    o[0] = make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(hit ? instId : 0xFFFFFFFFu),
-                       __uint_as_float(hit ? geomId : 0xFFFFFFFFu));
-    o[1] = make_float4(L.h.u, L.h.v, 0.0f, 0.0f);
+    store_record(reinterpret_cast<float4*>(reinterpret_cast<hrt_hit*>(out) + L.ray),
+                 make_float4(L.h.t, __uint_as_float(L.h.prim), __uint_as_float(hit ? instId : 0xFFFFFFFFu),
+                             __uint_as_float(hit ? geomId : 0xFFFFFFFFu)),
+                 make_float4(L.h.u, L.h.v, 0.0f, 0.0f));
   }
 }
 

@@ -249,6 +249,70 @@ def test_large_host_queries_are_pipelined_exactly(native):
     assert 0.2 < want_a.mean() < 1.0
 
 
+def test_host_queries_in_place_and_alignment(native):
+    """Page-locked rays and hits are read and written in place (nearest hits by
+    the one-thread-per-ray kernel); records at a 32-byte boundary take one
+    256-bit access, records at a 16-byte boundary two 128-bit ones; page-locked
+    arrays off a 16-byte boundary go through the staging copies; every form
+    gives the device query's results.  Arrays off a 16-byte boundary handed to
+    the device entry points are refused before any launch (checked with n = 0,
+    so that nothing could launch even if the check were missing)."""
+    import ctypes
+
+    import torch
+
+    from heavyrt_gb300 import PinnedBuffer
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(8, 120, 120)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 320, 200),
+                           wl.rays_at_triangles(6, v, idx, 40001, jitter=0.02)])
+    n = rays.shape[0]
+    s, _ = _scene(v, idx)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+    da = torch.empty(n, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    s.query_device(0, dr.data_ptr(), n, dh.data_ptr(), stream)
+    s.query_device(1, dr.data_ptr(), n, da.data_ptr(), stream)
+    torch.cuda.synchronize()
+    want_h, want_a = dh.cpu().numpy().view(np.uint32), da.cpu().numpy().astype(bool)
+    L = E.lib()
+    pin_r = PinnedBuffer(rays.nbytes + 64)
+    pin_h = PinnedBuffer(32 * n + 64)
+    pin_a = PinnedBuffer(n + 64)
+    for r_off, h_off in ((0, 0), (16, 16), (0, 16), (16, 0), (4, 0), (0, 4)):
+        pin_r.array(np.uint8, rays.nbytes + 64)[r_off:r_off + rays.nbytes] = rays.view(np.uint8).reshape(-1)
+        hv = pin_h.array(np.uint8, 32 * n + 64)
+        hv[:] = 0xAB
+        rp, hp = ctypes.c_void_p(pin_r.ptr + r_off), ctypes.c_void_p(pin_h.ptr + h_off)
+        assert L.hrt_query_nearest_host(s._h, rp, n, hp) == 0, (r_off, h_off, s.ctx.last_error())
+        got = hv[h_off:h_off + 32 * n].view(np.uint32).reshape(-1, 8)
+        np.testing.assert_array_equal(got, want_h, err_msg=f"rays +{r_off} B, hits +{h_off} B")
+        assert (hv[:h_off] == 0xAB).all() and (hv[h_off + 32 * n:] == 0xAB).all()
+        av = pin_a.array(np.uint8, n + 64)
+        av[:] = 7
+        assert L.hrt_query_any_host(s._h, rp, n, ctypes.c_void_p(pin_a.ptr + 1)) == 0
+        np.testing.assert_array_equal(av[1:n + 1].astype(bool), want_a)
+        assert av[0] == 7 and (av[n + 1:] == 7).all()
+    # device entry points: off a 16-byte boundary is an invalid argument
+    HRT_ERR_INVALID_ARGUMENT = 1
+    assert L.hrt_query_nearest(s._h, ctypes.c_void_p(dr.data_ptr() + 4), 0, ctypes.c_void_p(dh.data_ptr()),
+                               ctypes.c_void_p(stream)) == HRT_ERR_INVALID_ARGUMENT
+    assert L.hrt_query_nearest(s._h, ctypes.c_void_p(dr.data_ptr()), 0, ctypes.c_void_p(dh.data_ptr() + 8),
+                               ctypes.c_void_p(stream)) == HRT_ERR_INVALID_ARGUMENT
+    assert L.hrt_query_any(s._h, ctypes.c_void_p(dr.data_ptr() + 8), 0, ctypes.c_void_p(da.data_ptr()),
+                           ctypes.c_void_p(stream)) == HRT_ERR_INVALID_ARGUMENT
+    assert "16-byte aligned" in s.ctx.last_error()
+    # an any-hit output needs no alignment
+    assert L.hrt_query_any(s._h, ctypes.c_void_p(dr.data_ptr()), 0, ctypes.c_void_p(da.data_ptr() + 1),
+                           ctypes.c_void_p(stream)) == 0
+    pin_r.free()
+    pin_h.free()
+    pin_a.free()
+
+
 def test_instances_exact_transforms(native):
     """Several instances of one geometry; transforms exact in binary32 so the
     expected result is computed by tracing the oracle with transformed rays."""
