@@ -185,10 +185,12 @@ int hrt_query_any(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out,
 
 /* Same as the two calls above with HOST arrays; the results are in place when
  * the call returns.  Page-locked arrays (hrt_host_alloc, cudaHostAlloc,
- * cudaHostRegister) are used where they are: the traversal reads their rays
- * over the host link and writes any-hit flags straight into them; nearest hits
- * come back by copy.  Other host memory is copied in.  Batches above 2^18 rays
- * run as chunks whose copies overlap the traversal of other chunks. */
+ * cudaHostRegister) at a 16-byte boundary are used where they are: the
+ * traversal reads their rays over the host link and writes its results
+ * straight into them.  Other host memory is copied in and out; such batches
+ * above 2^18 rays run as chunks whose copies overlap the traversal of other
+ * chunks.  The device-pointer calls above want rays (and hits) at a 16-byte
+ * boundary and return HRT_ERR_INVALID_ARGUMENT otherwise. */
 int hrt_query_nearest_host(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits);
 int hrt_query_any_host(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out);
 
