@@ -358,6 +358,42 @@ def test_instances_exact_transforms(native):
     np.testing.assert_array_equal(got["primId"][found], best["primId"][found])
 
 
+@pytest.mark.parametrize("layout", ["bvh2", "bvh4", "bvh4_f16", "bvh4_q8"])
+def test_single_instance_transform_and_update(native, layout):
+    """One instance: under a transform the scene takes the general kernel (the
+    ray is mapped into the instance), after UpdateInstance to the identity and a
+    new commit the single-instance kernel; both equal the oracle."""
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(31, 5000, off=0.04)
+    m = np.diag([2.0, 2.0, 2.0, 1.0]).astype(np.float32)
+    m[:3, 3] = [0.5, -1.0, 0.25]
+    rays = np.concatenate([wl.sphere_rays(7, 3000, 8.0), wl.rays_at_triangles(8, v, idx, 3000, radius=4.0)])
+    s = SceneRT(layout=layout)
+    g = s.AddGeom_Triangles3f(v, v.shape[0], idx, idx.size, vByteStride=16)
+    s.AddInstance(g, m)
+    s.CommitScene()
+    o, _ = _oracle_expect(v, idx)
+    inv = np.linalg.inv(m.astype(np.float64)).astype(np.float32)
+    r = rays.copy()
+    o3, d3 = rays[:, 0:3], rays[:, 4:7]
+    for row in range(3):
+        a = inv[row]
+        r[:, row] = ((a[0] * o3[:, 0] + a[1] * o3[:, 1]) + a[2] * o3[:, 2]) + a[3] * np.float32(1.0)
+        r[:, 4 + row] = ((a[0] * d3[:, 0] + a[1] * d3[:, 1]) + a[2] * d3[:, 2]) + a[3] * np.float32(0.0)
+    want = o.trace(r)
+    got = s.RayQuery_NearestHit(rays)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(r, any_hit=True))
+    assert (want["geomId"] != MISS).mean() > 0.2
+    s.UpdateInstance(0, np.eye(4, dtype=np.float32))
+    s.CommitScene()
+    np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), o.trace(rays).view(np.uint32))
+    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True))
+    s.close()
+
+
 def test_empty_geometry_and_errors(native):
     from heavyrt_gb300 import HrtError, SceneRT
     from heavyrt_gb300 import engine as E
