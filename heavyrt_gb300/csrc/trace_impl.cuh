@@ -851,6 +851,26 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
   }
 }
 
+// One thread per ray over one instance: a warp's 32 consecutive rays end
+// together, so their results go out as one contiguous kilobyte (results
+// written in place over the host link want this).
+template <int LAYOUT, bool ANY, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+    k_trace_one_grid(const float4* __restrict__ rays, uint32_t n, const void* __restrict__ nodes,
+                     const TriRec* __restrict__ tris, uint32_t instId, uint32_t geomId, void* out, uint32_t* errorWord)
+{
+  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT>::value * THREADS entries
+  uint32_t* stack = s_stack + threadIdx.x;
+  const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
+  if (i >= n) return;
+  Lane1 L;
+  L.nodes = nodes;
+  L.tris = tris;
+  start_ray_one(L, i, rays);
+  while (!out_of_budget(L, errorWord) && !step_one<LAYOUT, ANY, THREADS>(L, stack, errorWord)) {}
+  write_result_one<ANY>(L, instId, geomId, out);
+}
+
 template <int LAYOUT, bool ANY, int THREADS>
 cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
@@ -860,7 +880,18 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   {
     cudaError_t e = cudaFuncSetAttribute(k_trace_one<LAYOUT, ANY, THREADS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_trace_one_grid<LAYOUT, ANY, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
     if (e != cudaSuccess) return e;
+  }
+  const InstanceDesc& d = *a.one;
+  const void* nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
+  if (!c.persistent)
+  {
+    k_trace_one_grid<LAYOUT, ANY, THREADS><<<(uint32_t)(((uint64_t)n + THREADS - 1) / THREADS), THREADS, smem, s>>>(
+        a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits, a.errorWord);
+    return cudaGetLastError();
   }
   int perSM = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_one<LAYOUT, ANY, THREADS>, THREADS,
@@ -872,8 +903,6 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   if (blocks > need) blocks = need;
   e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
-  const InstanceDesc& d = *a.one;
-  const void* nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
   k_trace_one<LAYOUT, ANY, THREADS><<<(uint32_t)blocks, THREADS, smem, s>>>(
       a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill,
       c.refillLanes);
@@ -960,11 +989,11 @@ cudaError_t trace_tlas(const TraceArgs& a, int kind, int counting, const TraceCo
 // Counting runs use the one-thread-per-ray grid at 128 threads: the counts do
 // not depend on the schedule.  A scene with an instance tree uses the
 // two-level kernels, except in segmented queries (one instance per ray).  A
-// scene of one untransformed instance uses the single-instance pool.
+// scene of one untransformed instance uses the single-instance kernels.
 template <int LAYOUT>
 cudaError_t trace_layout(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
-  if (a.one != nullptr && !counting && c.persistent && a.rayOffsets == nullptr && a.tlasRecs == nullptr)
+  if (a.one != nullptr && !counting && a.rayOffsets == nullptr && a.tlasRecs == nullptr)
     return trace_one<LAYOUT>(a, kind, c, numSMs, s);
   if (a.tlasRecs != nullptr && a.rayOffsets == nullptr)
     return trace_tlas<LAYOUT, true>(a, kind, counting, c, numSMs, s);
