@@ -257,11 +257,13 @@ __device__ __forceinline__ uint32_t q8_hi(float origin, float v, float scale, bo
 __device__ __forceinline__ void write_node4(int format, void* __restrict__ nodes, uint32_t outIdx, Slot (&slot)[4],
                                             int ns, uint32_t* errorWord)
 {
-  for (int k = ns; k < 4; k++)
-  {
-    for (int c = 0; c < 3; c++) { slot[k].lo[c] = 0.0f; slot[k].hi[c] = 0.0f; }
-    slot[k].ref = kEmptyRef;
-  }
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (k >= ns)
+    {
+      for (int c = 0; c < 3; c++) { slot[k].lo[c] = 0.0f; slot[k].hi[c] = 0.0f; }
+      slot[k].ref = kEmptyRef;
+    }
   if (format == 0)
   {
     Node4F32 o;
@@ -354,22 +356,18 @@ __device__ __forceinline__ int node4_slots(const BVHNode32* __restrict__ lr, con
     slot[0].ref = kLeafBit | runStarts[0];
     return 1;
   }
-  const uint32_t kids[2] = {lr[i].leftOffset, lr[i].escapeIndex};
-  uint32_t cand[4];
-  int nc = 0;
-  for (int k = 0; k < 2; k++)
+  // the children of each internal child (or the leaf child itself), left
+  // child's first, at fixed positions so that the slots stay in registers
+  const uint32_t k0 = lr[i].leftOffset, k1 = lr[i].escapeIndex;
+  const bool in0 = k0 + 1u < L, in1 = k1 + 1u < L;
+  const uint32_t a0 = in0 ? lr[k0].leftOffset : k0, b0 = in0 ? lr[k0].escapeIndex : 0u;
+  const uint32_t a1 = in1 ? lr[k1].leftOffset : k1, b1 = in1 ? lr[k1].escapeIndex : 0u;
+  const uint32_t cand[4] = {a0, in0 ? b0 : a1, in0 ? a1 : b1, b1};
+  const int nc = (in0 ? 2 : 1) + (in1 ? 2 : 1);
+#pragma unroll
+  for (int k = 0; k < 4; k++)
   {
-    const uint32_t c = kids[k];
-    if (c + 1u >= L)
-      cand[nc++] = c;
-    else
-    {
-      cand[nc++] = lr[c].leftOffset;
-      cand[nc++] = lr[c].escapeIndex;
-    }
-  }
-  for (int k = 0; k < nc; k++)
-  {
+    if (k >= nc) break;
     const uint32_t s = cand[k];
     const BVHNode32 n = lr[s];
     for (int c = 0; c < 3; c++) { slot[k].lo[c] = n.boxMin[c]; slot[k].hi[c] = n.boxMax[c]; }
