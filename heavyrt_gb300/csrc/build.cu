@@ -408,7 +408,7 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
   k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kRefitThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
                                                                    b.visit + N);
   k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
-  k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
+  if (b.recs) k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
   return cudaGetLastError();
 }
 
@@ -439,7 +439,7 @@ cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, c
   k_refit<<<(N + kRefitSlice - 1) / kRefitSlice, kRefitThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.parent, b.visit,
                                                                    b.visit + N);
   k_check_root<<<1, 1, 0, s>>>(b.params, b.visit, err);
-  k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
+  if (b.recs) k_records<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, b.recs);
   return cudaGetLastError();
 }
 

@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kThreads) k_seg_leaves(
     nd.escapeIndex = 0xFFFFFFFFu;
     lr[nodeOffsets[s] + L - 1 + k] = nd;
     lrCount[nodeOffsets[s] + L - 1 + k] = 0;
-    if (L == 1u)
+    if (L == 1u && recs != nullptr)
     {
       PairRec r;
       r.a = make_float4(mn[0], mn[1], mn[2], mx[0]);
@@ -396,6 +396,13 @@ __global__ void __launch_bounds__(kThreads) k_seg_records(const uint32_t* __rest
                                                           const uint32_t* __restrict__ visit, PairRec* __restrict__ recs,
                                                           uint32_t* errorWord)
 {
+  if (recs == nullptr)
+  {
+    // 4-wide layouts keep no pair records: only the check of each root
+    for (uint32_t s = blockIdx.x * kThreads + threadIdx.x; s < G; s += gridDim.x * kThreads)
+      if (intOffsets[s + 1] > intOffsets[s] && visit[intOffsets[s]] != 2u) atomicOr(errorWord, kErrLayout);
+    return;
+  }
   const uint32_t Itot = counts[1];
   for (uint32_t j = blockIdx.x * kThreads + threadIdx.x; j < Itot; j += gridDim.x * kThreads)
   {

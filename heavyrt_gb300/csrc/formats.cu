@@ -6,8 +6,9 @@
 // float2 texture coordinates, u32 indices and one u32 material id per
 // triangle.
 //
-// BVH blob ("HRTBVH01"): everything a built geometry keeps on the device
-// (vertices, build stage arrays, traversal records, 4-wide nodes), so that a
+// BVH blob ("HRTBVH02"): everything a built geometry keeps on the device
+// (vertices, build stage arrays, and the binary pair records or the 4-wide
+// nodes its layout traverses), so that a
 // geometry can be restored by copies alone, without a build: a warm start for
 // a server's resident scenes.  Blobs are tied to the layout they were built
 // with.
@@ -56,7 +57,7 @@ bool read_vsgf_header(FILE* f, VsgfHeader& h, uint64_t& actual)
 }
 
 // ---------------------------------------------------------------- BVH blobs
-constexpr char kBlobMagic[8] = {'H', 'R', 'T', 'B', 'V', 'H', '0', '1'};
+constexpr char kBlobMagic[8] = {'H', 'R', 'T', 'B', 'V', 'H', '0', '2'};
 
 struct BlobHeader
 {
@@ -85,10 +86,10 @@ std::vector<Part> parts(Geom& g, int layout)
                          {g.runStarts, 4 * L},
                          {g.lr, sizeof(BVHNode32) * nLR},
                          {g.lrCount, 4 * nLR},
-                         {g.recs, sizeof(PairRec) * (L > 1 ? L - 1 : 1)},
                          {g.tris, sizeof(TriRec) * N},
                          {g.sortedIdx, 12 * N}};
-  if (layout != HRT_LAYOUT_BVH2) p.push_back({g.nodes4, nodeBytes * g.nNodes4});
+  if (layout == HRT_LAYOUT_BVH2) p.push_back({g.recs, sizeof(PairRec) * (L > 1 ? L - 1 : 1)});
+  else p.push_back({g.nodes4, nodeBytes * g.nNodes4});
   return p;
 }
 
@@ -234,11 +235,12 @@ int hrt_geom_load(hrt_scene* s, const char* path, uint32_t* geomId)
                 {(void**)&g.runStarts, 4 * (L ? L : 1)},
                 {(void**)&g.lr, sizeof(BVHNode32) * (nLR ? nLR : 1)},
                 {(void**)&g.lrCount, 4 * (nLR ? nLR : 1)},
-                {(void**)&g.recs, sizeof(PairRec) * (L > 1 ? L - 1 : 1)},
                 {(void**)&g.tris, sizeof(TriRec) * (N ? N : 1)},
-                {(void**)&g.sortedIdx, 12 * (N ? N : 1)}};
+                {(void**)&g.sortedIdx, 12 * (N ? N : 1)},
+                {(void**)&g.recs, h.layout == HRT_LAYOUT_BVH2 ? sizeof(PairRec) * (L > 1 ? L - 1 : 1) : 0}};
   for (const A& a : allocs)
   {
+    if (a.bytes == 0) continue;
     const cudaError_t e = cudaMalloc(a.p, a.bytes);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "blob allocation"));
     g.bytes += a.bytes;

@@ -177,7 +177,9 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   HRT_CUDA(ctx, dalloc(&g.runStarts, N, bytes, st));
   HRT_CUDA(ctx, dalloc(&g.lr, 2 * (size_t)N - 1, bytes, st));
   HRT_CUDA(ctx, dalloc(&g.lrCount, 2 * (size_t)N - 1, bytes, st));
-  HRT_CUDA(ctx, dalloc(&g.recs, N > 1 ? N - 1 : 1, bytes, st));
+  // binary pair records only for the binary layout (the 4-wide layouts
+  // traverse their own nodes)
+  if (layout == HRT_LAYOUT_BVH2) HRT_CUDA(ctx, dalloc(&g.recs, N > 1 ? N - 1 : 1, bytes, st));
   HRT_CUDA(ctx, dalloc(&g.tris, N, bytes, st));
   HRT_CUDA(ctx, dalloc(&g.sortedIdx, 3 * (size_t)N, bytes, st));
   HRT_CUDA(ctx, cudaMallocAsync((void**)&keysAlt, sizeof(uint32_t) * N, st));
@@ -345,7 +347,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   HRT_CUDA(ctx, balloc(&b.runStarts, N, owned));
   HRT_CUDA(ctx, balloc(&b.lr, 2 * N, owned));
   HRT_CUDA(ctx, balloc(&b.lrCount, 2 * N, owned));
-  HRT_CUDA(ctx, balloc(&b.recs, N, owned));
+  if (s->layout == HRT_LAYOUT_BVH2) HRT_CUDA(ctx, balloc(&b.recs, N, owned));
   HRT_CUDA(ctx, balloc(&b.tris, N, owned));
   HRT_CUDA(ctx, balloc(&b.sortedIdx, 3 * N, owned));
   HRT_CUDA(ctx, balloc(&b.params, G, owned));
@@ -484,7 +486,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
     g.runStarts = b.runStarts + hLeaf[i];
     g.lr = b.lr + hNode[i];
     g.lrCount = b.lrCount + hNode[i];
-    g.recs = b.recs + hRec[i];
+    g.recs = b.recs ? b.recs + hRec[i] : nullptr;
     g.tris = b.tris + ht[i];
     g.sortedIdx = b.sortedIdx + 3 * (size_t)ht[i];
     g.params = b.params + i;

@@ -46,7 +46,7 @@ struct BuildBuffers
   uint32_t*  lrCount;         // 2*nTris-1
   uint32_t*  parent;          // 2*nTris-1
   uint32_t*  visit;           // 2*nTris: refit counters, then each internal node's range end
-  PairRec*   recs;            // max(nTris-1, 1)
+  PairRec*   recs;            // max(nTris-1, 1); null: no pair records (4-wide layouts)
   TriRec*    tris;            // nTris
   uint32_t*  sortedIdx;       // 3*nTris
   BuildParams* params;        // device
@@ -93,7 +93,7 @@ struct BatchBuffers
   uint32_t*  lrCount;           // 2*nTris
   uint32_t*  parent;            // 2*nTris
   uint32_t*  visit;             // 2*nTris: refit counters, then each internal node's range end
-  PairRec*   recs;              // nTris
+  PairRec*   recs;              // nTris; null: no pair records (4-wide layouts)
   TriRec*    tris;              // nTris; e1.w = triangle id local to the geometry
   uint32_t*  sortedIdx;         // 3*nTris, local vertex ids
   BuildParams* params;          // G: box, scale, nLeaves per geometry

@@ -118,8 +118,9 @@ uint64_t estimate_scene_bytes(uint64_t nTris, uint64_t nVert, int layout)
 {
   const uint64_t N = nTris ? nTris : 1;
   uint64_t b = 16 * nVert + N * (4 * 5 + sizeof(TriRec) + 12) + (2 * N) * (sizeof(BVHNode32) + 4) +
-               N * sizeof(PairRec) + sizeof(BuildParams);
-  if (layout != HRT_LAYOUT_BVH2) b += N * (layout == HRT_LAYOUT_BVH4_F32 ? sizeof(Node4F32) : sizeof(Node4F16));
+               sizeof(BuildParams);
+  if (layout == HRT_LAYOUT_BVH2) b += N * sizeof(PairRec);
+  else b += N * (layout == HRT_LAYOUT_BVH4_F32 ? sizeof(Node4F32) : sizeof(Node4F16));
   // transient build arrays (ping-pong, parents, visit counters, sort scratch)
   b += N * 4 * 6 + radix_sort_scratch_bytes((uint32_t)N) + 4 * 1024 * 32;
   // the staged copy of the inputs (16-byte vertices, indices) held until the build
