@@ -188,17 +188,18 @@ def build_bytes(n_tris: int, n_verts: int, n_leaves: int, n_nodes4: int, node4_b
     + 4 B histogram read per pair; run compaction 4 B per code in + 8 B per run
     out; leaves 4 + 12 + 48 + 48 + 12 B per triangle + 32 B per leaf; Karras
     hierarchy 2 log2(L) code reads + 16 B out per internal node; refit 2 x 32 B
-    + 2 x 4 B in, 32 B + 4 B out per internal node; pair records 96 B in + 64 B
-    out per internal node; 4-wide collapse 9 B of plan arrays per internal node
-    + 4 x 32 B in + one node out per 4-wide node."""
+    + 2 x 4 B in, 32 B + 4 B out per internal node; then for the binary layout
+    pair records 96 B in + 64 B out per internal node, for a 4-wide layout the
+    collapse: 9 B of plan arrays per internal node + 4 x 32 B in + one node out
+    per 4-wide node."""
     import math
 
     internal = max(n_leaves - 1, 0)
     log_l = math.log2(max(n_leaves, 2))
     return int(16 * n_verts + n_tris * (12 + 48 + 8 + 8) + n_tris * (4 * 16 + 4) + 4 * n_tris + 8 * n_leaves
                + n_tris * (4 + 12 + 48 + 48 + 12) + 32 * n_leaves + internal * (8 * log_l + 16)
-               + internal * (64 + 8 + 32 + 4) + internal * (96 + 64)
-               + (internal * 9 + n_nodes4 * (4 * 32 + node4_bytes) if n_nodes4 else 0))
+               + internal * (64 + 8 + 32 + 4)
+               + (internal * 9 + n_nodes4 * (4 * 32 + node4_bytes) if n_nodes4 else internal * (96 + 64)))
 
 
 def make_frame(args):
