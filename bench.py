@@ -85,6 +85,8 @@ def parse():
     p.add_argument("--soup-tris", type=int, default=8388608, help="soup size of the precision measurement")
     p.add_argument("--only-build", type=int, default=0, metavar="K",
                    help="only K builds of the headline scene (the launch list of the build)")
+    p.add_argument("--only-build-batched", type=int, default=0, metavar="K",
+                   help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     p.add_argument("--only-served", action="store_true",
                    help="run only the served-stream measurement (prints its JSON object)")
@@ -826,6 +828,22 @@ def run_builds(ctx, args, w):
             "median_ms": round(statistics.median(ms), 4) if ms else None}
 
 
+def run_builds_batched(ctx, args):
+    """K segmented builds of the 256-soup batch (BVH4 FP16, merge 1); GPU build time of each."""
+    from heavyrt_gb300 import autotune as AT
+    from heavyrt_gb300 import workload as wl
+
+    w = wl.config3(args.batch_scenes)
+    ms = []
+    for _ in range(args.only_build_batched):
+        scene, ids = AT.build_batch(ctx, w.verts, w.idx, "bvh4_f16", 1)
+        ms.append(scene.geom_info(ids[0])["build_ms"])
+        scene.close()
+    return {"workload": f"soups{len(w.verts)} ({sum(int(i.size) // 3 for i in w.idx)} tris), bvh4_f16 (merge 1)",
+            "builds": len(ms), "build_ms": [round(x, 4) for x in ms],
+            "median_ms": round(statistics.median(ms), 4) if ms else None}
+
+
 def run_frames(ctx, args, w, trace_configs=None) -> dict:
     """Whole frames of HeavyRT's two example renderers on the device (hrt_frame):
     RTAO (examples/02_rtao: eye rays, nearest hit, hit shading, 16 AO rays per
@@ -910,6 +928,10 @@ def run_engine(args):
     from heavyrt_gb300 import engine as E
 
     ctx = Context(local)
+    if args.only_build_batched:
+        if rank == 0:
+            print(json.dumps({"build_batched": run_builds_batched(ctx, args)}), flush=True)
+        return 0
     if args.only_batched:
         if rank == 0:
             print(json.dumps({"batched": run_batched(ctx, args)}), flush=True)
