@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_histograms(uint32_t* __restri
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restrict__ keysIn,
+__global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint32_t* __restrict__ keysIn,
                                                        const uint32_t* __restrict__ valsIn,
                                                        uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
                                                        uint32_t n, uint32_t shift, const uint32_t* __restrict__ digitBase,
