@@ -1190,7 +1190,7 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
     if (kind == 0)
     {
       grid.persistent = 0;
-      grid.threadsPerBlock = 256;
+      grid.threadsPerBlock = 128;
       q.config = &grid;
     }
     st = launch_query(s, kind, mappedRays, n, mappedOut, 0, cs, q);
@@ -1263,7 +1263,7 @@ static int query_host_async(hrt_scene* s, int kind, const float* rays, uint64_t 
   if (kind == 0 && mappedOut)
   {
     grid.persistent = 0;  // hits written in place: see query_host
-    grid.threadsPerBlock = 256;
+    grid.threadsPerBlock = 128;
     q.config = &grid;
   }
   int r = launch_query(s, kind, mappedRays ? mappedRays : dRays, n, mappedOut ? mappedOut : dOut, 0, st, q);
