@@ -358,6 +358,51 @@ def test_instances_exact_transforms(native):
     np.testing.assert_array_equal(got["primId"][found], best["primId"][found])
 
 
+@pytest.mark.parametrize("layout", ["bvh2", "bvh4_f16"])
+def test_in_place_host_queries_with_instance_tree(native, layout):
+    """Page-locked rays and results used in place on a scene of two instances
+    (the two-level kernels: instance tree, one-thread-per-ray form for nearest
+    hits) give the device query's results."""
+    import ctypes
+
+    import torch
+
+    from heavyrt_gb300 import PinnedBuffer, SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(41, 8000, off=0.04)
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = [2.5, 0.0, 0.0]
+    s = SceneRT(layout=layout)
+    g = s.AddGeom_Triangles3f(v, v.shape[0], idx, idx.size, vByteStride=16)
+    s.AddInstance(g)
+    s.AddInstance(g, m)
+    s.CommitScene()
+    rays = np.concatenate([wl.sphere_rays(3, 20000, 9.0), wl.rays_at_triangles(4, v, idx, 20000, radius=5.0)])
+    n = rays.shape[0]
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+    da = torch.empty(n, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    s.query_device(0, dr.data_ptr(), n, dh.data_ptr(), stream)
+    s.query_device(1, dr.data_ptr(), n, da.data_ptr(), stream)
+    torch.cuda.synchronize()
+    want_h, want_a = dh.cpu().numpy().view(np.uint32), da.cpu().numpy().astype(bool)
+    assert (want_h[:, 2] == 1).any() and (want_h[:, 2] == 0).any()  # hits on both instances
+    pin_r, pin_h, pin_a = PinnedBuffer(rays.nbytes), PinnedBuffer(32 * n), PinnedBuffer(n)
+    pin_r.array(np.float32, rays.size)[:] = rays.reshape(-1)
+    L = E.lib()
+    assert L.hrt_query_nearest_host(s._h, ctypes.c_void_p(pin_r.ptr), n, ctypes.c_void_p(pin_h.ptr)) == 0
+    assert L.hrt_query_any_host(s._h, ctypes.c_void_p(pin_r.ptr), n, ctypes.c_void_p(pin_a.ptr)) == 0
+    np.testing.assert_array_equal(pin_h.array(np.uint32, 8 * n).reshape(-1, 8), want_h)
+    np.testing.assert_array_equal(pin_a.array(np.uint8, n).astype(bool), want_a)
+    pin_r.free()
+    pin_h.free()
+    pin_a.free()
+    s.close()
+
+
 @pytest.mark.parametrize("layout", ["bvh2", "bvh4", "bvh4_f16", "bvh4_q8"])
 def test_single_instance_transform_and_update(native, layout):
     """One instance: under a transform the scene takes the general kernel (the
