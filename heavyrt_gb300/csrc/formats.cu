@@ -195,8 +195,10 @@ int hrt_geom_load(hrt_scene* s, const char* path, uint32_t* geomId)
   File f(path, "rb");
   if (!f.f) return fail(ctx, HRT_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
   BlobHeader h;
-  if (std::fread(&h, sizeof(h), 1, f.f) != 1 || std::memcmp(h.magic, kBlobMagic, 8) != 0)
+  if (std::fread(&h, sizeof(h), 1, f.f) != 1 || std::memcmp(h.magic, kBlobMagic, 6) != 0)
     return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "not a BVH blob");
+  if (std::memcmp(h.magic, kBlobMagic, 8) != 0)
+    return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "BVH blob of another format version: rebuild the geometry");
   std::lock_guard<std::mutex> lk(s->mu);
   if ((int)h.layout != s->layout) return fail(ctx, HRT_ERR_STATE, "the blob was built for another node layout");
   if (h.nTris > HRT_MAX_TRIS_PER_GEOM || h.nLeaves > h.nTris || (h.nTris && !h.nLeaves) ||
