@@ -40,6 +40,13 @@ def test_blob_round_trip(native, tmp_path, layout, merge):
     (tmp_path / "cut.bvh").write_bytes(blob[: len(blob) // 2])
     with pytest.raises(E.HrtError):
         SceneRT(layout=layout).load_geom(tmp_path / "cut.bvh")
+    # a blob of another format version is refused by name
+    assert blob[:6] == b"HRTBVH"
+    (tmp_path / "old.bvh").write_bytes(blob[:6] + b"01" + blob[8:])
+    c = SceneRT(layout=layout)
+    with pytest.raises(E.HrtError):
+        c.load_geom(tmp_path / "old.bvh")
+    assert "format version" in c.ctx.last_error()
 
 
 def test_vsgf_mesh_traces_like_oracle(native, tmp_path):
