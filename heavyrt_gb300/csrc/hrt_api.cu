@@ -725,7 +725,35 @@ bool lbvh_builder_name(const char* name)
   return s.find("lbvh") != std::string::npos;  // "cbvh_lbvh", "lbvh", "cbvh_lbvh_gpu" (core/builders/cbvh.cpp:45-55)
 }
 
-void* mapped_host(const void* p)
+// Whether the current device reaches pageable host memory through the host's
+// own page tables (address translation over NVLink-C2C on Grace-based
+// systems), so that a kernel may read and write such memory where it is;
+// cached per device.
+bool pageable_access()
+{
+  static std::atomic<int> known[64];  // 0 not asked yet, 1 no, 2 yes
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+  {
+    cudaGetLastError();
+    return false;
+  }
+  int k = known[dev].load(std::memory_order_relaxed);
+  if (k == 0)
+  {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess)
+    {
+      cudaGetLastError();
+      v = 0;
+    }
+    k = v ? 2 : 1;
+    known[dev].store(k, std::memory_order_relaxed);
+  }
+  return k == 2;
+}
+
+void* mapped_host(const void* p, bool pageable)
 {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
@@ -733,7 +761,9 @@ void* mapped_host(const void* p)
     cudaGetLastError();
     return nullptr;
   }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  if (pageable && a.type == cudaMemoryTypeUnregistered && pageable_access()) return const_cast<void*>(p);
+  return nullptr;
 }
 
 int ensure_stage(hrt_scene* s, uint64_t n)
@@ -1175,12 +1205,14 @@ static int query_host(hrt_scene* s, int kind, const float* rays, uint64_t n, voi
   int st = HRT_OK;
   // Page-locked host arrays are mapped into the GPU's address space: the
   // traversal reads such rays in place over the host link and writes the
-  // results in place too.  Nearest hits in place come from the one-thread-per-
+  // results in place too.  Where the device translates through the host's
+  // page tables, pageable rays are read in place as well (results into
+  // pageable memory still come back by copy).  Nearest hits in place come from the one-thread-per-
   // ray kernel, whose warps write 32 consecutive hits at once (the persistent
   // pool writes each hit when its ray ends, scattered 32-byte writes that the
   // link serves poorly).  Other host memory (or arrays that are not 16-byte
   // aligned) goes through the staging buffers.
-  const float* mappedRays = aligned_to(rays, 16) ? static_cast<const float*>(mapped_host(rays)) : nullptr;
+  const float* mappedRays = aligned_to(rays, 16) ? static_cast<const float*>(mapped_host(rays, true)) : nullptr;
   void* mappedOut = kind == 1 || aligned_to(out, 16) ? mapped_host(out) : nullptr;
   const bool inPlace = mappedRays && mappedOut;
   if (inPlace)
@@ -1247,7 +1279,7 @@ static int query_host_async(hrt_scene* s, int kind, const float* rays, uint64_t 
   if (!rays || !out) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "null ray or output pointer");
   hrt_context* ctx = s->ctx;
   cudaSetDevice(ctx->device);
-  const float* mappedRays = aligned_to(rays, 16) ? static_cast<const float*>(mapped_host(rays)) : nullptr;
+  const float* mappedRays = aligned_to(rays, 16) ? static_cast<const float*>(mapped_host(rays, true)) : nullptr;
   void* mappedOut = kind == 1 || aligned_to(out, 16) ? mapped_host(out) : nullptr;
   const size_t outSize = kind == 0 ? sizeof(hrt_hit) : 1;
   float* dRays = nullptr;

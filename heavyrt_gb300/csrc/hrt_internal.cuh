@@ -121,9 +121,12 @@ void make_instance_desc(const Geom& g, uint32_t geomId, uint32_t instId, const f
 // Column-major 4x4 -> rows 0..2 of its inverse (the reference checker's evaluation).
 void inverse4x4(const float* mc, float* inv12);
 bool is_identity(const float* m);
-// The device address of page-locked host memory (mapped into the GPU's
-// address space), or null for pageable memory.
-void* mapped_host(const void* p);
+// The address at which a kernel reaches host memory in place: the mapped
+// device address of page-locked memory; with `pageable`, pageable memory
+// itself where the device translates through the host's page tables
+// (pageable_access); null otherwise.
+void* mapped_host(const void* p, bool pageable = false);
+bool pageable_access();
 // True when p is a multiple of `bytes` (a power of two).  Kernels read rays
 // and write hits as 16-byte vectors, so arrays they access in place must be
 // 16-byte aligned; the entry points check this before any launch.

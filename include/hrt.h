@@ -187,7 +187,9 @@ int hrt_query_any(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out,
  * the call returns.  Page-locked arrays (hrt_host_alloc, cudaHostAlloc,
  * cudaHostRegister) at a 16-byte boundary are used where they are: the
  * traversal reads their rays over the host link and writes its results
- * straight into them.  Other host memory is copied in and out; such batches
+ * straight into them.  On devices that translate through the host's page
+ * tables (Grace-based systems) pageable rays are read in place too.  Other
+ * host memory is copied in and out; such batches
  * above 2^18 rays run as chunks whose copies overlap the traversal of other
  * chunks.  The device-pointer calls above want rays (and hits) at a 16-byte
  * boundary and return HRT_ERR_INVALID_ARGUMENT otherwise. */
