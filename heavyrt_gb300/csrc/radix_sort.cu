@@ -256,11 +256,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint32_t* __rest
 
 }  // namespace
 
-size_t radix_sort_scratch_bytes(uint32_t n)
+// Scratch of a four-pass sort of n pairs: digit histograms, pass counters,
+// and one look-back status word per tile and digit for every pass.
+constexpr size_t sort_scratch_bytes(size_t n)
 {
-  const size_t tiles = (n + kTile - 1) / kTile;
-  return sizeof(uint32_t) * (kPasses * kRadix + kPasses + 4 + (size_t)kPasses * tiles * kRadix);
+  return sizeof(uint32_t) *
+         (kPasses * kRadix + kPasses + 4 + (size_t)kPasses * ((n + kTile - 1) / kTile) * kRadix);
 }
+
+size_t radix_sort_scratch_bytes(uint32_t n) { return sort_scratch_bytes(n); }
 
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keysAlt, uint32_t* valsAlt, uint32_t n,
                              void* scratch, uint32_t* errorWord, int numSMs, cudaStream_t stream)
@@ -357,15 +361,15 @@ cudaError_t radix_sort_pairs_segmented(uint32_t* keys, uint32_t* vals, uint32_t*
 // ---------------------------------------------------------------------------
 // Allocation-free variant of the pair sort (hrt_sort_morton_pairs_noalloc).
 //
-// Some callers cannot call cudaMalloc: code that records work inside a CUDA
-// stream capture (allocation calls are not allowed while a capture is active),
-// host applications whose device memory is owned by another allocator that
-// reserves it up front, and latency-bound paths that cannot afford the
-// implicit synchronisation of an allocation.  For them this entry point takes
-// its scratch (ping-pong arrays, digit histograms, look-back tile status and
-// an error word) from one file-scope device array of fixed size, so it calls
-// no allocator at all.  The array is part of the library image: every GPU that
-// loads the library holds kNoAllocScratchBytes of it until the process exits.
+// Some callers cannot call cudaMalloc: host applications whose device memory
+// is owned by another allocator that reserves it up front (a renderer or a
+// game engine with its own heap, a process under a hard device-memory quota),
+// and latency-bound paths that cannot afford the implicit synchronisation of
+// an allocation.  For them this entry point takes its scratch (ping-pong
+// arrays, digit histograms, look-back tile status and an error word) from one
+// file-scope device array of fixed size, so it calls no allocator at all.
+// The array is part of the library image: every GPU that loads the library
+// holds kNoAllocScratchBytes of it until the process exits.
 #include <mutex>
 
 #include "../../include/hrt.h"
@@ -375,7 +379,9 @@ namespace
 
 constexpr uint32_t kNoAllocMaxPairs  = HRT_NOALLOC_MAX_PAIRS;
 constexpr uint32_t kNoAllocTiles     = (kNoAllocMaxPairs + hrt::kTileSize - 1) / hrt::kTileSize;
-constexpr size_t   kNoAllocSortBytes = sizeof(uint32_t) * (4 * 256 + 4 + 4 + (size_t)4 * kNoAllocTiles * 256);
+constexpr size_t   kNoAllocSortBytes = hrt::sort_scratch_bytes(kNoAllocMaxPairs);
+static_assert(kNoAllocSortBytes == sizeof(uint32_t) * (4 * 256 + 4 + 4 + (size_t)4 * kNoAllocTiles * 256),
+              "the fixed array holds the scratch of a sort of HRT_NOALLOC_MAX_PAIRS pairs");
 constexpr size_t   kNoAllocPingPong  = sizeof(uint32_t) * (size_t)kNoAllocMaxPairs;  // one array
 constexpr size_t   kNoAllocScratchBytes = 2 * kNoAllocPingPong + kNoAllocSortBytes + 256;
 constexpr int      kNoAllocMaxDevices = 64;
@@ -402,7 +408,9 @@ extern "C" int hrt_sort_morton_pairs_noalloc(uint32_t* keys, uint32_t* vals, uin
   int numSMs = 0;
   {
     // One-time set-up per device, with that device current: resolve the
-    // device address of the scratch array.
+    // device address of the scratch array.  The address is kept for the life
+    // of the process, so the entry point must not be used on a device after
+    // cudaDeviceReset (or any other teardown of its primary context).
     std::lock_guard<std::mutex> lk(g_noallocMu);
     if (!g_noallocPtr[dev])
     {

@@ -198,10 +198,14 @@ int hrt_query_any_host(hrt_scene* scene, const float* rays, uint64_t n, uint8_t*
 
 /* The host-pointer queries, enqueued on `stream` instead of waited for: the
  * results are in place once the stream has reached them.  Page-locked arrays
- * are used in place as above; other memory goes through stream-ordered device
- * allocations (a pageable result array makes the final copy synchronous).
- * Queries on different streams overlap, e.g. one batch's result copy with the
- * next batch's traversal.  The arrays must stay valid until the stream is done. */
+ * are used in place as above, and so are pageable rays on devices that
+ * translate through the host's page tables (Grace-based systems): there the
+ * traversal reads the caller's ray array while the stream runs, so its
+ * contents must not change until the stream is done.  Other memory goes
+ * through stream-ordered device allocations (a pageable result array makes
+ * the final copy synchronous).  Queries on different streams overlap, e.g.
+ * one batch's result copy with the next batch's traversal.  The arrays must
+ * stay valid until the stream is done. */
 int hrt_query_nearest_host_async(hrt_scene* scene, const float* rays, uint64_t n, hrt_hit* hits, void* stream);
 int hrt_query_any_host_async(hrt_scene* scene, const float* rays, uint64_t n, uint8_t* out, void* stream);
 
@@ -554,9 +558,10 @@ int hrt_host_free(void* p);
 /* Stable sort of (Morton code, triangle id) pairs by code -- the LBVH build's
  * radix sort -- that allocates nothing.  No counterpart in the reference.
  *
- * For callers that cannot call cudaMalloc: work recorded inside a CUDA stream
- * capture, host applications whose device memory is owned by another
- * allocator, and latency-bound paths that cannot take an allocation's implicit
+ * For callers that cannot call cudaMalloc: host applications whose device
+ * memory is owned by another allocator that reserves it up front (a renderer
+ * or engine with its own device heap, a process under a hard memory quota),
+ * and latency-bound paths that cannot take an allocation's implicit
  * synchronisation.  keys and vals are device arrays of n entries (input and
  * output, sorted in place); all scratch comes from one fixed device array that
  * the library holds on every GPU that loads it (about 2.4 MB) until the process
@@ -565,10 +570,12 @@ int hrt_host_free(void* p);
  * Runs on the calling thread's current device and on `stream`, and returns
  * after the stream has finished the sort (HRT_ERR_TIMEOUT if a device wait gave
  * up).  The first call on a device resolves the scratch array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture
- * begins.  Every call shares the one array, so calls whose work overlaps on
- * the GPU race with each other: serialise them (one stream, or wait between
- * calls). */
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any stream
+ * capture begins, and do not use the function on a device after
+ * cudaDeviceReset.  Every call shares the one array, which keeps the last
+ * call's contents (the call clears what must start at zero), so calls whose
+ * work overlaps on the GPU race with each other: serialise them (one stream,
+ * or wait between calls). */
 #define HRT_NOALLOC_MAX_PAIRS (1u << 18)
 int hrt_sort_morton_pairs_noalloc(uint32_t* keys, uint32_t* vals, uint64_t n, void* stream);
 
