@@ -87,6 +87,8 @@ def parse():
                    help="only K builds of the headline scene (the launch list of the build)")
     p.add_argument("--only-build-batched", type=int, default=0, metavar="K",
                    help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
+    p.add_argument("--no-oracle-check", action="store_true",
+                   help="skip the check of every ray of the headline frame against the oracle")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     p.add_argument("--only-served", action="store_true",
                    help="run only the served-stream measurement (prints its JSON object)")
@@ -478,116 +480,113 @@ def t_error_fp64(rays, hits, verts_all, sorted_idx_all, prim_base):
 
 
 def run_precision(ctx, args) -> dict:
-    """Heightfield (1024 x 1024 quads) plus an 8,388,608-triangle soup
-    (offsets +-0.005) as two instances; 1920 x 1080 eye rays and 16 AO rays per
-    primary hit.  Every layout traces the same rays; nearest hits of the
-    quantised layouts are compared with the FP32-node build (BVH4 FP32, same
-    tree) and the binary FP32 tree, any-hit flags with both, and the hit
-    distance with an FP64 evaluation on 1M sampled eye rays."""
+    """Quantised-node precision, each scene traced separately as configured:
+    the 2,097,152-triangle heightfield and the 8,388,608-triangle soup, each
+    with 1920 x 1080 eye rays that all hit and 16 AO rays per hit (~33M).
+    Every layout traces the same rays: the binary FP32 tree (the reference's
+    decisions), BVH4 with FP32 boxes, FP16 boxes and 8-bit offsets.  Nearest
+    hits of the quantised layouts are compared with the FP32-node build (same
+    tree) and with the binary tree, any-hit flags with both, and the hit
+    distance with an FP64 evaluation on 1M sampled eye rays per scene."""
     import torch
 
     from heavyrt_gb300 import SceneRT
     from heavyrt_gb300 import engine as E
     from heavyrt_gb300 import workload as wl
 
-    w = wl.config1(args.nx, args.width, args.height)
-    sv, sidx = wl.soup(0x5EED0006, args.soup_tris, -1.0, 1.0, 0.005)
-    geoms = [(w.verts, w.idx), (sv, sidx)]
-    n_h = len(w.idx) // 3
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     layouts = [("bvh2", None), ("bvh4", 1), ("bvh4_f16", 1), ("bvh4_q8", 1)]
-    res = {"workload": f"heightfield{args.nx}x{args.nx} + soup{args.soup_tris} (2 instances), eye {args.width}x"
-                       f"{args.height} + 16 AO per hit", "tris": int(n_h + len(sidx) // 3)}
-    d_eye = torch.from_numpy(w.eye_rays).cuda()
-    n_eye = len(w.eye_rays)
-    ref_hits = ref_any = ao = d_ao = None
-    out = {}
-    for layout, merge in layouts:
-        sc = SceneRT(ctx, layout=layout)
-        if merge is not None:
-            sc.set_bvh4_merge(merge)
-        gids = [sc.AddGeom_Triangles3f(v, len(v), i, i.size, vByteStride=16) for v, i in geoms]
-        for g in gids:
+    res = {"note": "mismatch = different hit distance (must be 0); equal_t_other_triangle = a tie between triangles "
+                   "at the same t, resolved by visit order", "scenes": {}}
+    for scene_name in ("heightfield", "soup"):
+        w = wl.config2(scene_name, args.width, args.height, args.soup_tris)
+        d_eye = torch.from_numpy(w.eye_rays).cuda()
+        n_eye = len(w.eye_rays)
+        ref_hits = ref_any = ao = d_ao = None
+        out = {}
+        sc_res = {"workload": w.name, "tris": int(w.params["tris"])}
+        for layout, merge in layouts:
+            sc = SceneRT(ctx, layout=layout)
+            if merge is not None:
+                sc.set_bvh4_merge(merge)
+            g = sc.AddGeom_Triangles3f(w.verts, len(w.verts), w.idx, w.idx.size, vByteStride=16)
             sc.AddInstance(g)
-        sc.CommitScene()
-        build_ms = sum(sc.geom_info(g)["build_ms"] for g in gids)
-        d_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
-        sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
-        torch.cuda.synchronize()
-        hits = d_hits.cpu().numpy().view(np.uint32)
-        if ao is None:
-            # AO rays from the binary FP32 tree's primary hits (same input for every layout)
-            si = [sc.export(g, E.EXPORT_SORTED_INDICES) for g in gids]
-            verts_all = np.concatenate([geoms[0][0], geoms[1][0]])
-            si_all = np.concatenate([si[0], si[1] + len(geoms[0][0])]).astype(np.uint32)
-            prim_base = np.array([0, n_h], dtype=np.int64)
-            hh = hits.copy()
-            m = hh[:, 1] != 0xFFFFFFFF
-            hh[m, 1] = hh[m, 1] + prim_base[hh[m, 3]].astype(np.uint32)
-            p = w.params
-            ao, _ = wl.ao_rays(p["ao_seed"], w.eye_rays, hh.view(np.float32), verts_all, si_all, p["ao_per_hit"],
-                               p["ao_length"], p["ao_offset"])
-            d_ao = torch.from_numpy(ao).cuda()
-            rng = np.random.default_rng(7)
-            sample = np.sort(rng.choice(n_eye, size=min(1000000, n_eye), replace=False))
-            res["t_error_vs_fp64"] = t_error_fp64(w.eye_rays[sample], hits[sample], verts_all, si_all, prim_base)
-        n_ao = len(ao)
-        d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
-        for k in range(3):
+            sc.CommitScene()
+            build_ms = sc.geom_info(g)["build_ms"]
+            d_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
             sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
-            sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
-        torch.cuda.synchronize()
-        steps = 10
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        t_eye = t_ao = 0.0
-        for _ in range(steps):
-            e[0].record(stream)
-            sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
-            e[1].record(stream)
-            sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
-            e[2].record(stream)
             torch.cuda.synchronize()
-            t_eye += e[0].elapsed_time(e[1])
-            t_ao += e[1].elapsed_time(e[2])
-        t_eye /= steps
-        t_ao /= steps
-        anyf = d_any.cpu().numpy()
-        pairs_eye, _ = sc.query_counters(0, d_eye.data_ptr(), n_eye, sh)
-        pairs_ao, tris_ao = sc.query_counters(1, d_ao.data_ptr(), n_ao, sh)
-        ao_bytes = LAYOUT_NODE_BYTES[layout] * pairs_ao + TRI_BYTES * tris_ao + (RAY_BYTES + 1) * n_ao
-        pk, _ = measured_peak()
-        entry = {"eye_ms": round(t_eye, 4), "ao_ms": round(t_ao, 4),
-                 "mrays_s": round((n_eye + n_ao) / (t_eye + t_ao) / 1e3, 2), "build_ms": round(build_ms, 3),
-                 "node_fetches_per_eye_ray": round(pairs_eye / n_eye, 3),
-                 "node_fetches_per_ao_ray": round(pairs_ao / n_ao, 3),
-                 "ao_roofline_frac": round(ao_bytes / (t_ao * 1e-3) / 1e9 / pk, 4),
-                 "bvh_bytes": int(sum(sc.geom_info(g)["bytes"] for g in gids))}
-        if ref_hits is None:
-            ref_hits, ref_any = hits, anyf
-        else:
-            diff = np.any(hits != ref_hits, axis=1)
-            same_t = hits[:, 0] == ref_hits[:, 0]
-            entry["nearest_mismatch_vs_bvh2"] = int(np.count_nonzero(diff & ~same_t))
-            entry["nearest_equal_t_other_triangle_vs_bvh2"] = int(np.count_nonzero(diff & same_t))
-            entry["anyhit_mismatch_vs_bvh2"] = int(np.count_nonzero(anyf != ref_any))
-            if layout != "bvh4":
-                f32 = out["bvh4"]["_hits"]
-                d32 = np.any(hits != f32, axis=1)
-                entry["nearest_mismatch_vs_fp32_nodes"] = int(np.count_nonzero(d32 & (hits[:, 0] != f32[:, 0])))
-                entry["nearest_equal_t_other_triangle_vs_fp32_nodes"] = int(
-                    np.count_nonzero(d32 & (hits[:, 0] == f32[:, 0])))
-        entry["_hits"] = hits
-        out[layout] = entry
-        sc.close()
-        del d_hits, d_any
-    for k in out:
-        out[k].pop("_hits")
-    res["eye_rays"] = n_eye
-    res["ao_rays"] = int(len(ao))
-    res["layouts"] = out
-    res["note"] = ("mismatch = different hit distance (must be 0); equal_t_other_triangle = a tie between triangles "
-                   "at the same t, resolved by visit order")
+            hits = d_hits.cpu().numpy().view(np.uint32)
+            if ao is None:
+                # AO rays from the binary FP32 tree's primary hits (same input for every layout)
+                si = sc.export(g, E.EXPORT_SORTED_INDICES)
+                ao = wl.frame_ao_rays(w, hits.view(np.float32), si)
+                d_ao = torch.from_numpy(ao).cuda()
+                rng = np.random.default_rng(7)
+                sample = np.sort(rng.choice(n_eye, size=min(1000000, n_eye), replace=False))
+                sc_res["t_error_vs_fp64"] = t_error_fp64(w.eye_rays[sample], hits[sample], w.verts,
+                                                         si.astype(np.uint32), np.zeros(1, np.int64))
+            n_ao = len(ao)
+            d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
+            for _ in range(3):
+                sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+                sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+            torch.cuda.synchronize()
+            steps = 10
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            t_eye = t_ao = 0.0
+            for _ in range(steps):
+                e[0].record(stream)
+                sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+                e[1].record(stream)
+                sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+                e[2].record(stream)
+                torch.cuda.synchronize()
+                t_eye += e[0].elapsed_time(e[1])
+                t_ao += e[1].elapsed_time(e[2])
+            t_eye /= steps
+            t_ao /= steps
+            anyf = d_any.cpu().numpy()
+            pairs_eye, _ = sc.query_counters(0, d_eye.data_ptr(), n_eye, sh)
+            pairs_ao, tris_ao = sc.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+            ao_bytes = LAYOUT_NODE_BYTES[layout] * pairs_ao + TRI_BYTES * tris_ao + (RAY_BYTES + 1) * n_ao
+            pk, _ = measured_peak()
+            entry = {"eye_ms": round(t_eye, 4), "ao_ms": round(t_ao, 4),
+                     "mrays_s": round((n_eye + n_ao) / (t_eye + t_ao) / 1e3, 2), "build_ms": round(build_ms, 3),
+                     "node_fetches_per_eye_ray": round(pairs_eye / n_eye, 3),
+                     "node_fetches_per_ao_ray": round(pairs_ao / n_ao, 3),
+                     "ao_roofline_frac": round(ao_bytes / (t_ao * 1e-3) / 1e9 / pk, 4),
+                     "bvh_bytes": int(sc.geom_info(g)["bytes"])}
+            if ref_hits is None:
+                ref_hits, ref_any = hits, anyf
+            else:
+                diff = np.any(hits != ref_hits, axis=1)
+                same_t = hits[:, 0] == ref_hits[:, 0]
+                entry["nearest_mismatch_vs_bvh2"] = int(np.count_nonzero(diff & ~same_t))
+                entry["nearest_equal_t_other_triangle_vs_bvh2"] = int(np.count_nonzero(diff & same_t))
+                entry["anyhit_mismatch_vs_bvh2"] = int(np.count_nonzero(anyf != ref_any))
+                if layout != "bvh4":
+                    f32 = out["bvh4"]["_hits"]
+                    d32 = np.any(hits != f32, axis=1)
+                    entry["nearest_mismatch_vs_fp32_nodes"] = int(np.count_nonzero(d32 & (hits[:, 0] != f32[:, 0])))
+                    entry["nearest_equal_t_other_triangle_vs_fp32_nodes"] = int(
+                        np.count_nonzero(d32 & (hits[:, 0] == f32[:, 0])))
+                    entry["anyhit_mismatch_vs_fp32_nodes"] = int(np.count_nonzero(anyf != out["bvh4"]["_any"]))
+            entry["_hits"] = hits
+            entry["_any"] = anyf
+            out[layout] = entry
+            sc.close()
+            del d_hits, d_any
+        for k in out:
+            out[k].pop("_hits")
+            out[k].pop("_any")
+        sc_res["eye_rays"] = n_eye
+        sc_res["ao_rays"] = int(len(ao))
+        sc_res["layouts"] = out
+        res["scenes"][scene_name] = sc_res
+        del d_eye, d_ao
+        torch.cuda.empty_cache()
     return res
 
 
@@ -1257,21 +1256,66 @@ def run_engine(args):
         line["gpu_launches_batched_per_step"] = 2
     if not args.no_precision:
         line["precision"] = run_precision(ctx, args)
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not (args.no_cpu_baseline and args.no_oracle_check):
         from oracle import oracle as orc
 
         o = orc.OracleBVH(w.verts, w.idx)
-        rate, used, sample = cpu_trace_rate(o, w.eye_rays, ao, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": round(rate, 3), "unit": UNIT, "cores": int(used), "kind": "port",
-                                "sample": sample, "cpu": host_cpu()}
-        # the frame's any-hit flags from the e2e leg agree with the oracle on the sample rows
-        step_ao = max(1, n_ao // 20000)
-        want = o.trace(ao[::step_ao], any_hit=True)
-        line["config"]["e2e_anyhit_matches_oracle_sample"] = bool(np.array_equal(got_any[::step_ao].astype(bool), want))
+        if not args.no_cpu_baseline:
+            rate, used, sample = cpu_trace_rate(o, w.eye_rays, ao, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": round(rate, 3), "unit": UNIT, "cores": int(used), "kind": "port",
+                                    "sample": sample, "cpu": host_cpu()}
+        if not args.no_oracle_check:
+            # every ray of the frame against the oracle (after the timed region):
+            # the timed layout's device-resident eye hits and AO flags, and the
+            # AO flags the e2e leg wrote into host memory
+            want = o.trace(w.eye_rays).view(np.uint32).reshape(-1, 8)
+            want_any = o.trace(ao, any_hit=True)
+            got = d_hits.cpu().numpy().view(np.uint32)
+            diff = np.any(got != want, axis=1)
+            same_t = got[:, 0] == want[:, 0]
+            cfg = line["config"]
+            cfg["oracle_checked_rays"] = int(n_eye + n_ao)
+            cfg["oracle_nearest_mismatch"] = int(np.count_nonzero(diff & ~same_t))
+            cfg["oracle_nearest_equal_t_other_triangle"] = int(np.count_nonzero(diff & same_t))
+            cfg["oracle_anyhit_mismatch"] = int(np.count_nonzero(d_any.cpu().numpy().astype(bool) != want_any))
+            cfg["oracle_e2e_anyhit_mismatch"] = int(np.count_nonzero(got_any.astype(bool) != want_any))
+    summarize(line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     replicas.finish(rk)
     return 0
+
+
+def summarize(line: dict):
+    """Scalar copies of the sections' key figures in the line's config (the
+    part of the line that record keepers keep whole)."""
+    cfg = line["config"]
+    if "plain" in line:
+        cfg["plain_mrays_s"] = line["plain"]["mrays_s"]
+    if "served" in line:
+        sv, pl = line["served"]["served"], line["served"]["plain"]
+        for k in ("p50_ms", "p99_ms", "max_ms", "mrays_s"):
+            cfg[f"served_{k}"] = sv[k]
+            cfg[f"served_plain_{k}"] = pl[k]
+        cfg["served_mean_requests_per_batch"] = sv["mean_requests_per_batch"]
+        cfg["served_engine_p99_ms"] = sv["engine_p99_ms"]
+    if "batched" in line:
+        b = line["batched"]
+        for k in ("batched_mrays_s", "plain_mrays_s", "speedup", "results_equal_plain"):
+            if k in b:
+                cfg[f"batched_{k}" if not k.startswith("batched_") else k] = b[k]
+    if "precision" in line:
+        bad = 0
+        for name, sc in line["precision"]["scenes"].items():
+            cfg[f"c2_{name}_t_max_rel_vs_fp64"] = sc["t_error_vs_fp64"]["max_rel"]
+            for lay, e in sc["layouts"].items():
+                cfg[f"c2_{name}_{lay}_mrays_s"] = e["mrays_s"]
+                bad += sum(v for k, v in e.items() if "mismatch" in k)
+        cfg["c2_hit_mismatches"] = int(bad)
+    if "frames" in line:
+        cfg["frames_rtao_mrays_s"] = line["frames"]["rtao"]["mrays_s"]
+        cfg["frames_rtao_ms"] = line["frames"]["rtao"]["ms_per_frame"]
+        cfg["frames_eye_mrays_s"] = line["frames"]["eye"]["mrays_s"]
 
 
 def main():

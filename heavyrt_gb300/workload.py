@@ -10,6 +10,11 @@ its eye-ray and RTAO renderers' inputs):
            eye rays 1920 x 1080 from (0,-2.5,1.5) at the origin (60 deg, +z up),
            16 cosine-weighted AO rays per primary hit, length 0.1 x scene
            diagonal, origin offset 1e-4 along the normal, any-hit.
+  config2: two scenes traced separately, each with 2M eye rays that all hit
+           and 16 AO rays per hit (33,177,600): the config1 heightfield seen
+           from (0,0,2) straight down (30 deg), and an 8,388,608-triangle soup
+           (vertex offsets U[-0.005,0.005]^3) seen from (0,0,3) (30 deg).
+  config3: 256 soups of log-uniform size, see config3().
 """
 from __future__ import annotations
 
@@ -191,6 +196,41 @@ def config1(nx: int = 1024, width: int = 1920, height: int = 1080) -> Workload:
                     {"tris": 2 * nx * nx, "width": width, "height": height, "seed": SEED_HEIGHTFIELD,
                      "ao_per_hit": 16, "ao_length": 0.1 * diag, "ao_offset": 1e-4, "ao_seed": SEED_AO,
                      "heightfield_params": hp.tolist()})
+
+
+SEED_SOUP_8M = 0x5EED0006
+
+
+def config2(scene: str, width: int = 1920, height: int = 1080, soup_tris: int = 8388608) -> Workload:
+    """One scene of the quantised-node precision configuration: "heightfield"
+    (config1's mesh) or "soup" (soup_tris triangles, offsets +-0.005).  The
+    30-degree cameras keep every eye ray on the mesh, so 16 AO rays per hit
+    make 16 x width x height AO rays."""
+    if scene == "heightfield":
+        v, idx, _ = heightfield(SEED_HEIGHTFIELD, 1024, 1024)
+        eye, name = (0.0, 0.0, 2.0), "heightfield1024x1024"
+    elif scene == "soup":
+        v, idx = soup(SEED_SOUP_8M, soup_tris, -1.0, 1.0, 0.005)
+        eye, name = (0.0, 0.0, 3.0), f"soup{soup_tris}"
+    else:
+        raise ValueError(scene)
+    rays = camera_rays(eye, (0, 0, 0), (0, 1, 0), 30.0, width, height, 0.0, 1e9)
+    lo = v[:, :3].min(axis=0)
+    hi = v[:, :3].max(axis=0)
+    diag = float(np.linalg.norm(hi.astype(np.float64) - lo.astype(np.float64)))
+    return Workload(f"{name}_eye{width}x{height}_ao16", v, idx, rays,
+                    {"tris": int(idx.size // 3), "width": width, "height": height, "eye": list(eye), "fov": 30.0,
+                     "ao_per_hit": 16, "ao_length": 0.1 * diag, "ao_offset": 1e-4, "ao_seed": SEED_AO})
+
+
+def frame_ao_rays(w: Workload, hits: np.ndarray, sorted_idx: np.ndarray):
+    """The AO rays of a workload's frame from its eye hits (CRT_Hit records of
+    a one-instance scene, sorted-order primIds) and the geometry's sorted index
+    buffer."""
+    p = w.params
+    ao, _ = ao_rays(p["ao_seed"], w.eye_rays, hits, w.verts, sorted_idx, p["ao_per_hit"], p["ao_length"],
+                    p["ao_offset"])
+    return ao
 
 
 def log_uniform_counts(seed: int, stream: int, n: int, lo: int, hi: int) -> np.ndarray:
