@@ -453,6 +453,21 @@ def run_batched(ctx, args, tune: bool = True) -> dict:
 
 # ---------------------------------------------------------------- quantised nodes
 
+def hit_diff(hits, ref, name: str) -> dict:
+    """Nearest-hit records (uint32 [n, 8]) against a reference set: mismatches
+    (hit/miss differs, or t beyond 1e-5 relative: must be 0), ties resolved to
+    another triangle (t within 1e-5 relative), and how many of those have the
+    same t bit for bit."""
+    diff = np.any(hits != ref, axis=1)
+    hm = (hits[:, 3] != 0xFFFFFFFF) != (ref[:, 3] != 0xFFFFFFFF)
+    tg = hits[:, 0].view(np.float32).astype(np.float64)
+    tr = ref[:, 0].view(np.float32).astype(np.float64)
+    near = np.abs(tg - tr) <= 1e-5 * np.abs(tr)
+    return {f"nearest_mismatch_vs_{name}": int(np.count_nonzero(diff & (hm | ~near))),
+            f"nearest_tie_vs_{name}": int(np.count_nonzero(diff & ~hm & near)),
+            f"nearest_tie_exact_t_vs_{name}": int(np.count_nonzero(diff & ~hm & (hits[:, 0] == ref[:, 0])))}
+
+
 def t_error_fp64(rays, hits, verts_all, sorted_idx_all, prim_base):
     """Relative error of the FP32 hit distance against the same ray-triangle
     intersection evaluated in FP64 (host), over the rays that hit."""
@@ -497,8 +512,8 @@ def run_precision(ctx, args) -> dict:
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     layouts = [("bvh2", None), ("bvh4", 1), ("bvh4_f16", 1), ("bvh4_q8", 1)]
-    res = {"note": "mismatch = different hit distance (must be 0); equal_t_other_triangle = a tie between triangles "
-                   "at the same t, resolved by visit order", "scenes": {}}
+    res = {"note": "mismatch = hit/miss differs or t differs by more than 1e-5 relative (must be 0); tie = another "
+                   "triangle at a t within 1e-5 relative (exact = the same t), resolved by visit order", "scenes": {}}
     for scene_name in ("heightfield", "soup"):
         w = wl.config2(scene_name, args.width, args.height, args.soup_tris)
         d_eye = torch.from_numpy(w.eye_rays).cuda()
@@ -561,17 +576,10 @@ def run_precision(ctx, args) -> dict:
             if ref_hits is None:
                 ref_hits, ref_any = hits, anyf
             else:
-                diff = np.any(hits != ref_hits, axis=1)
-                same_t = hits[:, 0] == ref_hits[:, 0]
-                entry["nearest_mismatch_vs_bvh2"] = int(np.count_nonzero(diff & ~same_t))
-                entry["nearest_equal_t_other_triangle_vs_bvh2"] = int(np.count_nonzero(diff & same_t))
+                entry.update(hit_diff(hits, ref_hits, "bvh2"))
                 entry["anyhit_mismatch_vs_bvh2"] = int(np.count_nonzero(anyf != ref_any))
                 if layout != "bvh4":
-                    f32 = out["bvh4"]["_hits"]
-                    d32 = np.any(hits != f32, axis=1)
-                    entry["nearest_mismatch_vs_fp32_nodes"] = int(np.count_nonzero(d32 & (hits[:, 0] != f32[:, 0])))
-                    entry["nearest_equal_t_other_triangle_vs_fp32_nodes"] = int(
-                        np.count_nonzero(d32 & (hits[:, 0] == f32[:, 0])))
+                    entry.update(hit_diff(hits, out["bvh4"]["_hits"], "fp32_nodes"))
                     entry["anyhit_mismatch_vs_fp32_nodes"] = int(np.count_nonzero(anyf != out["bvh4"]["_any"]))
             entry["_hits"] = hits
             entry["_any"] = anyf
@@ -1153,11 +1161,9 @@ def run_engine(args):
         pa_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in pe)
         hp = p_hits.cpu().numpy().view(np.uint32)
         hq = d_hits.cpu().numpy().view(np.uint32)
-        diff = np.any(hp != hq, axis=1)
         plain = {"layout": LAYOUT_DESC["bvh2"], "eye_ms": round(pe_ms, 4), "ao_ms": round(pa_ms, 4),
                  "mrays_s": round((n_eye + n_ao) / (pe_ms + pa_ms) / 1e3, 2),
-                 "nearest_mismatch": int(np.count_nonzero(diff & (hp[:, 0] != hq[:, 0]))),
-                 "nearest_equal_t_other_triangle": int(np.count_nonzero(diff & (hp[:, 0] == hq[:, 0]))),
+                 **hit_diff(hq, hp, "plain"),
                  "anyhit_mismatch": int(np.count_nonzero(p_any.cpu().numpy() != d_any.cpu().numpy()))}
         if not args.ncu:
             pp_eye, pt_eye = ps.query_counters(0, d_eye.data_ptr(), n_eye, sh)
@@ -1271,12 +1277,11 @@ def run_engine(args):
             want = o.trace(w.eye_rays).view(np.uint32).reshape(-1, 8)
             want_any = o.trace(ao, any_hit=True)
             got = d_hits.cpu().numpy().view(np.uint32)
-            diff = np.any(got != want, axis=1)
-            same_t = got[:, 0] == want[:, 0]
             cfg = line["config"]
             cfg["oracle_checked_rays"] = int(n_eye + n_ao)
-            cfg["oracle_nearest_mismatch"] = int(np.count_nonzero(diff & ~same_t))
-            cfg["oracle_nearest_equal_t_other_triangle"] = int(np.count_nonzero(diff & same_t))
+            dd = hit_diff(got, want, "oracle")
+            cfg["oracle_nearest_mismatch"] = dd["nearest_mismatch_vs_oracle"]
+            cfg["oracle_nearest_tie"] = dd["nearest_tie_vs_oracle"]
             cfg["oracle_anyhit_mismatch"] = int(np.count_nonzero(d_any.cpu().numpy().astype(bool) != want_any))
             cfg["oracle_e2e_anyhit_mismatch"] = int(np.count_nonzero(got_any.astype(bool) != want_any))
     summarize(line)

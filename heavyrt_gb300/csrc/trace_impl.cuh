@@ -23,8 +23,14 @@
 // the schedule.  A one-thread-per-ray grid is kept as a configuration.
 //
 // Memory: a child pair is one 64-byte record (four 128-bit read-only loads), a
-// triangle one 48-byte record (three); the short stack lives in shared memory,
-// interleaved by thread so a warp's pushes and pops hit 32 different banks.
+// triangle one 48-byte record (three).  The stack's first S entries live in
+// shared memory, interleaved by thread so a warp's pushes and pops hit 32
+// different banks; deeper entries spill to a per-thread array in local memory
+// (S is a launch parameter, full depth by default, so no entry spills).
+//
+// Triangle test: the reference's Moller-Trumbore (records {A, B-A, C-A}), or,
+// for scenes built for it, the watertight test of Woop, Benthin & Wald
+// (records {A, B, C}); both are template variants of the same kernels.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -52,6 +58,28 @@ template <int LAYOUT, bool TLAS = false> struct StackDepth
 };
 
 constexpr uint32_t kTlasMode = 0xFFFFFFFEu;  // Lane::inst while the lane walks the instance tree
+
+// A lane's traversal stack: entries below `shared` in shared memory (entry k
+// of thread t at sh[k * THREADS]), the rest in the lane's spill array.
+template <int THREADS> struct Stack
+{
+  uint32_t* sh;
+  uint32_t* spill;  // DEPTH - shared entries (local memory)
+  int       shared;
+  __device__ __forceinline__ void put(int k, uint32_t v)
+  {
+    if (k < shared) sh[k * THREADS] = v;
+    else spill[k - shared] = v;
+  }
+  __device__ __forceinline__ uint32_t get(int k) const { return k < shared ? sh[k * THREADS] : spill[k - shared]; }
+};
+
+// Shared-memory entries per lane for a requested short-stack size (0 or
+// anything at or above the depth bound: the whole stack).
+template <int DEPTH> __host__ __device__ __forceinline__ int shared_entries(int requested)
+{
+  return (requested <= 0 || requested >= DEPTH) ? DEPTH : requested;
+}
 
 // Instance tree (TLAS): a binary LBVH over the instances' world-space boxes,
 // built like a geometry's tree from one pseudo-triangle per instance; a leaf
@@ -200,6 +228,112 @@ __device__ __forceinline__ bool leaf_test(const TriRec* __restrict__ tris, uint3
     if (__float_as_uint(A.w) & ENDBIT) return false;  // last triangle of the leaf
     j++;
   }
+}
+
+// ------------------------------------------------------- watertight triangle test
+// Woop, Benthin & Wald, "Watertight Ray/Triangle Intersection", JCGT 2(1),
+// 2013: the ray's dominant axis becomes z (kx, ky keep the winding), the
+// triangle is translated to the ray origin and sheared so that the ray runs
+// along +z, and the signs of the three 2D edge functions at the origin decide
+// the hit (both windings accepted).  The paper re-evaluates an edge function
+// in double precision when it comes out zero; here each one is Kahan's
+// difference of products (the rounding error of one product recovered by an
+// FMA), whose relative error stays below 2 ulp, so its sign is exact in FP32
+// and the test needs no FP64.  An edge shared by two triangles then gets
+// exactly opposite signs on both sides: no ray passes between them.  Records
+// hold the vertices {A, B, C} (w: flags, triangle id, 0).  Outputs match the
+// Moller-Trumbore fields: u = the weight of C, v = the weight of B.
+struct WtRay
+{
+  int   kx, ky, kz;
+  float sx, sy, sz;
+};
+
+__device__ __forceinline__ float pick3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ void wt_setup(const Ray& r, WtRay& w)
+{
+  const float ax = fabsf(r.dx), ay = fabsf(r.dy), az = fabsf(r.dz);
+  w.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+  w.kx = w.kz == 2 ? 0 : w.kz + 1;
+  w.ky = w.kx == 2 ? 0 : w.kx + 1;
+  const float dz = pick3(r.dx, r.dy, r.dz, w.kz);
+  if (dz < 0.0f)
+  {
+    const int t = w.kx;
+    w.kx = w.ky;
+    w.ky = t;
+  }
+  w.sx = __fdiv_rn(pick3(r.dx, r.dy, r.dz, w.kx), dz);
+  w.sy = __fdiv_rn(pick3(r.dx, r.dy, r.dz, w.ky), dz);
+  w.sz = __fdiv_rn(1.0f, dz);
+}
+
+// a*b - c*d with the rounding error of c*d restored (Kahan).
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d)
+{
+  const float w = __fmul_rn(c, d);
+  const float e = __fmaf_rn(-c, d, w);
+  const float f = __fmaf_rn(a, b, -w);
+  return __fadd_rn(f, e);
+}
+
+template <bool ANY, bool COUNT, uint32_t ENDBIT = 1u>
+__device__ __forceinline__ bool leaf_test_wt(const TriRec* __restrict__ tris, uint32_t j, const Ray& r, Hit& h,
+                                             uint32_t instIndex, uint64_t& nTris)
+{
+  WtRay w;
+  wt_setup(r, w);
+  while (true)
+  {
+    const float4* q = reinterpret_cast<const float4*>(tris + j);
+    const float4 A = __ldg(q + 0);
+    const float4 B = __ldg(q + 1);
+    const float4 Cv = __ldg(q + 2);
+    if (COUNT) nTris++;
+    const float a0 = __fsub_rn(A.x, r.ox), a1 = __fsub_rn(A.y, r.oy), a2 = __fsub_rn(A.z, r.oz);
+    const float b0 = __fsub_rn(B.x, r.ox), b1 = __fsub_rn(B.y, r.oy), b2 = __fsub_rn(B.z, r.oz);
+    const float c0 = __fsub_rn(Cv.x, r.ox), c1 = __fsub_rn(Cv.y, r.oy), c2 = __fsub_rn(Cv.z, r.oz);
+    const float az = pick3(a0, a1, a2, w.kz), bz = pick3(b0, b1, b2, w.kz), cz = pick3(c0, c1, c2, w.kz);
+    const float ax = __fsub_rn(pick3(a0, a1, a2, w.kx), __fmul_rn(w.sx, az));
+    const float ay = __fsub_rn(pick3(a0, a1, a2, w.ky), __fmul_rn(w.sy, az));
+    const float bx = __fsub_rn(pick3(b0, b1, b2, w.kx), __fmul_rn(w.sx, bz));
+    const float by = __fsub_rn(pick3(b0, b1, b2, w.ky), __fmul_rn(w.sy, bz));
+    const float cx = __fsub_rn(pick3(c0, c1, c2, w.kx), __fmul_rn(w.sx, cz));
+    const float cy = __fsub_rn(pick3(c0, c1, c2, w.ky), __fmul_rn(w.sy, cz));
+    const float U = diff_of_products(cx, by, cy, bx);
+    const float V = diff_of_products(ax, cy, ay, cx);
+    const float W = diff_of_products(bx, ay, by, ax);
+    const bool outside = (U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f);
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (!outside && det != 0.0f)
+    {
+      const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, __fmul_rn(w.sz, az)), __fmul_rn(V, __fmul_rn(w.sz, bz))),
+                                __fmul_rn(W, __fmul_rn(w.sz, cz)));
+      const float inv = __fdiv_rn(1.0f, det);
+      const float t = __fmul_rn(T, inv);
+      if (t > r.tNear && t < h.t)
+      {
+        h.t = t;
+        h.u = __fmul_rn(W, inv);
+        h.v = __fmul_rn(V, inv);
+        h.prim = j;
+        h.inst = instIndex;
+        if (ANY) return true;
+      }
+    }
+    if (__float_as_uint(A.w) & ENDBIT) return false;  // last triangle of the leaf
+    j++;
+  }
+}
+
+// The scene's triangle test: 0 Moller-Trumbore (the reference's), 1 watertight.
+template <int TRI, bool ANY, bool COUNT, uint32_t ENDBIT>
+__device__ __forceinline__ bool test_leaf(const TriRec* __restrict__ tris, uint32_t j, const Ray& r, Hit& h,
+                                          uint32_t instIndex, uint64_t& nTris)
+{
+  if constexpr (TRI == 1) return leaf_test_wt<ANY, COUNT, ENDBIT>(tris, j, r, h, instIndex, nTris);
+  else return leaf_test<ANY, COUNT, ENDBIT>(tris, j, r, h, instIndex, nTris);
 }
 
 // ---------------------------------------------------------------- 4-wide nodes

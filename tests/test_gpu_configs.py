@@ -16,8 +16,9 @@ core/builders/lbvh.cpp, core/BVH2CommonRT.cpp:9-141), through the C ABI:
 
 Integer results are bit-exact.  The binary layout makes the reference's
 decisions, so its hits equal the oracle's bit for bit.  The 4-wide layouts
-visit children in another order: hit/miss and t are bit-exact, and a
-different triangle is allowed only where it has the same t (a tie)."""
+visit children in another order: hit/miss is exact, any-hit flags are exact,
+and a different triangle is allowed only at a tie within 1e-5 relative t
+(see _compare_nearest)."""
 import numpy as np
 import pytest
 
@@ -54,15 +55,25 @@ def _trace_device(s, kind, rays):
 
 def _compare_nearest(got, want, layout):
     """got: uint32 [n, 8] hit records; want: the oracle's hits.  Returns the
-    number of ties resolved to another triangle."""
+    number of near ties resolved to another triangle.
+
+    The binary layout is bit-exact.  A 4-wide layout visits children in
+    another order, and its quantised boxes are larger: it may test a triangle
+    that the reference's order pruned, and the reference's 1e-6 barycentric
+    slack accepts hit points slightly outside a triangle's box, so such a
+    triangle can give a t one rounding below the reference's.  There the
+    tolerance is the stated one: the same triangle gives the same record bit
+    for bit, another triangle only at a tie within 1e-5 relative t."""
     w = np.ascontiguousarray(want).view(np.uint32).reshape(-1, 8)
     if layout == "bvh2":
         np.testing.assert_array_equal(got, w)
         return 0
     np.testing.assert_array_equal(got[:, 3] != MISS, w[:, 3] != MISS)
-    np.testing.assert_array_equal(got[:, 0], w[:, 0])  # t, bit for bit
     same = got[:, 1] == w[:, 1]
     np.testing.assert_array_equal(got[same], w[same])
+    tg = got[~same, 0].view(np.float32).astype(np.float64)
+    tw = w[~same, 0].view(np.float32).astype(np.float64)
+    assert np.all(np.abs(tg - tw) <= 1e-5 * np.abs(tw)), (tg, tw)
     ties = int(np.count_nonzero(~same))
     assert ties <= max(2, got.shape[0] // 100000), ties
     return ties
