@@ -87,6 +87,7 @@ def parse():
                    help="only K builds of the headline scene (the launch list of the build)")
     p.add_argument("--only-build-batched", type=int, default=0, metavar="K",
                    help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
+    p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
     p.add_argument("--no-oracle-check", action="store_true",
                    help="skip the check of every ray of the headline frame against the oracle")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
@@ -596,6 +597,94 @@ def run_precision(ctx, args) -> dict:
         del d_eye, d_ao
         torch.cuda.empty_cache()
     return res
+
+
+def edge_distance64(rays, verts, sorted_idx, prim):
+    """Smallest FP64 barycentric of each ray against the triangle at sorted
+    position prim (negative: outside): the ray's distance to the triangle's
+    nearest edge in barycentric units."""
+    v = np.asarray(verts, np.float64)[:, :3]
+    t = np.asarray(sorted_idx, np.int64).reshape(-1, 3)[np.asarray(prim, np.int64)]
+    a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+    o, d = rays[:, 0:3].astype(np.float64), rays[:, 4:7].astype(np.float64)
+    e1, e2 = b - a, c - a
+    pv = np.cross(d, e2)
+    det = np.einsum("ij,ij->i", e1, pv)
+    sv = o - a
+    qv = np.cross(sv, e1)
+    wb = np.einsum("ij,ij->i", sv, pv) / det
+    wc = np.einsum("ij,ij->i", d, qv) / det
+    return np.minimum(np.minimum(wb, wc), 1.0 - wb - wc)
+
+
+def run_watertight(ctx, args, w, ao, mt_hits, mt_any, configs) -> dict:
+    """The headline frame with the watertight triangle test (same layout,
+    merge bound and launch shapes): its speed, and every ray whose result
+    differs from the reference's MT test (hit/miss, or another triangle),
+    classified by the ray's FP64 distance to the nearest edge of the triangle
+    either test hit (barycentric units; MT accepts down to -1e-6)."""
+    import torch
+
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import engine as E
+
+    sc = SceneRT(ctx, layout=args.layout, triangle_test=E.TRI_WATERTIGHT)
+    if args.layout != "bvh2":
+        sc.set_bvh4_merge(args.merge)
+    g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+    sc.AddInstance(g)
+    sc.CommitScene()
+    for k in (0, 1):
+        sc.set_trace_config(k, **configs[k])
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    n_eye, n_ao = len(w.eye_rays), len(ao)
+    d_eye = torch.from_numpy(w.eye_rays).cuda()
+    d_ao = torch.from_numpy(ao).cuda()
+    d_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
+    d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+        sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    steps = max(5, min(50, args.steps))
+    e[0].record(stream)
+    for _ in range(steps):
+        sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+    e[1].record(stream)
+    for _ in range(steps):
+        sc.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+    e[2].record(stream)
+    torch.cuda.synchronize()
+    eye_ms, ao_ms = e[0].elapsed_time(e[1]) / steps, e[1].elapsed_time(e[2]) / steps
+    si = sc.export(g, E.EXPORT_SORTED_INDICES)
+    wt = d_hits.cpu().numpy().view(np.uint32)
+    wt_any = d_any.cpu().numpy().astype(bool)
+    sc.close()
+    hm, hw = mt_hits[:, 3] != 0xFFFFFFFF, wt[:, 3] != 0xFFFFFFFF
+    differ = (hm != hw) | (hm & hw & (mt_hits[:, 1] != wt[:, 1]))
+    idx = np.nonzero(differ)[0]
+    dist = np.full(idx.size, np.inf)
+    for hits, has in ((mt_hits, hm), (wt, hw)):
+        m = has[idx]
+        if m.any():
+            dd = np.abs(edge_distance64(w.eye_rays[idx[m]], w.verts, si, hits[idx[m], 1]))
+            dist[m] = np.minimum(dist[m], dd)
+    bins = {"le_1e-7": int(np.count_nonzero(dist <= 1e-7)),
+            "le_1e-6": int(np.count_nonzero((dist > 1e-7) & (dist <= 1e-6))),
+            "le_1e-5": int(np.count_nonzero((dist > 1e-6) & (dist <= 1e-5))),
+            "gt_1e-5": int(np.count_nonzero(dist > 1e-5))}
+    same = hm & hw & (mt_hits[:, 1] == wt[:, 1])
+    tm = mt_hits[same, 0].view(np.float32).astype(np.float64)
+    tw = wt[same, 0].view(np.float32).astype(np.float64)
+    return {"layout": args.layout, "eye_ms": round(eye_ms, 4), "ao_ms": round(ao_ms, 4),
+            "mrays_s": round((n_eye + n_ao) / (eye_ms + ao_ms) / 1e3, 2),
+            "eye_rays_differing_from_mt": int(idx.size), "eye_hits_mt": int(hm.sum()), "eye_hits_wt": int(hw.sum()),
+            "differing_by_edge_distance": bins,
+            "same_triangle_t_max_rel_vs_mt": float((np.abs(tm - tw) / np.abs(tm)).max()) if tm.size else 0.0,
+            "ao_rays_differing_from_mt": int(np.count_nonzero(wt_any != mt_any)),
+            "note": "edge distance = smallest FP64 barycentric (abs) of the ray against the triangle either test hit"}
 
 
 # ---------------------------------------------------------------- served stream
@@ -1249,6 +1338,10 @@ def run_engine(args):
         line["plain"] = plain
         line["speedup_vs_plain"] = round(line["value"] / plain["mrays_s"], 3)
 
+    if not args.no_watertight:
+        line["watertight"] = run_watertight(ctx, args, w, ao, d_hits.cpu().numpy().view(np.uint32),
+                                            d_any.cpu().numpy().astype(bool),
+                                            {k: scene.trace_config(k) for k in (0, 1)})
     if not args.no_frames:
         line["frames"] = run_frames(ctx, args, w, {k: scene.trace_config(k) for k in (0, 1)})
     # the served stream runs before the 256-scene batched measurement: on these
@@ -1317,6 +1410,12 @@ def summarize(line: dict):
                 cfg[f"c2_{name}_{lay}_mrays_s"] = e["mrays_s"]
                 bad += sum(v for k, v in e.items() if "mismatch" in k)
         cfg["c2_hit_mismatches"] = int(bad)
+    if "watertight" in line:
+        wt = line["watertight"]
+        cfg["watertight_mrays_s"] = wt["mrays_s"]
+        cfg["watertight_eye_rays_differing_from_mt"] = wt["eye_rays_differing_from_mt"]
+        cfg["watertight_differing_beyond_1e-5_of_an_edge"] = wt["differing_by_edge_distance"]["gt_1e-5"]
+        cfg["watertight_ao_rays_differing_from_mt"] = wt["ao_rays_differing_from_mt"]
     if "frames" in line:
         cfg["frames_rtao_mrays_s"] = line["frames"]["rtao"]["mrays_s"]
         cfg["frames_rtao_ms"] = line["frames"]["rtao"]["ms_per_frame"]

@@ -9,9 +9,9 @@ launch shape tuned per query kind, and the structure with the lowest summed
 query time kept.  Results never depend on the choice (the traversal makes the
 reference's decisions in every layout); only speed does.
 
-Stack depth is not a tuning knob: it is fixed per layout by the depth bound
-of a tree over 30-bit Morton codes (32 entries for BVH2, 48 for BVH4), so no
-ray can overflow it.
+The launch shape includes the short stack's size: the entries a ray keeps in
+shared memory (16..64; deeper entries spill to local memory, so every size is
+correct for every tree), tuned by the engine after the block shape.
 """
 from __future__ import annotations
 
@@ -32,7 +32,8 @@ class TuneResult:
     merge: int | None
     configs: dict                       # kind -> launch config
     ms: dict                            # kind -> mean ms of one query
-    table: list = field(default_factory=list)  # every candidate: (layout, merge, ms nearest, ms any)
+    # every candidate: (layout, merge, ms nearest, ms any, stack entries nearest, stack entries any)
+    table: list = field(default_factory=list)
 
 
 def build_batch(ctx, verts, idx, layout: str, merge):
@@ -58,7 +59,8 @@ def tune_batch(ctx, verts, idx, d_rays, n_rays: int, d_offsets, d_seg_inst, n_se
         for kind, out in ((0, d_hits), (1, d_any)):
             desc = E.query_desc(kind, d_rays, n_rays, out, d_offsets, d_seg_inst, n_seg)
             cfgs[kind], ms[kind] = scene.autotune(desc, repeats)
-        table.append((layout, merge, round(ms[0], 4), round(ms[1], 4)))
+        table.append((layout, merge, round(ms[0], 4), round(ms[1], 4), cfgs[0]["stackEntries"],
+                      cfgs[1]["stackEntries"]))
         if best is None or ms[0] + ms[1] < best.ms[0] + best.ms[1]:
             best = TuneResult(layout, merge, cfgs, ms)
         scene.close()
@@ -69,7 +71,8 @@ def tune_batch(ctx, verts, idx, d_rays, n_rays: int, d_offsets, d_seg_inst, n_se
 def apply(scene: E.SceneRT, result: TuneResult):
     """Sets a tuned launch shape on a scene built with result's structure."""
     for kind, c in result.configs.items():
-        scene.set_trace_config(kind, c["threadsPerBlock"], c["persistent"], c["stepsPerRefill"], c["refillLanes"])
+        scene.set_trace_config(kind, c["threadsPerBlock"], c["persistent"], c["stepsPerRefill"], c["refillLanes"],
+                               c["stackEntries"])
 
 
 def seg_inst_identity(n: int) -> np.ndarray:

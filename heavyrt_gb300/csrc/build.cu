@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(kThreads) k_leaves(const float4* __restrict__ 
                                                      const uint32_t* __restrict__ runStarts, uint32_t nTris,
                                                      uint32_t nVerts, const BuildParams* __restrict__ params,
                                                      BVHNode32* __restrict__ lr, TriRec* __restrict__ tris,
-                                                     uint32_t* __restrict__ sortedIdx, uint32_t* errorWord)
+                                                     uint32_t* __restrict__ sortedIdx, uint32_t* errorWord,
+                                                     int vertexRecords)
 {
   const uint32_t L = params->nLeaves <= nTris ? params->nLeaves : 0u;
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < L; i += gridDim.x * kThreads)
@@ -178,6 +179,12 @@ __global__ void __launch_bounds__(kThreads) k_leaves(const float4* __restrict__ 
       r.a = make_float4(a.x, a.y, a.z, __uint_as_float(j + 1 == end ? 3u : 0u));
       r.e1 = make_float4(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z), __uint_as_float(tri));
       r.e2 = make_float4(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z), 0.0f);
+      if (vertexRecords)
+      {
+        // the watertight test wants the vertices themselves
+        r.e1 = make_float4(b.x, b.y, b.z, __uint_as_float(tri));
+        r.e2 = make_float4(c.x, c.y, c.z, 0.0f);
+      }
       tris[j] = r;
       sortedIdx[3 * (size_t)j + 0] = ia;
       sortedIdx[3 * (size_t)j + 1] = ib;
@@ -399,7 +406,8 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
                                                           b.params, err);
   // 5. leaves, 6. hierarchy, 7. refit, 8. records
   const uint32_t g = grid_for(N, numSMs, 8);
-  k_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vals, b.runStarts, N, b.nVerts, b.params, b.lr, b.tris, b.sortedIdx, err);
+  k_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vals, b.runStarts, N, b.nVerts, b.params, b.lr, b.tris, b.sortedIdx, err,
+                                  b.vertexRecords);
   e = cudaMemsetAsync(b.parent, 0xFF, sizeof(uint32_t) * (2 * (size_t)N - 1), s);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);
@@ -430,7 +438,7 @@ cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, c
   k_box_final<<<1, kThreads, 0, s>>>(partial, pb, boxOut);
   const uint32_t g = grid_for(N, numSMs, 8);
   k_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vals, b.runStarts, N, b.nVerts, b.params, b.lr, b.tris, b.sortedIdx,
-                                  err);
+                                  err, b.vertexRecords);
   cudaError_t e = cudaMemsetAsync(b.parent, 0xFF, sizeof(uint32_t) * (2 * (size_t)N - 1), s);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(b.visit, 0, sizeof(uint32_t) * N, s);

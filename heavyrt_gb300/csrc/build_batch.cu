@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kThreads) k_seg_leaves(
     const uint32_t* __restrict__ nodeOffsets, const uint32_t* __restrict__ recOffsets, uint32_t G,
     const uint32_t* __restrict__ counts, const uint32_t* __restrict__ sortedTri, const uint32_t* __restrict__ runStarts,
     BVHNode32* __restrict__ lr, uint32_t* __restrict__ lrCount, TriRec* __restrict__ tris,
-    uint32_t* __restrict__ sortedIdx, PairRec* __restrict__ recs, uint32_t* errorWord)
+    uint32_t* __restrict__ sortedIdx, PairRec* __restrict__ recs, uint32_t* errorWord, int vertexRecords)
 {
   const uint32_t Ltot = counts[0];
   for (uint32_t g = blockIdx.x * kThreads + threadIdx.x; g < Ltot; g += gridDim.x * kThreads)
@@ -256,6 +256,11 @@ __global__ void __launch_bounds__(kThreads) k_seg_leaves(
       r.a = make_float4(a.x, a.y, a.z, __uint_as_float(j + 1 == end ? 3u : 0u));
       r.e1 = make_float4(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z), __uint_as_float(tri - tb));
       r.e2 = make_float4(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z), 0.0f);
+      if (vertexRecords)
+      {
+        r.e1 = make_float4(b.x, b.y, b.z, __uint_as_float(tri - tb));
+        r.e2 = make_float4(c.x, c.y, c.z, 0.0f);
+      }
       tris[j] = r;
       sortedIdx[3 * (size_t)j + 0] = ia;
       sortedIdx[3 * (size_t)j + 1] = ib;
@@ -495,7 +500,7 @@ cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t s)
   if (e != cudaSuccess) return e;
   k_seg_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vertOffsets, b.triOffsets, b.leafOffsets, b.nodeOffsets,
                                       b.recOffsets, G, b.counts, b.vals, b.runStarts, b.lr, b.lrCount, b.tris,
-                                      b.sortedIdx, b.recs, b.errorWord);
+                                      b.sortedIdx, b.recs, b.errorWord, b.vertexRecords);
   k_seg_karras<<<g, kThreads, 0, s>>>(b.compressed, b.leafOffsets, b.intOffsets, b.nodeOffsets, G, b.counts, b.lr,
                                       b.parent, b.visit + N);
   k_seg_refit<<<(N + bc::kRefitSlice - 1) / bc::kRefitSlice, bc::kRefitThreads, 0, s>>>(

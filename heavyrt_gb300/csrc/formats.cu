@@ -165,7 +165,7 @@ int hrt_geom_save(const hrt_scene* s, uint32_t geomId, const char* path)
   Geom g = s->geoms[geomId];
   BlobHeader h;
   std::memcpy(h.magic, kBlobMagic, 8);
-  h.layout = (uint32_t)s->layout;
+  h.layout = (uint32_t)s->layout | ((uint32_t)g.triTest << 8);  // triangle-record form in bits 8..15
   h.merge = (uint32_t)g.bvh4Merge;
   h.nTris = g.nTris;
   h.nVerts = g.nVerts;
@@ -200,7 +200,10 @@ int hrt_geom_load(hrt_scene* s, const char* path, uint32_t* geomId)
   if (std::memcmp(h.magic, kBlobMagic, 8) != 0)
     return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "BVH blob of another format version: rebuild the geometry");
   std::lock_guard<std::mutex> lk(s->mu);
+  const int triTest = (int)(h.layout >> 8);
+  h.layout &= 0xFFu;
   if ((int)h.layout != s->layout) return fail(ctx, HRT_ERR_STATE, "the blob was built for another node layout");
+  if (triTest != s->triTest) return fail(ctx, HRT_ERR_STATE, "the blob was built for another triangle test");
   if (h.nTris > HRT_MAX_TRIS_PER_GEOM || h.nLeaves > h.nTris || (h.nTris && !h.nLeaves) ||
       (h.layout != HRT_LAYOUT_BVH2 && h.nTris && !h.nNodes4))
     return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "inconsistent BVH blob header");
@@ -211,6 +214,7 @@ int hrt_geom_load(hrt_scene* s, const char* path, uint32_t* geomId)
   g.nLeaves = h.nLeaves;
   g.nNodes4 = h.nNodes4;
   g.bvh4Merge = (int)h.merge;
+  g.triTest = triTest;
   g.host = h.params;
   for (int c = 0; c < 4; c++)
   {

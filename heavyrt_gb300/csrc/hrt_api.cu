@@ -126,12 +126,13 @@ bool is_identity(const float* m)
 }
 
 int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
-                   uint64_t stride, int layout)
+                   uint64_t stride, int layout, int triTest)
 {
   hrt_context* ctx = s->ctx;
   cudaStream_t st = ctx->stream;
   const uint32_t N = (uint32_t)(nIdx / 3);
   g.nTris = N;
+  g.triTest = triTest;
   g.nVerts = (uint32_t)nVert;
   uint64_t* bytes = &g.bytes;
   HRT_CUDA(ctx, dalloc(&g.verts, nVert, bytes, st));
@@ -209,6 +210,7 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   b.sortedIdx = g.sortedIdx;
   b.params = g.params;
   b.scratch = scratch;
+  b.vertexRecords = triTest == HRT_TRI_WATERTIGHT;
 
   cudaEvent_t e0, e1;
   HRT_CUDA(ctx, cudaEventCreate(&e0));
@@ -327,6 +329,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   b.triOffsets = dTOff;
   b.G = G;
   b.nTris = (uint32_t)N;
+  b.vertexRecords = s->triTest == HRT_TRI_WATERTIGHT;
   // scene-box chunks of each geometry's vertices
   std::vector<uint32_t> hChunk(G + 1, 0);
   for (uint32_t i = 0; i < G; i++) hChunk[i + 1] = hChunk[i] + (hv[i + 1] - hv[i] + kBatchBoxChunk - 1) / kBatchBoxChunk;
@@ -475,6 +478,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
     const uint32_t Li = hLeaf[i + 1] - hLeaf[i];
     g.shared = true;
     g.bvh4Merge = s->bvh4Merge;
+    g.triTest = s->triTest;
     g.nTris = Ni;
     g.nVerts = hv[i + 1] - hv[i];
     g.nLeaves = Li;
@@ -667,6 +671,7 @@ int refit_geometry(hrt_scene* s, Geom& g, const float* vpos, const uint32_t* idx
   b.sortedIdx = g.sortedIdx;
   b.params = g.params;
   b.scratch = scratch;
+  b.vertexRecords = g.triTest == HRT_TRI_WATERTIGHT;
   cudaEvent_t e0, e1;
   HRT_CUDA(ctx, cudaEventCreate(&e0));
   HRT_CUDA(ctx, cudaEventCreate(&e1));
@@ -819,6 +824,7 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
     a.tlasTris = s->tlas.tris;
   }
   if (s->single && !q.rayOffsets) a.one = &s->singleDesc;
+  a.triTest = s->triTest;
   cudaError_t e = trace(a, kind, counting, s->layout, q.config ? *q.config : s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
@@ -968,7 +974,7 @@ int hrt_add_geom_triangles3f(hrt_scene* s, const float* vpos, uint64_t nVert, co
   std::lock_guard<std::mutex> lk(s->mu);
   cudaSetDevice(ctx->device);
   Geom g;
-  const int st = build_geometry(s, g, vpos, nVert, idx, nIdx, vByteStride, s->layout);
+  const int st = build_geometry(s, g, vpos, nVert, idx, nIdx, vByteStride, s->layout, s->triTest);
   if (st != HRT_OK)
   {
     cudaStreamSynchronize(ctx->stream);
@@ -1054,7 +1060,7 @@ int hrt_update_geom_triangles3f(hrt_scene* s, uint32_t geomId, const float* vpos
     if (g.shared)
       return fail(ctx, HRT_ERR_UNSUPPORTED, "a batch-built geometry can only be refit (BUILD_REFIT)");
     Geom ng;
-    st = build_geometry(s, ng, vpos, nVert, idx, nIdx, vByteStride, s->layout);
+    st = build_geometry(s, ng, vpos, nVert, idx, nIdx, vByteStride, s->layout, s->triTest);
     cudaStreamSynchronize(ctx->stream);
     if (st == HRT_OK)
     {
@@ -1475,6 +1481,13 @@ int hrt_scene_set_option(hrt_scene* s, int option, int value)
       s->useTlas = value;
       s->committed = false;
       return HRT_OK;
+    case HRT_OPTION_TRIANGLE_TEST:
+      if (value != HRT_TRI_MOLLER_TRUMBORE && value != HRT_TRI_WATERTIGHT)
+        return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown triangle test");
+      if (!s->geoms.empty())
+        return fail(s->ctx, HRT_ERR_STATE, "the triangle test is chosen before the first geometry is added");
+      s->triTest = value;
+      return HRT_OK;
     default: return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }
@@ -1491,13 +1504,14 @@ int hrt_scene_set_trace_config(hrt_scene* s, int kind, const hrt_trace_config* c
   if (!s || !c || (kind != 0 && kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
   if ((c->threadsPerBlock != 64 && c->threadsPerBlock != 128 && c->threadsPerBlock != 256) ||
       (c->persistent != 0 && c->persistent != 1) || c->stepsPerRefill < 1 || c->stepsPerRefill > 1024 ||
-      c->refillLanes < 1 || c->refillLanes > 32)
+      c->refillLanes < 1 || c->refillLanes > 32 || c->stackEntries < 0 || c->stackEntries > HRT_MAX_STACK_ENTRIES)
     return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "trace config out of range");
   std::lock_guard<std::mutex> g(s->mu);
   s->cfg[kind].threadsPerBlock = c->threadsPerBlock;
   s->cfg[kind].persistent = c->persistent;
   s->cfg[kind].stepsPerRefill = c->stepsPerRefill;
   s->cfg[kind].refillLanes = c->refillLanes;
+  s->cfg[kind].stackEntries = c->stackEntries;
   return HRT_OK;
 }
 
@@ -1508,6 +1522,7 @@ int hrt_scene_get_trace_config(const hrt_scene* s, int kind, hrt_trace_config* c
   c->persistent = s->cfg[kind].persistent;
   c->stepsPerRefill = s->cfg[kind].stepsPerRefill;
   c->refillLanes = s->cfg[kind].refillLanes;
+  c->stackEntries = s->cfg[kind].stackEntries;
   return HRT_OK;
 }
 
@@ -1660,6 +1675,38 @@ int hrt_scene_autotune(hrt_scene* s, const hrt_query_desc* q, int repeats, hrt_t
       bestC = c;
     }
   }
+  // second stage: the short stack's size under the best launch shape
+  // (entries beyond it spill to local memory; 64 covers every depth bound of
+  // a single-level tree)
+  if (st == HRT_OK)
+  {
+    const TraceConfig shape = bestC;
+    for (int entries : {16, 24, 32, 48, 64})
+    {
+      TraceConfig c = shape;
+      c.stackEntries = entries;
+      s->cfg[q->kind] = c;
+      st = launch_query(s, q->kind, q->rays, q->n, q->out, 0, cs, sg);  // warm-up
+      if (st != HRT_OK) break;
+      cudaEventRecord(e0, cs);
+      for (int r = 0; r < repeats && st == HRT_OK; r++) st = launch_query(s, q->kind, q->rays, q->n, q->out, 0, cs, sg);
+      cudaEventRecord(e1, cs);
+      if (st != HRT_OK) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess)
+      {
+        st = cuda_fail(ctx, cudaGetLastError(), "autotune timing");
+        break;
+      }
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= (float)repeats;
+      if (ms < bestT)
+      {
+        bestT = ms;
+        bestC = c;
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   s->cfg[q->kind] = (st == HRT_OK) ? bestC : saved;
@@ -1677,6 +1724,7 @@ int hrt_scene_autotune(hrt_scene* s, const hrt_query_desc* q, int repeats, hrt_t
     best->persistent = bestC.persistent;
     best->stepsPerRefill = bestC.stepsPerRefill;
     best->refillLanes = bestC.refillLanes;
+    best->stackEntries = bestC.stackEntries;
   }
   if (bestMs) *bestMs = bestT;
   return HRT_OK;

@@ -50,6 +50,7 @@ struct Geom
   uint32_t     nNodes4 = 0;
   bool         shared = false;    // arrays point into a batch allocation (hrt_add_geoms_triangles3f_batched)
   int          bvh4Merge = 0;     // leaf merge bound the 4-wide nodes were built with
+  int          triTest = 0;       // triangle records for HRT_TRI_* (1: vertices, for the watertight test)
 };
 
 struct Instance
@@ -77,6 +78,7 @@ struct hrt_scene
   int                   layout = HRT_LAYOUT_BVH2;
   int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
   int                   useTlas = 1;    // HRT_OPTION_TLAS
+  int                   triTest = 0;    // HRT_OPTION_TRIANGLE_TEST
   Geom                  tlas;           // instance tree of the committed scene (nTris = 0: none)
   InstanceDesc*         dInst = nullptr;
   uint32_t              nInstDev = 0;
@@ -114,7 +116,7 @@ void free_geom(Geom& g);
 // s->ctx->stream from host or device arrays; synchronous.  The scene supplies the
 // context and the BVH4 merge option; it is not modified.
 int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, const uint32_t* idx, uint64_t nIdx,
-                   uint64_t stride, int layout);
+                   uint64_t stride, int layout, int triTest = HRT_TRI_MOLLER_TRUMBORE);
 // Traversal view of a geometry under an instance transform (inv12: rows 0..2
 // of the inverse; identity when null).
 void make_instance_desc(const Geom& g, uint32_t geomId, uint32_t instId, const float* inv12, InstanceDesc& d);

@@ -51,6 +51,7 @@ struct BuildBuffers
   uint32_t*  sortedIdx;       // 3*nTris
   BuildParams* params;        // device
   void*      scratch;         // build_scratch_bytes(nTris)
+  int        vertexRecords = 0;  // 1: triangle records hold {A, B, C} (watertight test), else {A, B-A, C-A}
 };
 size_t build_scratch_bytes(uint32_t nTris);
 // Runs the whole LBVH build asynchronously on `stream`.  Errors found on the
@@ -109,6 +110,7 @@ struct BatchBuffers
   const uint32_t* boxChunkOffsets;  // G+1 (device)
   uint32_t        nBoxChunks;
   float4*         boxPartial;       // 2 * nBoxChunks
+  int             vertexRecords = 0;  // as BuildBuffers::vertexRecords
 };
 constexpr uint32_t kBatchBoxChunk = 8192;
 size_t build_batch_scratch_bytes(uint32_t nTris, uint32_t G);
@@ -198,6 +200,9 @@ struct TraceArgs
   // host copy of the descriptor when the scene is one valid instance under the
   // identity transform (the single-instance kernel), else null
   const InstanceDesc* one = nullptr;
+  // triangle test of every geometry traced: 0 Moller-Trumbore (records
+  // {A, B-A, C-A}), 1 watertight (records {A, B, C})
+  int                 triTest = 0;
 };
 
 // Launch shape of the traversal (tuned per workload).
@@ -207,6 +212,8 @@ struct TraceConfig
   int persistent = 1;         // 1: persistent warp pool with lane refill; 0: one thread per ray
   int stepsPerRefill = 16;    // traversal steps between refill checks
   int refillLanes = 24;       // a warp refills when at least this many lanes are idle
+  int stackEntries = 0;       // stack entries per lane in shared memory, the rest in local
+                              // memory; 0 (or at least the depth bound): all in shared memory
 };
 
 // kind 0: nearest, 1: any.  counting = 1 also accumulates counters (node

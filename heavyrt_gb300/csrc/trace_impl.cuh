@@ -495,7 +495,7 @@ template <int LAYOUT> struct EndBit
 // One child pair of a binary tree: BVH2TraverseC32's decisions
 // (core/BVH2CommonRT.cpp:88-113).
 template <bool COUNT, int THREADS, int DEPTH, typename LaneT>
-__device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ recs, uint32_t* __restrict__ stack,
+__device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ recs, Stack<THREADS>& st,
                                           uint64_t& nPairs, uint32_t* errorWord)
 {
   const float4* p = reinterpret_cast<const float4*>(recs + L.cur);
@@ -520,14 +520,14 @@ __device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ 
       atomicOr(errorWord, kErrStack);
       return -1;
     }
-    stack[L.top * THREADS] = first0 ? e.y : e.x;
+    st.put(L.top, first0 ? e.y : e.x);
     L.top++;
   }
   return 0;
 }
 
 template <int LAYOUT, bool ANY, bool COUNT, int THREADS, int DEPTH, typename LaneT>
-__device__ __forceinline__ int visit_node(LaneT& L, uint32_t* __restrict__ stack, uint64_t& nPairs, uint32_t* errorWord)
+__device__ __forceinline__ int visit_node(LaneT& L, Stack<THREADS>& st, uint64_t& nPairs, uint32_t* errorWord)
 {
   if constexpr (LAYOUT != 0)
   {
@@ -563,7 +563,7 @@ __device__ __forceinline__ int visit_node(LaneT& L, uint32_t* __restrict__ stack
             atomicOr(errorWord, kErrStack);
             return -1;
           }
-          stack[L.top * THREADS] = first;
+          st.put(L.top, first);
           L.top++;
         }
         first = ref[k];
@@ -590,13 +590,13 @@ __device__ __forceinline__ int visit_node(LaneT& L, uint32_t* __restrict__ stack
           atomicOr(errorWord, kErrStack);
           return -1;
         }
-        stack[L.top * THREADS] = ref[k];
+        st.put(L.top, ref[k]);
         L.top++;
       }
     return 0;
   }
   else
-    return visit_pair<COUNT, THREADS, DEPTH>(L, reinterpret_cast<const PairRec*>(L.nodes), stack, nPairs, errorWord);
+    return visit_pair<COUNT, THREADS, DEPTH>(L, reinterpret_cast<const PairRec*>(L.nodes), st, nPairs, errorWord);
 }
 
 // One traversal step (an internal node, or a leaf followed by a pop).
@@ -624,11 +624,11 @@ __device__ __forceinline__ void tlas_begin(Lane& L)
 
 // Pops the instance tree's stack; true when the ray is finished.
 template <int THREADS>
-__device__ __forceinline__ bool tlas_pop(Lane& L, const uint32_t* __restrict__ stack)
+__device__ __forceinline__ bool tlas_pop(Lane& L, const Stack<THREADS>& st)
 {
   if (L.top == 0) return true;
   L.top--;
-  L.cur = stack[L.top * THREADS];
+  L.cur = st.get(L.top);
   return false;
 }
 
@@ -636,7 +636,7 @@ __device__ __forceinline__ bool tlas_pop(Lane& L, const uint32_t* __restrict__ s
 // the run is done, returns to the instance tree.  True when the ray is finished.
 template <int LAYOUT, int THREADS>
 __device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
-                                          const uint32_t* __restrict__ stack)
+                                          const Stack<THREADS>& st)
 {
   while (L.tnext != kNoRay)
   {
@@ -653,13 +653,12 @@ __device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restric
   }
   L.inst = kTlasMode;
   world_ray(L);
-  return tlas_pop<THREADS>(L, stack);
+  return tlas_pop<THREADS>(L, st);
 }
 
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
 __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
-                                     uint32_t* __restrict__ stack, uint64_t& nPairs, uint64_t& nTris,
-                                     uint32_t* errorWord)
+                                     Stack<THREADS>& st, uint64_t& nPairs, uint64_t& nTris, uint32_t* errorWord)
 {
   constexpr int DEPTH = StackDepth<LAYOUT, TLAS>::value;
   if (TLAS && L.inst == kTlasMode)
@@ -667,25 +666,25 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
     // instance tree: a pair of instance boxes, or a leaf (a run of instances)
     if ((L.cur & kLeafBit) == 0u)
     {
-      const int r = visit_pair<COUNT, THREADS, DEPTH>(L, tl.recs, stack, nPairs, errorWord);
+      const int r = visit_pair<COUNT, THREADS, DEPTH>(L, tl.recs, st, nPairs, errorWord);
       if (r < 0) return true;
-      return r == 1 ? tlas_pop<THREADS>(L, stack) : false;
+      return r == 1 ? tlas_pop<THREADS>(L, st) : false;
     }
-    if (L.cur == kEmptyRef) return tlas_pop<THREADS>(L, stack);
+    if (L.cur == kEmptyRef) return tlas_pop<THREADS>(L, st);
     L.tnext = L.cur & ~kLeafBit;
-    return tlas_next<LAYOUT, THREADS>(L, inst, tl, stack);
+    return tlas_next<LAYOUT, THREADS>(L, inst, tl, st);
   }
   bool pop;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, ANY, COUNT, THREADS, DEPTH>(L, stack, nPairs, errorWord);
+    const int r = visit_node<LAYOUT, ANY, COUNT, THREADS, DEPTH>(L, st, nPairs, errorWord);
     if (r < 0) return true;
     pop = (r == 1);
   }
   else
   {
     if (L.cur != kEmptyRef &&
-        leaf_test<ANY, COUNT, EndBit<LAYOUT>::value>(L.tris, L.cur & ~kLeafBit, L.r, L.h, L.inst, nTris))
+        test_leaf<TRI, ANY, COUNT, EndBit<LAYOUT>::value>(L.tris, L.cur & ~kLeafBit, L.r, L.h, L.inst, nTris))
       return true;  // any-hit found
     pop = true;
   }
@@ -694,10 +693,10 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
     if (L.top > L.base)
     {
       L.top--;
-      L.cur = stack[L.top * THREADS];
+      L.cur = st.get(L.top);
       return false;
     }
-    if (TLAS) return tlas_next<LAYOUT, THREADS>(L, inst, tl, stack);
+    if (TLAS) return tlas_next<LAYOUT, THREADS>(L, inst, tl, st);
     return !begin_instance<LAYOUT>(L, inst, L.inst + 1);
   }
   return false;
@@ -781,14 +780,16 @@ __device__ __forceinline__ void flush_counters(uint64_t nPairs, uint64_t nTris, 
 
 // Persistent warp pool.  Lanes run `steps` traversal steps between refills; a
 // warp refills when at least `refill` lanes are idle (or all are).
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
 __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict__ rays, uint32_t n,
                                                         const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
                                                         void* out, unsigned long long* counters, uint32_t* errorWord,
-                                                        unsigned int* rayCounter, int steps, int refill)
+                                                        unsigned int* rayCounter, int steps, int refill,
+                                                        int stackShared)
 {
-  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT, TLAS>::value * THREADS entries
-  uint32_t* stack = s_stack + threadIdx.x;
+  extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
+  uint32_t spill[StackDepth<LAYOUT, TLAS>::value];
+  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ltMask = (1u << lane) - 1u;
   uint64_t nPairs = 0, nTris = 0;
@@ -827,7 +828,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
       for (int s = 0; s < steps; s++)
       {
         if (out_of_budget(L, errorWord) ||
-            step<LAYOUT, ANY, COUNT, THREADS, TLAS>(L, inst, tl, stack, nPairs, nTris, errorWord))
+            step<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>(L, inst, tl, st, nPairs, nTris, errorWord))
         {
           write_result<ANY>(L, inst, out);
           L.ray = kNoRay;
@@ -840,13 +841,15 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
 }
 
 // One thread per ray.
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
 __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict__ rays, uint32_t n,
                                                         const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
-                                                        void* out, unsigned long long* counters, uint32_t* errorWord)
+                                                        void* out, unsigned long long* counters, uint32_t* errorWord,
+                                                        int stackShared)
 {
-  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT, TLAS>::value * THREADS entries
-  uint32_t* stack = s_stack + threadIdx.x;
+  extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
+  uint32_t spill[StackDepth<LAYOUT, TLAS>::value];
+  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
   uint64_t nPairs = 0, nTris = 0;
   const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
   if (i < n)
@@ -858,7 +861,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
     else live = begin_instance<LAYOUT>(L, inst, first_instance(L, i, sg));
     if (live)
       while (!out_of_budget(L, errorWord) &&
-             !step<LAYOUT, ANY, COUNT, THREADS, TLAS>(L, inst, tl, stack, nPairs, nTris, errorWord)) {}
+             !step<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>(L, inst, tl, st, nPairs, nTris, errorWord)) {}
     write_result<ANY>(L, inst, out);
   }
   flush_counters<COUNT>(nPairs, nTris, counters);
@@ -902,23 +905,23 @@ __device__ __forceinline__ void start_ray_one(Lane1& L, uint32_t i, const float4
 }
 
 // One step of the single-instance kernel; true when the ray is finished.
-template <int LAYOUT, bool ANY, int THREADS>
-__device__ __forceinline__ bool step_one(Lane1& L, uint32_t* __restrict__ stack, uint32_t* errorWord)
+template <int LAYOUT, int TRI, bool ANY, int THREADS>
+__device__ __forceinline__ bool step_one(Lane1& L, Stack<THREADS>& st, uint32_t* errorWord)
 {
   constexpr int DEPTH = StackDepth<LAYOUT, false>::value;
   uint64_t none = 0;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, ANY, false, THREADS, DEPTH>(L, stack, none, errorWord);
+    const int r = visit_node<LAYOUT, ANY, false, THREADS, DEPTH>(L, st, none, errorWord);
     if (r < 0) return true;
     if (r == 0) return false;
   }
   else if (L.cur != kEmptyRef &&
-           leaf_test<ANY, false, EndBit<LAYOUT>::value>(L.tris, L.cur & ~kLeafBit, L.r, L.h, 0u, none))
+           test_leaf<TRI, ANY, false, EndBit<LAYOUT>::value>(L.tris, L.cur & ~kLeafBit, L.r, L.h, 0u, none))
     return true;  // any-hit found
   if (L.top == 0) return true;
   L.top--;
-  L.cur = stack[L.top * THREADS];
+  L.cur = st.get(L.top);
   return false;
 }
 
@@ -938,15 +941,16 @@ __device__ __forceinline__ void write_result_one(const Lane1& L, uint32_t instId
 }
 
 // Persistent warp pool over one instance (the refill rule of k_trace_pool).
-template <int LAYOUT, bool ANY, int THREADS>
+template <int LAYOUT, int TRI, bool ANY, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict__ rays, uint32_t n,
                                                        const void* __restrict__ nodes, const TriRec* __restrict__ tris,
                                                        uint32_t instId, uint32_t geomId, void* out,
                                                        uint32_t* errorWord, unsigned int* rayCounter, int steps,
-                                                       int refill)
+                                                       int refill, int stackShared)
 {
-  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT>::value * THREADS entries
-  uint32_t* stack = s_stack + threadIdx.x;
+  extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
+  uint32_t spill[StackDepth<LAYOUT, false>::value];
+  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ltMask = (1u << lane) - 1u;
   Lane1 L;
@@ -974,7 +978,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
     {
       for (int s = 0; s < steps; s++)
       {
-        if (out_of_budget(L, errorWord) || step_one<LAYOUT, ANY, THREADS>(L, stack, errorWord))
+        if (out_of_budget(L, errorWord) || step_one<LAYOUT, TRI, ANY, THREADS>(L, st, errorWord))
         {
           write_result_one<ANY>(L, instId, geomId, out);
           L.ray = kNoRay;
@@ -988,48 +992,54 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
 // One thread per ray over one instance: a warp's 32 consecutive rays end
 // together, so their results go out as one contiguous kilobyte (results
 // written in place over the host link want this).
-template <int LAYOUT, bool ANY, int THREADS>
+template <int LAYOUT, int TRI, bool ANY, int THREADS>
 __global__ void __launch_bounds__(THREADS)
     k_trace_one_grid(const float4* __restrict__ rays, uint32_t n, const void* __restrict__ nodes,
-                     const TriRec* __restrict__ tris, uint32_t instId, uint32_t geomId, void* out, uint32_t* errorWord)
+                     const TriRec* __restrict__ tris, uint32_t instId, uint32_t geomId, void* out, uint32_t* errorWord,
+                     int stackShared)
 {
-  extern __shared__ uint32_t s_stack[];  // StackDepth<LAYOUT>::value * THREADS entries
-  uint32_t* stack = s_stack + threadIdx.x;
+  extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
+  uint32_t spill[StackDepth<LAYOUT, false>::value];
+  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
   const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
   if (i >= n) return;
   Lane1 L;
   L.nodes = nodes;
   L.tris = tris;
   start_ray_one(L, i, rays);
-  while (!out_of_budget(L, errorWord) && !step_one<LAYOUT, ANY, THREADS>(L, stack, errorWord)) {}
+  while (!out_of_budget(L, errorWord) && !step_one<LAYOUT, TRI, ANY, THREADS>(L, st, errorWord)) {}
   write_result_one<ANY>(L, instId, geomId, out);
 }
 
-template <int LAYOUT, bool ANY, int THREADS>
+// Dynamic shared memory of a traversal kernel: `shared` stack entries per
+// thread; above 48 KB a block needs the opt-in attribute.
+template <typename K> cudaError_t allow_smem(K kernel, size_t smem)
+{
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <int LAYOUT, int TRI, bool ANY, int THREADS>
 cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   const uint32_t n = (uint32_t)a.n;
-  constexpr size_t smem = sizeof(uint32_t) * StackDepth<LAYOUT, false>::value * THREADS;
-  if (smem > 48 * 1024)
-  {
-    cudaError_t e = cudaFuncSetAttribute(k_trace_one<LAYOUT, ANY, THREADS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_trace_one_grid<LAYOUT, ANY, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  const int shared = shared_entries<StackDepth<LAYOUT, false>::value>(c.stackEntries);
+  const size_t smem = sizeof(uint32_t) * (size_t)shared * THREADS;
   const InstanceDesc& d = *a.one;
   const void* nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
   if (!c.persistent)
   {
-    k_trace_one_grid<LAYOUT, ANY, THREADS><<<(uint32_t)(((uint64_t)n + THREADS - 1) / THREADS), THREADS, smem, s>>>(
-        a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits, a.errorWord);
+    cudaError_t e = allow_smem(k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, smem);
+    if (e != cudaSuccess) return e;
+    k_trace_one_grid<LAYOUT, TRI, ANY, THREADS><<<(uint32_t)(((uint64_t)n + THREADS - 1) / THREADS), THREADS, smem,
+                                                  s>>>(a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits,
+                                                       a.errorWord, shared);
     return cudaGetLastError();
   }
+  cudaError_t e = allow_smem(k_trace_one<LAYOUT, TRI, ANY, THREADS>, smem);
+  if (e != cudaSuccess) return e;
   int perSM = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_one<LAYOUT, ANY, THREADS>, THREADS,
-                                                                smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_one<LAYOUT, TRI, ANY, THREADS>, THREADS, smem);
   if (e != cudaSuccess) return e;
   if (perSM < 1) perSM = 1;
   uint64_t blocks = (uint64_t)numSMs * perSM;
@@ -1037,50 +1047,44 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   if (blocks > need) blocks = need;
   e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
-  k_trace_one<LAYOUT, ANY, THREADS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+  k_trace_one<LAYOUT, TRI, ANY, THREADS><<<(uint32_t)blocks, THREADS, smem, s>>>(
       a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill,
-      c.refillLanes);
+      c.refillLanes, shared);
   return cudaGetLastError();
 }
 
-template <int LAYOUT>
+template <int LAYOUT, int TRI>
 cudaError_t trace_one(const TraceArgs& a, int kind, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   switch (c.threadsPerBlock)
   {
     case 64:
-      return kind == 0 ? launch_one<LAYOUT, false, 64>(a, c, numSMs, s) : launch_one<LAYOUT, true, 64>(a, c, numSMs, s);
+      return kind == 0 ? launch_one<LAYOUT, TRI, false, 64>(a, c, numSMs, s)
+                       : launch_one<LAYOUT, TRI, true, 64>(a, c, numSMs, s);
     case 256:
-      return kind == 0 ? launch_one<LAYOUT, false, 256>(a, c, numSMs, s)
-                       : launch_one<LAYOUT, true, 256>(a, c, numSMs, s);
+      return kind == 0 ? launch_one<LAYOUT, TRI, false, 256>(a, c, numSMs, s)
+                       : launch_one<LAYOUT, TRI, true, 256>(a, c, numSMs, s);
     default:
-      return kind == 0 ? launch_one<LAYOUT, false, 128>(a, c, numSMs, s)
-                       : launch_one<LAYOUT, true, 128>(a, c, numSMs, s);
+      return kind == 0 ? launch_one<LAYOUT, TRI, false, 128>(a, c, numSMs, s)
+                       : launch_one<LAYOUT, TRI, true, 128>(a, c, numSMs, s);
   }
 }
 
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
 cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   const uint32_t n = (uint32_t)a.n;
   const Segments sg{a.rayOffsets, a.segInst, a.nSeg, a.nInst};
   const Tlas tl{a.tlasRecs, a.tlasTris, a.nInst};
-  // the short stack is dynamic shared memory: above 48 KB a block needs the opt-in attribute
-  constexpr size_t smem = sizeof(uint32_t) * StackDepth<LAYOUT, TLAS>::value * THREADS;
-  if (smem > 48 * 1024)
-  {
-    cudaError_t e = cudaFuncSetAttribute(k_trace_pool<LAYOUT, ANY, COUNT, THREADS, TLAS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_trace_grid<LAYOUT, ANY, COUNT, THREADS, TLAS>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  const int shared = shared_entries<StackDepth<LAYOUT, TLAS>::value>(c.stackEntries);
+  const size_t smem = sizeof(uint32_t) * (size_t)shared * THREADS;
   if (c.persistent && !COUNT)
   {
+    cudaError_t e = allow_smem(k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>, smem);
+    if (e != cudaSuccess) return e;
     int perSM = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &perSM, k_trace_pool<LAYOUT, ANY, COUNT, THREADS, TLAS>, THREADS, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>,
+                                                      THREADS, smem);
     if (e != cudaSuccess) return e;
     if (perSM < 1) perSM = 1;
     uint64_t blocks = (uint64_t)numSMs * perSM;
@@ -1088,35 +1092,38 @@ cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStr
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    k_trace_pool<LAYOUT, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
-        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes);
+    k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes,
+        shared);
   }
   else
   {
+    cudaError_t e = allow_smem(k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>, smem);
+    if (e != cudaSuccess) return e;
     const uint64_t blocks = ((uint64_t)n + THREADS - 1) / THREADS;
-    k_trace_grid<LAYOUT, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
-        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord);
+    k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, shared);
   }
   return cudaGetLastError();
 }
 
-template <int LAYOUT, bool TLAS>
+template <int LAYOUT, int TRI, bool TLAS>
 cudaError_t trace_tlas(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   if (counting)
-    return kind == 0 ? launch<LAYOUT, false, true, 128, TLAS>(a, c, numSMs, s)
-                     : launch<LAYOUT, true, true, 128, TLAS>(a, c, numSMs, s);
+    return kind == 0 ? launch<LAYOUT, TRI, false, true, 128, TLAS>(a, c, numSMs, s)
+                     : launch<LAYOUT, TRI, true, true, 128, TLAS>(a, c, numSMs, s);
   switch (c.threadsPerBlock)
   {
     case 64:
-      return kind == 0 ? launch<LAYOUT, false, false, 64, TLAS>(a, c, numSMs, s)
-                       : launch<LAYOUT, true, false, 64, TLAS>(a, c, numSMs, s);
+      return kind == 0 ? launch<LAYOUT, TRI, false, false, 64, TLAS>(a, c, numSMs, s)
+                       : launch<LAYOUT, TRI, true, false, 64, TLAS>(a, c, numSMs, s);
     case 256:
-      return kind == 0 ? launch<LAYOUT, false, false, 256, TLAS>(a, c, numSMs, s)
-                       : launch<LAYOUT, true, false, 256, TLAS>(a, c, numSMs, s);
+      return kind == 0 ? launch<LAYOUT, TRI, false, false, 256, TLAS>(a, c, numSMs, s)
+                       : launch<LAYOUT, TRI, true, false, 256, TLAS>(a, c, numSMs, s);
     default:
-      return kind == 0 ? launch<LAYOUT, false, false, 128, TLAS>(a, c, numSMs, s)
-                       : launch<LAYOUT, true, false, 128, TLAS>(a, c, numSMs, s);
+      return kind == 0 ? launch<LAYOUT, TRI, false, false, 128, TLAS>(a, c, numSMs, s)
+                       : launch<LAYOUT, TRI, true, false, 128, TLAS>(a, c, numSMs, s);
   }
 }
 
@@ -1124,14 +1131,14 @@ cudaError_t trace_tlas(const TraceArgs& a, int kind, int counting, const TraceCo
 // not depend on the schedule.  A scene with an instance tree uses the
 // two-level kernels, except in segmented queries (one instance per ray).  A
 // scene of one untransformed instance uses the single-instance kernels.
-template <int LAYOUT>
+template <int LAYOUT, int TRI>
 cudaError_t trace_layout(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   if (a.one != nullptr && !counting && a.rayOffsets == nullptr && a.tlasRecs == nullptr)
-    return trace_one<LAYOUT>(a, kind, c, numSMs, s);
+    return trace_one<LAYOUT, TRI>(a, kind, c, numSMs, s);
   if (a.tlasRecs != nullptr && a.rayOffsets == nullptr)
-    return trace_tlas<LAYOUT, true>(a, kind, counting, c, numSMs, s);
-  return trace_tlas<LAYOUT, false>(a, kind, counting, c, numSMs, s);
+    return trace_tlas<LAYOUT, TRI, true>(a, kind, counting, c, numSMs, s);
+  return trace_tlas<LAYOUT, TRI, false>(a, kind, counting, c, numSMs, s);
 }
 
 }  // namespace
@@ -1141,5 +1148,10 @@ cudaError_t trace_l0(const TraceArgs& a, int kind, int counting, const TraceConf
 cudaError_t trace_l1(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
 cudaError_t trace_l2(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
 cudaError_t trace_l3(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+// The same with the watertight triangle test (trace_w*.cu).
+cudaError_t trace_w0(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+cudaError_t trace_w1(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+cudaError_t trace_w2(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
+cudaError_t trace_w3(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s);
 
 }  // namespace hrt

@@ -5,6 +5,6 @@ namespace hrt
 {
 cudaError_t trace_l0(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
-  return trace_layout<0>(a, kind, counting, c, numSMs, s);
+  return trace_layout<0, 0>(a, kind, counting, c, numSMs, s);
 }
 }  // namespace hrt

@@ -5,6 +5,6 @@ namespace hrt
 {
 cudaError_t trace_l2(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
-  return trace_layout<2>(a, kind, counting, c, numSMs, s);
+  return trace_layout<2, 0>(a, kind, counting, c, numSMs, s);
 }
 }  // namespace hrt

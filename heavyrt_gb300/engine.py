@@ -44,6 +44,9 @@ EXPORT_NODES4 = 9
 
 # node layouts (include/hrt.h); names accepted as CreateSceneRT's a_layoutName
 LAYOUT_BVH2, LAYOUT_BVH4_F32, LAYOUT_BVH4_F16, LAYOUT_BVH4_Q8 = 0, 1, 2, 3
+OPTION_BVH4_MERGE, OPTION_TLAS, OPTION_TRIANGLE_TEST = 1, 2, 3
+TRI_MOLLER_TRUMBORE, TRI_WATERTIGHT = 0, 1
+TRI_TEST_NAMES = {"mt": TRI_MOLLER_TRUMBORE, "moller_trumbore": TRI_MOLLER_TRUMBORE, "watertight": TRI_WATERTIGHT}
 LAYOUT_NAMES = {"": LAYOUT_BVH2, "bvh2": LAYOUT_BVH2, "bvh4": LAYOUT_BVH4_F32, "bvh4_f32": LAYOUT_BVH4_F32,
                 "bvh4_f16": LAYOUT_BVH4_F16, "bvh4_half": LAYOUT_BVH4_F16, "bvh4_q8": LAYOUT_BVH4_Q8}
 
@@ -70,7 +73,7 @@ class TraceConfig(C.Structure):
     """hrt_trace_config (include/hrt.h): launch shape of the traversal kernel."""
 
     _fields_ = [("threadsPerBlock", C.c_int), ("persistent", C.c_int), ("stepsPerRefill", C.c_int),
-                ("refillLanes", C.c_int)]
+                ("refillLanes", C.c_int), ("stackEntries", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -303,7 +306,8 @@ def _as_rays(posAndNear, dirAndFar=None) -> np.ndarray:
 class SceneRT:
     """GPU LBVH scene behind HeavyRT's ISceneObject interface (core/CrossRT.h:64-193)."""
 
-    def __init__(self, ctx: Context | None = None, build_name: str = "cbvh_lbvh", layout=LAYOUT_BVH2):
+    def __init__(self, ctx: Context | None = None, build_name: str = "cbvh_lbvh", layout=LAYOUT_BVH2,
+                 triangle_test=TRI_MOLLER_TRUMBORE):
         self.ctx = ctx or default_context()
         self._h = C.c_void_p()
         self.ctx.check(lib().hrt_scene_create(self.ctx.handle, build_name.encode() if build_name else None,
@@ -315,14 +319,22 @@ class SceneRT:
             layout = LAYOUT_NAMES[layout.lower()]
         if layout != LAYOUT_BVH2:
             self.ctx.check(lib().hrt_scene_set_layout(self._h, int(layout)), "set_layout")
+        if isinstance(triangle_test, str):
+            triangle_test = TRI_TEST_NAMES[triangle_test.lower()]
+        if triangle_test != TRI_MOLLER_TRUMBORE:
+            self.set_triangle_test(triangle_test)
 
     def set_bvh4_merge(self, value: int):
         """0: the reference's leaf merge rule; M: merge subtrees of <= M triangles."""
-        self.ctx.check(lib().hrt_scene_set_option(self._h, 1, int(value)), "set_option")
+        self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_BVH4_MERGE, int(value)), "set_option")
 
     def set_tlas(self, enabled: bool):
         """Instance tree over the instances (default on; takes effect at CommitScene)."""
-        self.ctx.check(lib().hrt_scene_set_option(self._h, 2, int(bool(enabled))), "set_option")
+        self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_TLAS, int(bool(enabled))), "set_option")
+
+    def set_triangle_test(self, test: int):
+        """TRI_MOLLER_TRUMBORE (the reference's test) or TRI_WATERTIGHT; before the first geometry."""
+        self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_TRIANGLE_TEST, int(test)), "set_option")
 
     @property
     def layout(self) -> int:
@@ -486,8 +498,9 @@ class SceneRT:
                        "query_counters")
         return int(c[0]), int(c[1])
 
-    def set_trace_config(self, kind: int, threadsPerBlock=128, persistent=1, stepsPerRefill=16, refillLanes=24):
-        c = TraceConfig(threadsPerBlock, persistent, stepsPerRefill, refillLanes)
+    def set_trace_config(self, kind: int, threadsPerBlock=128, persistent=1, stepsPerRefill=16, refillLanes=24,
+                         stackEntries=0):
+        c = TraceConfig(threadsPerBlock, persistent, stepsPerRefill, refillLanes, stackEntries)
         self.ctx.check(lib().hrt_scene_set_trace_config(self._h, kind, C.byref(c)), "set_trace_config")
 
     def trace_config(self, kind: int) -> dict:

@@ -26,7 +26,8 @@ ORACLE = ROOT / "oracle"
 INCLUDE = ROOT / "include"
 
 CUDA_SOURCES = ["radix_sort.cu", "build.cu", "build_batch.cu", "bvh4.cu", "trace.cu", "trace_l0.cu", "trace_l1.cu",
-                "trace_l2.cu", "trace_l3.cu", "hrt_api.cu", "server.cu", "raygen.cu", "render.cu", "formats.cu"]
+                "trace_l2.cu", "trace_l3.cu", "trace_w0.cu", "trace_w1.cu", "trace_w2.cu", "trace_w3.cu", "hrt_api.cu",
+                "server.cu", "raygen.cu", "render.cu", "formats.cu"]
 CUDA_HEADERS = ["hrt_common.cuh", "build_common.cuh", "hrt_kernels.cuh", "hrt_internal.cuh", "trace_impl.cuh",
                 "raygen_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -129,6 +129,23 @@ int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
  *                          Results are the same either way, except which of two
  *                          instances wins an exact tie in t. */
 #define HRT_OPTION_TLAS 2
+/*   HRT_OPTION_TRIANGLE_TEST  the ray-triangle test of every geometry of the
+ *                          scene, chosen before the first geometry is added
+ *                          (HRT_ERR_STATE afterwards):
+ *     HRT_TRI_MOLLER_TRUMBORE (default) HeavyRT's test (core/BVH2CommonRT.cpp:9-47):
+ *                          Moller-Trumbore with 1e-6 barycentric slack,
+ *                          results bit-exact with the reference;
+ *     HRT_TRI_WATERTIGHT   the watertight test of Woop, Benthin & Wald (JCGT
+ *                          2013) in FP32 with exact edge-function signs: no
+ *                          ray passes between two triangles that share an
+ *                          edge, and no hit is accepted outside a triangle.
+ *                          Hits agree with the reference except for rays
+ *                          within about 1e-6 (in barycentric terms) of an
+ *                          edge.  The scene's triangle records then hold the
+ *                          three vertices instead of a vertex and two edges. */
+#define HRT_OPTION_TRIANGLE_TEST 3
+#define HRT_TRI_MOLLER_TRUMBORE  0
+#define HRT_TRI_WATERTIGHT       1
 int hrt_scene_set_option(hrt_scene* scene, int option, int value);
 
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */
@@ -216,14 +233,21 @@ int hrt_scene_check(hrt_scene* scene);
 
 /* Launch shape of the traversal kernel, per query kind (0 nearest, 1 any);
  * results never depend on it.  No reference counterpart (the reference runs
- * one ray per virtual call).  Defaults: 128 threads, persistent pool,
- * 16 steps between refills, refill at 24 idle lanes. */
+ * one ray per virtual call with an 80-entry stack, core/raytrace_common.h:34).
+ * Defaults: 128 threads, persistent pool, 16 steps between refills, refill at
+ * 24 idle lanes, the whole stack in shared memory.
+ * stackEntries: traversal stack entries per ray kept in shared memory; deeper
+ * entries spill to the thread's local memory, so any value is correct for any
+ * tree.  0, or a value at or above the layout's depth bound (32 binary, 48
+ * 4-wide, +32 with an instance tree), keeps the whole stack in shared memory. */
+#define HRT_MAX_STACK_ENTRIES 128
 typedef struct hrt_trace_config
 {
   int threadsPerBlock; /* 64, 128 or 256                                          */
   int persistent;      /* 1: persistent warp pool that refills idle lanes; 0: one thread per ray */
   int stepsPerRefill;  /* traversal steps between refill checks (1..1024)        */
   int refillLanes;     /* a warp refills when at least this many lanes are idle (1..32) */
+  int stackEntries;    /* short-stack entries in shared memory (0..HRT_MAX_STACK_ENTRIES) */
 } hrt_trace_config;
 int hrt_scene_set_trace_config(hrt_scene* scene, int kind, const hrt_trace_config* config);
 int hrt_scene_get_trace_config(const hrt_scene* scene, int kind, hrt_trace_config* config);
@@ -289,7 +313,8 @@ int hrt_graph_destroy(hrt_graph* graph);
 /* Launch-shape autotuner: times `query` (repeats timed runs after one
  * warm-up) under every trace configuration of a fixed grid (64/128/256
  * threads; one ray per thread, or the persistent pool with 4..64 steps per
- * refill and 8..32 idle lanes to refill), sets the fastest as the scene's
+ * refill and 8..32 idle lanes to refill), then the best of those with 16, 24,
+ * 32, 48 and 64 shared-memory stack entries; sets the fastest as the scene's
  * configuration for query->kind, and returns it with its mean time in ms.
  * Synchronous; overwrites query->out (with identical results). */
 int hrt_scene_autotune(hrt_scene* scene, const hrt_query_desc* query, int repeats, hrt_trace_config* best,

@@ -175,6 +175,7 @@ typedef struct
   float*    verts;         /* 4*nV, copy of vertex positions with w = 1 */
   uint32_t  nVerts;
   int       status;        /* 0 ok, 1 leaf count above 127 */
+  int       triTest;       /* 0 the reference's Moller-Trumbore, 1 watertight */
 } ora_bvh;
 
 /* delta(), core/builders/lbvh.cpp:386-403. */
@@ -576,6 +577,8 @@ uint32_t ora_num_tris(const ora_bvh* B) { return B->nTris; }
 uint32_t ora_num_leaves(const ora_bvh* B) { return B->nLeaves; }
 uint32_t ora_num_nodes(const ora_bvh* B) { return B->nNodes; }
 int ora_status(const ora_bvh* B) { return B->status; }
+/* 0: the reference's Moller-Trumbore test (default), 1: the watertight test. */
+void ora_set_triangle_test(ora_bvh* B, int test) { B->triTest = test; }
 void ora_get_box(const ora_bvh* B, float* out12)
 {
   memcpy(out12, B->bmin, 16); memcpy(out12 + 4, B->bmax, 16); memcpy(out12 + 8, B->scale, 16);
@@ -656,6 +659,80 @@ static inline int leaf_test(const ora_bvh* B, const float o[3], const float d[3]
   return found;
 }
 
+/* Watertight ray-triangle test of Woop, Benthin & Wald ("Watertight
+ * Ray/Triangle Intersection", JCGT 2(1), 2013), restated for the engine's
+ * HRT_TRI_WATERTIGHT mode (not a reference function: HeavyRT has only the
+ * Moller-Trumbore test above).  The ray's dominant axis becomes z (kx, ky
+ * swapped when that component is negative, keeping the winding), vertices are
+ * translated to the ray origin and sheared, and the signs of the three edge
+ * functions U, V, W at the origin decide the hit, both windings accepted.  The
+ * paper's double-precision re-evaluation of a zero edge function is replaced
+ * by Kahan's difference of products (one product's rounding error restored by
+ * a fused multiply-add), whose relative error is below 2 ulp, so every sign is
+ * exact in binary32.  t = T / det as T * (1 / det); coords = (W, V) / det, the
+ * weights of C and B, the fields the Moller-Trumbore test fills.  fmaf is the
+ * correctly rounded fused multiply-add on every platform. */
+static inline float ora_pick3(const float v[3], int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); }
+
+static inline float ora_diff_of_products(float a, float b, float c, float d)
+{
+  const float w = c * d;
+  const float e = fmaf(-c, d, w);
+  const float f = fmaf(a, b, -w);
+  return f + e;
+}
+
+static inline int leaf_test_wt(const ora_bvh* B, const float o[3], const float d[3], float tNear, uint32_t start,
+                               uint32_t count, ora_hit* hit)
+{
+  const float ad[3] = {fabsf(d[0]), fabsf(d[1]), fabsf(d[2])};
+  const int kz = (ad[0] >= ad[1] && ad[0] >= ad[2]) ? 0 : (ad[1] >= ad[2] ? 1 : 2);
+  int kx = kz == 2 ? 0 : kz + 1;
+  int ky = kx == 2 ? 0 : kx + 1;
+  const float dz = ora_pick3(d, kz);
+  if (dz < 0.0f)
+  {
+    const int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  const float sx = ora_pick3(d, kx) / dz, sy = ora_pick3(d, ky) / dz, sz = 1.0f / dz;
+  int found = 0;
+  for (uint32_t tri = start; tri < start + count; tri++)
+  {
+    const float* V0 = B->verts + 4 * (size_t)B->indicesSorted[3 * tri + 0];
+    const float* V1 = B->verts + 4 * (size_t)B->indicesSorted[3 * tri + 1];
+    const float* V2 = B->verts + 4 * (size_t)B->indicesSorted[3 * tri + 2];
+    const float a[3] = {V0[0] - o[0], V0[1] - o[1], V0[2] - o[2]};
+    const float b[3] = {V1[0] - o[0], V1[1] - o[1], V1[2] - o[2]};
+    const float c[3] = {V2[0] - o[0], V2[1] - o[1], V2[2] - o[2]};
+    const float az = ora_pick3(a, kz), bz = ora_pick3(b, kz), cz = ora_pick3(c, kz);
+    const float ax = ora_pick3(a, kx) - sx * az, ay = ora_pick3(a, ky) - sy * az;
+    const float bx = ora_pick3(b, kx) - sx * bz, by = ora_pick3(b, ky) - sy * bz;
+    const float cx = ora_pick3(c, kx) - sx * cz, cy = ora_pick3(c, ky) - sy * cz;
+    const float U = ora_diff_of_products(cx, by, cy, bx);
+    const float V = ora_diff_of_products(ax, cy, ay, cx);
+    const float W = ora_diff_of_products(bx, ay, by, ax);
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) continue;
+    const float det = (U + V) + W;
+    if (det == 0.0f) continue;
+    const float T = (U * (sz * az) + V * (sz * bz)) + W * (sz * cz);
+    const float inv = 1.0f / det;
+    const float t = T * inv;
+    if (t > tNear && t < hit->t)
+    {
+      hit->t = t;
+      hit->primId = tri;
+      hit->instId = 0;
+      hit->geomId = 0;
+      hit->coords[0] = W * inv;
+      hit->coords[1] = V * inv;
+      found = 1;
+    }
+  }
+  return found;
+}
+
 /* BVH2TraverseC32, core/BVH2CommonRT.cpp:49-141, on the peach node array.
  * anyHit != 0 stops at the first accepted triangle, as the reference's siblings
  * do for RayQuery_AnyHit (core/BVH2CommonRTStacklessLBVH.cpp:65,161-165).
@@ -701,7 +778,8 @@ static void traverse(const ora_bvh* B, const float* ray8, int anyHit, ora_hit* h
       const uint32_t start = off & ORA_START_MASK;
       const uint32_t count = (off & ORA_SIZE_MASK) >> 24;
       if (counters) counters[1] += count;
-      const int found = leaf_test(B, o, d, tNear, start, count, hit);
+      const int found = B->triTest ? leaf_test_wt(B, o, d, tNear, start, count, hit)
+                                   : leaf_test(B, o, d, tNear, start, count, hit);
       if (anyHit && found) return;
       pop = 1;
     }

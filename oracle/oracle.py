@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
         L.ora_copy_u32.argtypes = [vp, i32, vp]
         L.ora_trace.restype = i32
         L.ora_trace.argtypes = [vp, vp, u64, i32, vp, vp, i32, vp]
+        L.ora_set_triangle_test.argtypes = [vp, i32]
         L.ora_eye_rays.argtypes = [vp, vp, u32, u32, C.c_float, C.c_float, vp]
         f32 = C.c_float
         L.ora_pack_xy.argtypes = [u32, u32, vp]
@@ -114,10 +115,14 @@ class OracleBVH:
     def sorted_indices(self):
         return self._u32(8, 3 * self.n_tris)
 
-    def trace(self, rays: np.ndarray, any_hit: bool = False, threads: int = 0, counters: bool = False):
+    def trace(self, rays: np.ndarray, any_hit: bool = False, threads: int = 0, counters: bool = False,
+              watertight: bool = False):
+        """BVH2TraverseC32 over the rays; with watertight=True the leaves use
+        the watertight triangle test instead of the reference's MT test."""
         r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
         n = r.shape[0]
         cnt = np.zeros(2, dtype=np.uint64)
+        lib().ora_set_triangle_test(self._h, 1 if watertight else 0)
         if any_hit:
             out = np.empty(n, dtype=np.uint8)
             used = lib().ora_trace(self._h, _p(r), n, 1, None, _p(out), threads, _p(cnt) if counters else None)
