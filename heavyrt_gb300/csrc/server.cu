@@ -55,6 +55,7 @@ struct SceneRec
   uint64_t              lastUse = 0;
   uint64_t              reserved = 0;  // bytes held against the budget
   Geom                  geom;
+  InstanceDesc          desc{};            // host copy of the scene's table entry (valid once ready)
   void*                 dVerts = nullptr;  // inputs of a pending build, copied to the device
   uint32_t*             dIdx = nullptr;
   uint64_t              nIdx = 0;
@@ -72,7 +73,8 @@ struct hrt_server
   cudaStream_t            stageStream = nullptr;  // copies of new scenes' inputs
   hrt_scene               proto;          // layout / merge options for builds
   hrt_server_config       cfg{};
-  TraceConfig             trace[2];
+  TraceConfig             trace[2];     // segmented batches
+  TraceConfig             traceOne[2];  // batches of one request (single-instance kernels)
   InstanceDesc*           dTable = nullptr;
   std::vector<SceneRec>   scenes;
   std::vector<uint32_t>   freeSlots;
@@ -112,6 +114,7 @@ struct Slot
   bool                  busy = false;
   uint32_t              batch = 0;
   std::vector<Request*> reqs;
+  InstanceDesc          one{};  // the scene of a batch of one request (copied under the server lock)
 };
 
 uint64_t estimate_scene_bytes(uint64_t nTris, uint64_t nVert, int layout)
@@ -179,7 +182,49 @@ cudaError_t issue(hrt_server* S, Slot* sl)
   const Request* only = sl->reqs.size() == 1 ? sl->reqs[0] : nullptr;
   const float4* inPlaceRays =
       only && aligned_to(only->rays, 16) ? static_cast<const float4*>(mapped_host(only->rays)) : nullptr;
-  void* inPlaceOut = only && only->kind == 1 ? mapped_host(only->out) : nullptr;
+  void* inPlaceOut =
+      only && (only->kind == 1 || aligned_to(only->out, 16)) ? mapped_host(only->out) : nullptr;
+  if (only && sl->one.valid)
+  {
+    // One request against one scene of one untransformed geometry: the
+    // single-instance kernels (fewer registers, no segment search), rays read
+    // in place when page-locked, results written in place when page-locked
+    // (nearest hits by the one-thread-per-ray kernel, whose warps write 32
+    // consecutive hits at once); the same results as the segmented launch.
+    cudaStream_t st = sl->stream;
+    cudaError_t e = cudaMemsetAsync(sl->dErr, 0, 8 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const int k = only->kind;
+    if (!inPlaceRays)
+    {
+      e = cudaMemcpyAsync(sl->rays, only->rays, 32 * only->n, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return e;
+    }
+    TraceArgs a;
+    a.rays = inPlaceRays ? inPlaceRays : sl->rays;
+    a.n = only->n;
+    a.inst = S->dTable;
+    a.nInst = S->cfg.maxScenes;
+    a.hits = inPlaceOut ? inPlaceOut : (k == 0 ? static_cast<void*>(sl->hits) : static_cast<void*>(sl->any));
+    a.counters = nullptr;
+    a.errorWord = sl->dErr;
+    a.rayCounter = sl->counters + k;
+    a.one = &sl->one;
+    TraceConfig c = S->traceOne[k];
+    if (k == 0 && inPlaceOut) c.persistent = 0;
+    e = hrt::trace(a, k, 0, S->cfg.layout, c, S->ctx->numSMs, st);
+    if (e != cudaSuccess) return e;
+    if (!inPlaceOut)
+    {
+      e = k == 0 ? cudaMemcpyAsync(only->out, sl->hits, sizeof(hrt_hit) * only->n, cudaMemcpyDeviceToHost, st)
+                 : cudaMemcpyAsync(only->out, sl->any, only->n, cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess) return e;
+    }
+    e = cudaMemcpyAsync(sl->hErr, sl->dErr, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchHostFunc(st, on_slot_done, sl);
+  }
+  if (only && only->kind == 0) inPlaceOut = nullptr;  // the segmented path copies nearest hits out
   uint32_t* hOff[2] = {sl->hIdx, sl->hIdx + (2 * maxReq + 1)};
   uint32_t* dOff[2] = {sl->dIdx, sl->dIdx + (2 * maxReq + 1)};
   uint32_t cnt[2] = {0, 0};
@@ -289,6 +334,12 @@ void dispatcher_main(hrt_server* S)
       it = S->queue.erase(it);
     }
     if (free->reqs.empty()) continue;
+    free->one = InstanceDesc{};
+    if (free->reqs.size() == 1)
+    {
+      const InstanceDesc& d = S->scenes[free->reqs[0]->scene].desc;
+      if (d.valid && d.identity) free->one = d;
+    }
     free->busy = true;
     free->batch = S->nextBatch++;
     const double t = S->now();
@@ -378,6 +429,7 @@ void builder_main(hrt_server* S)
     if (st == HRT_OK)
     {
       sc.geom = g;
+      sc.desc = d;
       sc.reserved = g.bytes;
       sc.state = HRT_SCENE_READY;
       S->resident += g.bytes;
@@ -470,6 +522,14 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
     S->trace[k].stepsPerRefill = 16;
     S->trace[k].refillLanes = 8;
   }
+  // single requests: the single-instance kernels' shapes of the RTAO frame's
+  // sweep (nearest hits written in place switch to one thread per ray)
+  S->traceOne[0].threadsPerBlock = 64;
+  S->traceOne[0].persistent = 0;
+  S->traceOne[1].threadsPerBlock = 128;
+  S->traceOne[1].persistent = 1;
+  S->traceOne[1].stepsPerRefill = 8;
+  S->traceOne[1].refillLanes = 8;
   auto bail = [&](cudaError_t e, const char* what) {
     destroy_slots(S);
     if (S->dTable) cudaFree(S->dTable);

@@ -35,7 +35,7 @@ def _u32(h):
     return np.ascontiguousarray(h).view(np.uint32).reshape(-1, 8)
 
 
-def _compare(got, want, layout):
+def _compare(got, want, layout, tie_limit=True):
     g, w = _u32(got), _u32(want)
     if layout == "bvh2":
         np.testing.assert_array_equal(g, w)
@@ -46,7 +46,8 @@ def _compare(got, want, layout):
     tg = g[~same, 0].view(np.float32).astype(np.float64)
     tw = w[~same, 0].view(np.float32).astype(np.float64)
     assert np.all(np.abs(tg - tw) <= 1e-5 * np.abs(tw))
-    assert np.count_nonzero(~same) <= max(2, g.shape[0] // 100000)
+    if tie_limit:
+        assert np.count_nonzero(~same) <= max(2, g.shape[0] // 100000)
 
 
 def _heightfield_edge_rays(v, nx):
@@ -126,7 +127,9 @@ def test_watertight_heightfield_edges_never_leak(native):
         s, _ = _scene(v, idx, layout, merge)
         got = s.RayQuery_NearestHit(rays)
         assert np.all(got["geomId"] != MISS), layout
-        _compare(got, want, layout)
+        # rays aimed at shared edges and vertices tie between the triangles
+        # that meet there; the 4-wide order may pick another of them
+        _compare(got, want, layout, tie_limit=False)
         assert s.RayQuery_AnyHit(rays).all()
         s.close()
 
