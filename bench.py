@@ -273,6 +273,17 @@ def host_cpu() -> str:
     return f"{name or platform.processor() or platform.machine()} ({os.cpu_count()} logical cores)"
 
 
+# Speed of the restatement against the reference's own traversal compiled from
+# its sources (oracle/time_port_vs_reference.py: the frame's 6,073,008 rays,
+# nearest hit for every ray, identical results, same machine and threads).
+# The reference's sources exist only where the checker is built, so the factor
+# is a recorded measurement: the port runs this much faster than the
+# reference, i.e. the reference itself would be this much slower than the
+# CPU baseline reported here.
+PORT_OVER_REFERENCE = {"min": 1.08, "max": 1.21, "machine": "x86-64 Xeon @ 2.7 GHz, 8 and 1 threads",
+                       "script": "oracle/time_port_vs_reference.py"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -310,7 +321,7 @@ def run_reference(args):
         "config": {"workload": w.name, "tris": int(w.idx.size // 3), "eye_rays": int(n_eye), "ao_rays": int(n_ao),
                    "parallelism": "cpu", "l2": "n/a (host)"},
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": int(used), "kind": "port", "sample": sample,
-                         "cpu": host_cpu()},
+                         "cpu": host_cpu(), "port_over_reference": PORT_OVER_REFERENCE},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -1362,7 +1373,7 @@ def run_engine(args):
         if not args.no_cpu_baseline:
             rate, used, sample = cpu_trace_rate(o, w.eye_rays, ao, args.cpu_seconds)
             line["cpu_baseline"] = {"value": round(rate, 3), "unit": UNIT, "cores": int(used), "kind": "port",
-                                    "sample": sample, "cpu": host_cpu()}
+                                    "sample": sample, "cpu": host_cpu(), "port_over_reference": PORT_OVER_REFERENCE}
         if not args.no_oracle_check:
             # every ray of the frame against the oracle (after the timed region):
             # the timed layout's device-resident eye hits and AO flags, and the
