@@ -88,6 +88,9 @@ def parse():
     p.add_argument("--only-build-batched", type=int, default=0, metavar="K",
                    help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
     p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
+    p.add_argument("--l2-persist", type=int, default=0, metavar="MIB",
+                   help="persisting-L2 window over the headline scene's nodes (MiB set aside; 0 none)")
+    p.add_argument("--no-l2-sweep", action="store_true", help="skip the persisting-L2 window sweep")
     p.add_argument("--no-oracle-check", action="store_true",
                    help="skip the check of every ray of the headline frame against the oracle")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
@@ -610,6 +613,40 @@ def run_precision(ctx, args) -> dict:
     return res
 
 
+def run_l2_window(scene, d_eye, d_ao, d_hits, d_any, args) -> dict:
+    """The headline scene's eye and AO launches with a persisting-L2 window
+    over its node array (hrt OPTION_L2_PERSIST) of 0 / 16 / 32 / 64 MiB set
+    aside; results must equal the launches without a window."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    n_eye, n_ao = d_eye.shape[0], d_ao.shape[0]
+    want_h, want_a = d_hits.clone(), d_any.clone()
+    out = {"node_bytes": int(scene.export(0, 9).nbytes) if args.layout != "bvh2" else None, "sweep": []}
+    steps = max(5, min(40, args.steps))
+    for mib in (0, 16, 32, 64, 0):
+        scene.set_l2_persist(mib)
+        for _ in range(3):
+            scene.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+            scene.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        for _ in range(steps):
+            scene.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
+        e[1].record(stream)
+        for _ in range(steps):
+            scene.query_device(1, d_ao.data_ptr(), n_ao, d_any.data_ptr(), sh)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        out["sweep"].append({"mib": mib, "eye_ms": round(e[0].elapsed_time(e[1]) / steps, 4),
+                             "ao_ms": round(e[1].elapsed_time(e[2]) / steps, 4),
+                             "results_equal": bool(torch.equal(d_hits, want_h) and torch.equal(d_any, want_a))})
+    scene.set_l2_persist(args.l2_persist)
+    return out
+
+
 def edge_distance64(rays, verts, sorted_idx, prim):
     """Smallest FP64 barycentric of each ray against the triangle at sorted
     position prim (negative: outside): the ray's distance to the triangle's
@@ -1071,6 +1108,8 @@ def run_engine(args):
         return sc, g
 
     scene, gid = make_scene(args.layout)
+    if args.l2_persist:
+        scene.set_l2_persist(args.l2_persist)
     info = scene.geom_info(gid)
     # build time: a few more builds of the same geometry
     build_ms = [info["build_ms"]]
@@ -1349,6 +1388,8 @@ def run_engine(args):
         line["plain"] = plain
         line["speedup_vs_plain"] = round(line["value"] / plain["mrays_s"], 3)
 
+    if not args.no_l2_sweep:
+        line["l2_window"] = run_l2_window(scene, d_eye, d_ao, d_hits, d_any, args)
     if not args.no_watertight:
         line["watertight"] = run_watertight(ctx, args, w, ao, d_hits.cpu().numpy().view(np.uint32),
                                             d_any.cpu().numpy().astype(bool),
@@ -1421,6 +1462,10 @@ def summarize(line: dict):
                 cfg[f"c2_{name}_{lay}_mrays_s"] = e["mrays_s"]
                 bad += sum(v for k, v in e.items() if "mismatch" in k)
         cfg["c2_hit_mismatches"] = int(bad)
+    if "l2_window" in line:
+        for e in line["l2_window"]["sweep"][:-1]:
+            cfg[f"l2_window_{e['mib']}mib_ao_ms"] = e["ao_ms"]
+            cfg[f"l2_window_{e['mib']}mib_eye_ms"] = e["eye_ms"]
     if "watertight" in line:
         wt = line["watertight"]
         cfg["watertight_mrays_s"] = wt["mrays_s"]

@@ -825,6 +825,20 @@ int launch_query(hrt_scene* s, int kind, const float* rays, uint64_t n, void* ou
   }
   if (s->single && !q.rayOffsets) a.one = &s->singleDesc;
   a.triTest = s->triTest;
+  if (a.one && s->l2PersistMB > 0)
+  {
+    // L2 window over the geometry's nodes: as much of the array as the
+    // device's window and the persisting set-aside hold, the share of it
+    // that fits the set-aside marked persisting
+    int maxWin = 0, maxPersist = 0;
+    cudaDeviceGetAttribute(&maxWin, cudaDevAttrMaxAccessPolicyWindowSize, s->ctx->device);
+    cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, s->ctx->device);
+    const size_t setAside = std::min<size_t>((size_t)s->l2PersistMB << 20, (size_t)maxPersist);
+    a.persistBase = s->layout == HRT_LAYOUT_BVH2 ? static_cast<const void*>(s->singleDesc.recs) : s->singleDesc.nodes4;
+    a.persistBytes = std::min<size_t>(s->singleNodeBytes, (size_t)maxWin);
+    a.persistHitRatio = a.persistBytes ? std::min(1.0f, (float)setAside / (float)a.persistBytes) : 0.0f;
+    if (setAside == 0) a.persistBytes = 0;
+  }
   cudaError_t e = trace(a, kind, counting, s->layout, q.config ? *q.config : s->cfg[kind], s->ctx->numSMs, st);
   if (e != cudaSuccess) return cuda_fail(s->ctx, e, "trace launch");
   return HRT_OK;
@@ -1154,7 +1168,15 @@ int hrt_commit_scene(hrt_scene* s, int quality)
   s->dInst = nullptr;
   s->nInstDev = (uint32_t)d.size();
   s->single = d.size() == 1 && d[0].identity && d[0].valid && s->tlas.nTris == 0;
-  if (s->single) s->singleDesc = d[0];
+  if (s->single)
+  {
+    s->singleDesc = d[0];
+    const Geom& g0 = s->geoms[s->insts[0].geomId];
+    s->singleNodeBytes = s->layout == HRT_LAYOUT_BVH2 ? sizeof(PairRec) * (size_t)(g0.nLeaves > 1 ? g0.nLeaves - 1 : 1)
+                                                      : (s->layout == HRT_LAYOUT_BVH4_F32 ? sizeof(Node4F32)
+                                                                                         : sizeof(Node4F16)) *
+                                                            (size_t)g0.nNodes4;
+  }
   if (!d.empty())
   {
     HRT_CUDA(ctx, cudaMalloc((void**)&s->dInst, sizeof(InstanceDesc) * d.size()));
@@ -1481,6 +1503,22 @@ int hrt_scene_set_option(hrt_scene* s, int option, int value)
       s->useTlas = value;
       s->committed = false;
       return HRT_OK;
+    case HRT_OPTION_L2_PERSIST:
+    {
+      if (value < 0 || value > 4096) return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "L2 persisting size out of range");
+      int maxPersist = 0;
+      cudaSetDevice(s->ctx->device);
+      if (cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, s->ctx->device) != cudaSuccess)
+        return fail(s->ctx, HRT_ERR_CUDA, "cannot read the persisting L2 capacity");
+      if (value > 0 && maxPersist == 0) return fail(s->ctx, HRT_ERR_UNSUPPORTED, "device has no persisting L2");
+      // the set-aside is a limit of the process's context on this device
+      const size_t bytes = std::min<size_t>((size_t)value << 20, (size_t)maxPersist);
+      if ((value > 0 || s->l2PersistMB > 0) && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes) != cudaSuccess)
+        return fail(s->ctx, HRT_ERR_CUDA, "cannot set the persisting L2 size");
+      if (value == 0 && s->l2PersistMB > 0) cudaCtxResetPersistingL2Cache();  // persisting lines back to normal
+      s->l2PersistMB = value;
+      return HRT_OK;
+    }
     case HRT_OPTION_TRIANGLE_TEST:
       if (value != HRT_TRI_MOLLER_TRUMBORE && value != HRT_TRI_WATERTIGHT)
         return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown triangle test");

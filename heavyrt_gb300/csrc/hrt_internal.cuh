@@ -79,6 +79,8 @@ struct hrt_scene
   int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
   int                   useTlas = 1;    // HRT_OPTION_TLAS
   int                   triTest = 0;    // HRT_OPTION_TRIANGLE_TEST
+  int                   l2PersistMB = 0;  // HRT_OPTION_L2_PERSIST
+  size_t                singleNodeBytes = 0;  // node array of the single instance's geometry
   Geom                  tlas;           // instance tree of the committed scene (nTris = 0: none)
   InstanceDesc*         dInst = nullptr;
   uint32_t              nInstDev = 0;

@@ -203,6 +203,11 @@ struct TraceArgs
   // triangle test of every geometry traced: 0 Moller-Trumbore (records
   // {A, B-A, C-A}), 1 watertight (records {A, B, C})
   int                 triTest = 0;
+  // L2 access-policy window of the single-instance kernels (bytes = 0: none):
+  // this range of the node array is marked persisting in L2
+  const void*         persistBase = nullptr;
+  size_t              persistBytes = 0;
+  float               persistHitRatio = 1.0f;
 };
 
 // Launch shape of the traversal (tuned per workload).

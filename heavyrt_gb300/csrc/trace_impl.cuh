@@ -1027,14 +1027,30 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   const size_t smem = sizeof(uint32_t) * (size_t)shared * THREADS;
   const InstanceDesc& d = *a.one;
   const void* nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
+  // launch configuration, with the L2 access-policy window when one is asked for
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t lc = {};
+  lc.blockDim = dim3(THREADS);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = s;
+  if (a.persistBytes)
+  {
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(a.persistBase);
+    attr[0].val.accessPolicyWindow.num_bytes = a.persistBytes;
+    attr[0].val.accessPolicyWindow.hitRatio = a.persistHitRatio;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+  }
   if (!c.persistent)
   {
     cudaError_t e = allow_smem(k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, smem);
     if (e != cudaSuccess) return e;
-    k_trace_one_grid<LAYOUT, TRI, ANY, THREADS><<<(uint32_t)(((uint64_t)n + THREADS - 1) / THREADS), THREADS, smem,
-                                                  s>>>(a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits,
-                                                       a.errorWord, shared);
-    return cudaGetLastError();
+    lc.gridDim = dim3((uint32_t)(((uint64_t)n + THREADS - 1) / THREADS));
+    return cudaLaunchKernelEx(&lc, k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, a.rays, n, nodes, d.tris, d.instId,
+                              d.geomId, a.hits, a.errorWord, shared);
   }
   cudaError_t e = allow_smem(k_trace_one<LAYOUT, TRI, ANY, THREADS>, smem);
   if (e != cudaSuccess) return e;
@@ -1047,10 +1063,9 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   if (blocks > need) blocks = need;
   e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
-  k_trace_one<LAYOUT, TRI, ANY, THREADS><<<(uint32_t)blocks, THREADS, smem, s>>>(
-      a.rays, n, nodes, d.tris, d.instId, d.geomId, a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill,
-      c.refillLanes, shared);
-  return cudaGetLastError();
+  lc.gridDim = dim3((uint32_t)blocks);
+  return cudaLaunchKernelEx(&lc, k_trace_one<LAYOUT, TRI, ANY, THREADS>, a.rays, n, nodes, d.tris, d.instId, d.geomId,
+                            a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes, shared);
 }
 
 template <int LAYOUT, int TRI>

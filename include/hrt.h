@@ -146,6 +146,17 @@ int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
 #define HRT_OPTION_TRIANGLE_TEST 3
 #define HRT_TRI_MOLLER_TRUMBORE  0
 #define HRT_TRI_WATERTIGHT       1
+/*   HRT_OPTION_L2_PERSIST  value > 0: the node array of a scene of one
+ *                          untransformed geometry is kept in L2 for its
+ *                          queries: the process's persisting-L2 set-aside on
+ *                          the scene's device becomes `value` MiB (capped by
+ *                          the device's maximum; a context-wide limit that
+ *                          ends with the process), and each traversal launch
+ *                          marks the node array persisting through an
+ *                          access-policy window (the share that fits the
+ *                          set-aside).  0 (default): no window.  Results
+ *                          never depend on it. */
+#define HRT_OPTION_L2_PERSIST 4
 int hrt_scene_set_option(hrt_scene* scene, int option, int value);
 
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */

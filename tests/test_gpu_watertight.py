@@ -227,6 +227,7 @@ def test_watertight_batch_refit_and_blob(native, tmp_path):
     r.ClearScene()
     r.AddInstance(gid2)
     r.CommitScene()
+    want[want[:, 3] != MISS, 3] = gid2  # the restored geometry's id in this scene
     np.testing.assert_array_equal(_u32(r.RayQuery_NearestHit(rays[1])), want)
     r.close()
     mt = SceneRT(layout="bvh4_f16")
