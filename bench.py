@@ -88,6 +88,8 @@ def parse():
     p.add_argument("--only-build-batched", type=int, default=0, metavar="K",
                    help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
     p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
+    p.add_argument("--eye-order", default="tiles", choices=["tiles", "given"],
+                   help="eye rays traced in 8x4 pixel tiles of the image (index arithmetic) or in the order given")
     p.add_argument("--l2-persist", type=int, default=0, metavar="MIB",
                    help="persisting-L2 window over the headline scene's nodes (MiB set aside; 0 none)")
     p.add_argument("--no-l2-sweep", action="store_true", help="skip the persisting-L2 window sweep")
@@ -1139,13 +1141,21 @@ def run_engine(args):
     eye_bytes = node_bytes * eye_pairs + TRI_BYTES * eye_tris + RAY_BYTES * n_eye + 32 * n_eye
     ao_bytes = node_bytes * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
 
+    # the eye rays are one row-major image: let the traversal take them in
+    # 8 x 4 pixel tiles (the autotuner keeps this property of the rays)
+    if args.eye_order == "tiles":
+        scene.set_trace_config(0, imageWidth=args.width)
     tuned = None
     fixed = {0: args.launch_nearest, 1: args.launch_any}
     if any(fixed.values()) or (not args.no_autotune and not args.ncu):
         tuned = {}
         for kind, (dr, n, do) in enumerate(((d_eye, n_eye, d_hits), (d_ao, n_ao, d_any))):
             if fixed[kind]:
-                scene.set_trace_config(kind, *[int(x) for x in fixed[kind].split(",")])
+                vals = [int(x) for x in fixed[kind].split(",")]
+                cfg = dict(zip(["threadsPerBlock", "persistent", "stepsPerRefill", "refillLanes", "stackEntries"],
+                               vals))
+                cfg["imageWidth"] = scene.trace_config(kind)["imageWidth"]
+                scene.set_trace_config(kind, **cfg)
                 tuned[kind] = scene.trace_config(kind)
             elif not args.no_autotune and not args.ncu:
                 tuned[kind], _ = scene.autotune(E.query_desc(kind, dr.data_ptr(), n, do.data_ptr()), 3)
@@ -1383,6 +1393,8 @@ def run_engine(args):
         "clocks": clk,
     }
     line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
+    line["config"]["eye_ray_order"] = (f"8x4 pixel tiles of the {args.width}-wide image (index arithmetic, results "
+                                       "in ray order)" if args.eye_order == "tiles" else "as given (row-major)")
     line["config"]["launch"] = tuned if tuned is not None else "default"
     if plain is not None:
         line["plain"] = plain

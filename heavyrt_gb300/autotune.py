@@ -72,7 +72,7 @@ def apply(scene: E.SceneRT, result: TuneResult):
     """Sets a tuned launch shape on a scene built with result's structure."""
     for kind, c in result.configs.items():
         scene.set_trace_config(kind, c["threadsPerBlock"], c["persistent"], c["stepsPerRefill"], c["refillLanes"],
-                               c["stackEntries"])
+                               c["stackEntries"], c["imageWidth"])
 
 
 def seg_inst_identity(n: int) -> np.ndarray:

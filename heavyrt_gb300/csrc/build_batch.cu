@@ -293,14 +293,20 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
                                                          uint32_t* __restrict__ parent, uint32_t* __restrict__ rangeEnd)
 {
   const uint32_t Itot = counts[1];
-  for (uint32_t j = blockIdx.x * kThreads + threadIdx.x; j < Itot; j += gridDim.x * kThreads)
+  // a warp's 32 consecutive internal nodes searched together (lanes may
+  // belong to different geometries); the loop bound is uniform over the warp
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < Itot; base += gridDim.x * kThreads)
   {
-    const uint32_t s = find_segment(intOffsets, G, j);
-    const int L = (int)(leafOffsets[s + 1] - leafOffsets[s]);
-    const int i = (int)(j - intOffsets[s]);
-    uint32_t left, right;
-    int other;
-    bc::karras_node(compressed + leafOffsets[s], L, i, left, right, other);
+    const uint32_t j = base + lane;
+    const bool active = j < Itot;
+    const uint32_t s = active ? find_segment(intOffsets, G, j) : 0u;
+    const int L = active ? (int)(leafOffsets[s + 1] - leafOffsets[s]) : 0;
+    const int i = active ? (int)(j - intOffsets[s]) : 0;
+    uint32_t left = 0, right = 0;
+    int other = 0;
+    bc::karras_node_warp(compressed, active ? (int)leafOffsets[s] : 0, L, i, active, left, right, other);
+    if (!active) continue;
     const uint32_t nb = nodeOffsets[s];
     lr[nb + i].leftOffset = left;
     lr[nb + i].escapeIndex = right;

@@ -1542,7 +1542,8 @@ int hrt_scene_set_trace_config(hrt_scene* s, int kind, const hrt_trace_config* c
   if (!s || !c || (kind != 0 && kind != 1)) return HRT_ERR_INVALID_ARGUMENT;
   if ((c->threadsPerBlock != 64 && c->threadsPerBlock != 128 && c->threadsPerBlock != 256) ||
       (c->persistent != 0 && c->persistent != 1) || c->stepsPerRefill < 1 || c->stepsPerRefill > 1024 ||
-      c->refillLanes < 1 || c->refillLanes > 32 || c->stackEntries < 0 || c->stackEntries > HRT_MAX_STACK_ENTRIES)
+      c->refillLanes < 1 || c->refillLanes > 32 || c->stackEntries < 0 || c->stackEntries > HRT_MAX_STACK_ENTRIES ||
+      c->imageWidth < 0)
     return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "trace config out of range");
   std::lock_guard<std::mutex> g(s->mu);
   s->cfg[kind].threadsPerBlock = c->threadsPerBlock;
@@ -1550,6 +1551,7 @@ int hrt_scene_set_trace_config(hrt_scene* s, int kind, const hrt_trace_config* c
   s->cfg[kind].stepsPerRefill = c->stepsPerRefill;
   s->cfg[kind].refillLanes = c->refillLanes;
   s->cfg[kind].stackEntries = c->stackEntries;
+  s->cfg[kind].imageWidth = c->imageWidth;
   return HRT_OK;
 }
 
@@ -1561,6 +1563,7 @@ int hrt_scene_get_trace_config(const hrt_scene* s, int kind, hrt_trace_config* c
   c->stepsPerRefill = s->cfg[kind].stepsPerRefill;
   c->refillLanes = s->cfg[kind].refillLanes;
   c->stackEntries = s->cfg[kind].stackEntries;
+  c->imageWidth = s->cfg[kind].imageWidth;
   return HRT_OK;
 }
 
@@ -1666,6 +1669,7 @@ int hrt_scene_autotune(hrt_scene* s, const hrt_query_desc* q, int repeats, hrt_t
   for (int tpb : {64, 128, 256})
   {
     TraceConfig c;
+    c.imageWidth = s->cfg[q->kind].imageWidth;  // a property of the rays, kept
     c.threadsPerBlock = tpb;
     c.persistent = 0;
     grid.push_back(c);
@@ -1763,6 +1767,7 @@ int hrt_scene_autotune(hrt_scene* s, const hrt_query_desc* q, int repeats, hrt_t
     best->stepsPerRefill = bestC.stepsPerRefill;
     best->refillLanes = bestC.refillLanes;
     best->stackEntries = bestC.stackEntries;
+    best->imageWidth = bestC.imageWidth;
   }
   if (bestMs) *bestMs = bestT;
   return HRT_OK;

@@ -59,6 +59,43 @@ template <int LAYOUT, bool TLAS = false> struct StackDepth
 
 constexpr uint32_t kTlasMode = 0xFFFFFFFEu;  // Lane::inst while the lane walks the instance tree
 
+// Order in which a launch takes its rays.  With width > 0 the rays form
+// row-major images `width` rays wide, and work item i maps to a pixel of an
+// 8 x 4 tile (32 consecutive work items = one warp = one tile, tiles row after
+// row): neighbouring pixels trace together.  Index arithmetic only; each ray's
+// result still goes to the ray's own index.
+struct RayOrder
+{
+  uint32_t nWork;        // work items (>= rays; tiles that cross the image edge pad it)
+  uint32_t width;        // 0: work item i is ray i
+  uint32_t tilesPerRow;
+};
+
+__device__ __forceinline__ uint32_t work_ray(const RayOrder& o, uint32_t i, uint32_t n)
+{
+  if (o.width == 0) return i < n ? i : kNoRay;
+  const uint32_t t = i >> 5, l = i & 31u;
+  const uint32_t x = (t % o.tilesPerRow) * 8u + (l & 7u);
+  const uint32_t y = (t / o.tilesPerRow) * 4u + (l >> 3);
+  if (x >= o.width) return kNoRay;
+  const uint64_t r = (uint64_t)y * o.width + x;
+  return r < n ? (uint32_t)r : kNoRay;
+}
+
+__host__ __forceinline__ RayOrder ray_order(uint32_t n, int width)
+{
+  RayOrder o{n, 0u, 0u};
+  if (width <= 0 || n == 0) return o;
+  const uint64_t w = (uint64_t)width;
+  const uint64_t tilesPerRow = (w + 7) / 8, rows = (n + w - 1) / w;
+  const uint64_t work = tilesPerRow * ((rows + 3) / 4) * 32;
+  if (work > 0x7FFFFFFFull) return o;  // too much padding for 32-bit work counters: rays in order
+  o.nWork = (uint32_t)work;
+  o.width = (uint32_t)w;
+  o.tilesPerRow = (uint32_t)tilesPerRow;
+  return o;
+}
+
 // A lane's traversal stack: entries below `shared` in shared memory (entry k
 // of thread t at sh[k * THREADS]), the rest in the lane's spill array.
 template <int THREADS> struct Stack
@@ -785,7 +822,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
                                                         const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
                                                         void* out, unsigned long long* counters, uint32_t* errorWord,
                                                         unsigned int* rayCounter, int steps, int refill,
-                                                        int stackShared)
+                                                        int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
   uint32_t spill[StackDepth<LAYOUT, TLAS>::value];
@@ -805,11 +842,12 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(rayCounter, (unsigned int)__popc(idle));
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+      if (base + (uint32_t)__popc(idle) >= order.nWork) exhausted = true;
       if (L.ray == kNoRay)
       {
-        const uint32_t i = base + __popc(idle & ltMask);
-        if (i < n)
+        const uint32_t w = base + __popc(idle & ltMask);
+        const uint32_t i = w < order.nWork ? work_ray(order, w, n) : kNoRay;
+        if (i != kNoRay)
         {
           start_ray(L, i, rays);
           bool live = true;
@@ -845,14 +883,15 @@ template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
 __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict__ rays, uint32_t n,
                                                         const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
                                                         void* out, unsigned long long* counters, uint32_t* errorWord,
-                                                        int stackShared)
+                                                        int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
   uint32_t spill[StackDepth<LAYOUT, TLAS>::value];
   Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
   uint64_t nPairs = 0, nTris = 0;
-  const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
-  if (i < n)
+  const uint32_t w = blockIdx.x * THREADS + threadIdx.x;
+  const uint32_t i = w < order.nWork ? work_ray(order, w, n) : kNoRay;
+  if (i != kNoRay)
   {
     Lane L;
     start_ray(L, i, rays);
@@ -946,7 +985,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
                                                        const void* __restrict__ nodes, const TriRec* __restrict__ tris,
                                                        uint32_t instId, uint32_t geomId, void* out,
                                                        uint32_t* errorWord, unsigned int* rayCounter, int steps,
-                                                       int refill, int stackShared)
+                                                       int refill, int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
   uint32_t spill[StackDepth<LAYOUT, false>::value];
@@ -967,11 +1006,12 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(rayCounter, (unsigned int)__popc(idle));
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
-      if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+      if (base + (uint32_t)__popc(idle) >= order.nWork) exhausted = true;
       if (L.ray == kNoRay)
       {
-        const uint32_t i = base + __popc(idle & ltMask);
-        if (i < n) start_ray_one(L, i, rays);
+        const uint32_t w = base + __popc(idle & ltMask);
+        const uint32_t i = w < order.nWork ? work_ray(order, w, n) : kNoRay;
+        if (i != kNoRay) start_ray_one(L, i, rays);
       }
     }
     if (L.ray != kNoRay)
@@ -996,13 +1036,14 @@ template <int LAYOUT, int TRI, bool ANY, int THREADS>
 __global__ void __launch_bounds__(THREADS)
     k_trace_one_grid(const float4* __restrict__ rays, uint32_t n, const void* __restrict__ nodes,
                      const TriRec* __restrict__ tris, uint32_t instId, uint32_t geomId, void* out, uint32_t* errorWord,
-                     int stackShared)
+                     int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
   uint32_t spill[StackDepth<LAYOUT, false>::value];
   Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
-  const uint32_t i = blockIdx.x * THREADS + threadIdx.x;
-  if (i >= n) return;
+  const uint32_t w = blockIdx.x * THREADS + threadIdx.x;
+  const uint32_t i = w < order.nWork ? work_ray(order, w, n) : kNoRay;
+  if (i == kNoRay) return;
   Lane1 L;
   L.nodes = nodes;
   L.tris = tris;
@@ -1025,6 +1066,7 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   const uint32_t n = (uint32_t)a.n;
   const int shared = shared_entries<StackDepth<LAYOUT, false>::value>(c.stackEntries);
   const size_t smem = sizeof(uint32_t) * (size_t)shared * THREADS;
+  const RayOrder order = ray_order(n, c.imageWidth);
   const InstanceDesc& d = *a.one;
   const void* nodes = LAYOUT == 0 ? static_cast<const void*>(d.recs) : d.nodes4;
   // launch configuration, with the L2 access-policy window when one is asked for
@@ -1048,9 +1090,9 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   {
     cudaError_t e = allow_smem(k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, smem);
     if (e != cudaSuccess) return e;
-    lc.gridDim = dim3((uint32_t)(((uint64_t)n + THREADS - 1) / THREADS));
+    lc.gridDim = dim3((uint32_t)(((uint64_t)order.nWork + THREADS - 1) / THREADS));
     return cudaLaunchKernelEx(&lc, k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, a.rays, n, nodes, d.tris, d.instId,
-                              d.geomId, a.hits, a.errorWord, shared);
+                              d.geomId, a.hits, a.errorWord, shared, order);
   }
   cudaError_t e = allow_smem(k_trace_one<LAYOUT, TRI, ANY, THREADS>, smem);
   if (e != cudaSuccess) return e;
@@ -1059,13 +1101,13 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   if (e != cudaSuccess) return e;
   if (perSM < 1) perSM = 1;
   uint64_t blocks = (uint64_t)numSMs * perSM;
-  const uint64_t need = ((uint64_t)n + THREADS - 1) / THREADS;
+  const uint64_t need = ((uint64_t)order.nWork + THREADS - 1) / THREADS;
   if (blocks > need) blocks = need;
   e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   lc.gridDim = dim3((uint32_t)blocks);
   return cudaLaunchKernelEx(&lc, k_trace_one<LAYOUT, TRI, ANY, THREADS>, a.rays, n, nodes, d.tris, d.instId, d.geomId,
-                            a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes, shared);
+                            a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes, shared, order);
 }
 
 template <int LAYOUT, int TRI>
@@ -1093,6 +1135,7 @@ cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStr
   const Tlas tl{a.tlasRecs, a.tlasTris, a.nInst};
   const int shared = shared_entries<StackDepth<LAYOUT, TLAS>::value>(c.stackEntries);
   const size_t smem = sizeof(uint32_t) * (size_t)shared * THREADS;
+  const RayOrder order = ray_order(n, c.imageWidth);
   if (c.persistent && !COUNT)
   {
     cudaError_t e = allow_smem(k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>, smem);
@@ -1103,21 +1146,21 @@ cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStr
     if (e != cudaSuccess) return e;
     if (perSM < 1) perSM = 1;
     uint64_t blocks = (uint64_t)numSMs * perSM;
-    const uint64_t need = ((uint64_t)n + THREADS - 1) / THREADS;
+    const uint64_t need = ((uint64_t)order.nWork + THREADS - 1) / THREADS;
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
     k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
         a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes,
-        shared);
+        shared, order);
   }
   else
   {
     cudaError_t e = allow_smem(k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>, smem);
     if (e != cudaSuccess) return e;
-    const uint64_t blocks = ((uint64_t)n + THREADS - 1) / THREADS;
+    const uint64_t blocks = ((uint64_t)order.nWork + THREADS - 1) / THREADS;
     k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
-        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, shared);
+        a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, shared, order);
   }
   return cudaGetLastError();
 }

@@ -73,7 +73,7 @@ class TraceConfig(C.Structure):
     """hrt_trace_config (include/hrt.h): launch shape of the traversal kernel."""
 
     _fields_ = [("threadsPerBlock", C.c_int), ("persistent", C.c_int), ("stepsPerRefill", C.c_int),
-                ("refillLanes", C.c_int), ("stackEntries", C.c_int)]
+                ("refillLanes", C.c_int), ("stackEntries", C.c_int), ("imageWidth", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -503,8 +503,8 @@ class SceneRT:
         return int(c[0]), int(c[1])
 
     def set_trace_config(self, kind: int, threadsPerBlock=128, persistent=1, stepsPerRefill=16, refillLanes=24,
-                         stackEntries=0):
-        c = TraceConfig(threadsPerBlock, persistent, stepsPerRefill, refillLanes, stackEntries)
+                         stackEntries=0, imageWidth=0):
+        c = TraceConfig(threadsPerBlock, persistent, stepsPerRefill, refillLanes, stackEntries, imageWidth)
         self.ctx.check(lib().hrt_scene_set_trace_config(self._h, kind, C.byref(c)), "set_trace_config")
 
     def trace_config(self, kind: int) -> dict:

@@ -247,6 +247,8 @@ int hrt_scene_check(hrt_scene* scene);
  * one ray per virtual call with an 80-entry stack, core/raytrace_common.h:34).
  * Defaults: 128 threads, persistent pool, 16 steps between refills, refill at
  * 24 idle lanes, the whole stack in shared memory.
+ * imageWidth is a property of the rays the kind's queries pass (the
+ * autotuner keeps it).
  * stackEntries: traversal stack entries per ray kept in shared memory; deeper
  * entries spill to the thread's local memory, so any value is correct for any
  * tree.  0, or a value at or above the layout's depth bound (32 binary, 48
@@ -259,6 +261,10 @@ typedef struct hrt_trace_config
   int stepsPerRefill;  /* traversal steps between refill checks (1..1024)        */
   int refillLanes;     /* a warp refills when at least this many lanes are idle (1..32) */
   int stackEntries;    /* short-stack entries in shared memory (0..HRT_MAX_STACK_ENTRIES) */
+  int imageWidth;      /* > 0: the rays form row-major images this many rays wide (as a
+                          renderer's eye rays do), and the traversal takes them in 8 x 4
+                          pixel tiles so that neighbouring pixels trace together; results
+                          still go to each ray's index.  0: rays taken in the order given */
 } hrt_trace_config;
 int hrt_scene_set_trace_config(hrt_scene* scene, int kind, const hrt_trace_config* config);
 int hrt_scene_get_trace_config(const hrt_scene* scene, int kind, hrt_trace_config* config);

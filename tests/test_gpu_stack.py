@@ -96,3 +96,52 @@ def test_stack_entries_out_of_range_refused(native):
     s.set_trace_config(0, 128, 1, 16, 24, 128)
     assert s.trace_config(0)["stackEntries"] == 128
     s.close()
+
+
+@pytest.mark.parametrize("layout", ["bvh2", "bvh4_f16"])
+def test_image_tile_order_gives_the_same_results(native, layout):
+    """Rays taken in 8 x 4 pixel tiles of row-major images (imageWidth): the
+    results of the given order, for widths that divide the ray count and that
+    do not, in the single-instance, two-level and segmented kernels."""
+    import torch
+
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    hv, hidx, _ = wl.heightfield(9, 96, 96)
+    rays = wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 203, 77)
+    for n_inst in (1, 3):
+        s = SceneRT(layout=layout)
+        gid = s.AddGeom_Triangles3f(hv, hv.shape[0], hidx, hidx.size, vByteStride=16)
+        for k in range(n_inst):
+            m = np.eye(4, dtype=np.float32)
+            m[2, 3] = 0.3 * k
+            s.AddInstance(gid, m)
+        s.CommitScene()
+        ref = s.RayQuery_NearestHit(rays).view(np.uint32)
+        ref_any = s.RayQuery_AnyHit(rays)
+        assert ref_any.any()
+        for width in (1, 7, 8, 203, 4096):
+            for persistent in (1, 0):
+                for kind in (0, 1):
+                    s.set_trace_config(kind, 128, persistent, 16, 24, 0, width)
+                np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), ref,
+                                              err_msg=f"{n_inst} {width} {persistent}")
+                np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), ref_any)
+        # segmented launch over the scene's instances with the tile order
+        if n_inst == 3:
+            dr = torch.from_numpy(rays).cuda()
+            offs = np.array([0, 5000, 9000, len(rays)], np.uint32)
+            do = torch.from_numpy(offs.view(np.int32)).cuda()
+            ds = torch.from_numpy(np.array([2, 0, 1], np.int32)).cuda()
+            outs = []
+            for width in (0, 203):
+                s.set_trace_config(0, 128, 1, 16, 24, 0, width)
+                out = torch.zeros((len(rays), 8), dtype=torch.int32, device="cuda")
+                s.query_multi(E.query_desc(0, dr.data_ptr(), len(rays), out.data_ptr(), do.data_ptr(),
+                                           ds.data_ptr(), 3))
+                torch.cuda.synchronize()
+                outs.append(out.cpu().numpy())
+            np.testing.assert_array_equal(outs[0], outs[1])
+        s.close()
