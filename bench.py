@@ -715,26 +715,40 @@ def run_watertight(ctx, args, w, ao, mt_hits, mt_any, configs) -> dict:
     hm, hw = mt_hits[:, 3] != 0xFFFFFFFF, wt[:, 3] != 0xFFFFFFFF
     differ = (hm != hw) | (hm & hw & (mt_hits[:, 1] != wt[:, 1]))
     idx = np.nonzero(differ)[0]
-    dist = np.full(idx.size, np.inf)
-    for hits, has in ((mt_hits, hm), (wt, hw)):
+    # FP64 smallest barycentric of the triangle each test hit (negative: the
+    # ray passes outside that triangle)
+    bm = np.full(idx.size, np.nan)
+    bw = np.full(idx.size, np.nan)
+    for hits, has, dst in ((mt_hits, hm, bm), (wt, hw, bw)):
         m = has[idx]
         if m.any():
-            dd = np.abs(edge_distance64(w.eye_rays[idx[m]], w.verts, si, hits[idx[m], 1]))
-            dist[m] = np.minimum(dist[m], dd)
-    bins = {"le_1e-7": int(np.count_nonzero(dist <= 1e-7)),
-            "le_1e-6": int(np.count_nonzero((dist > 1e-7) & (dist <= 1e-6))),
-            "le_1e-5": int(np.count_nonzero((dist > 1e-6) & (dist <= 1e-5))),
-            "gt_1e-5": int(np.count_nonzero(dist > 1e-5))}
+            dst[m] = edge_distance64(w.eye_rays[idx[m]], w.verts, si, hits[idx[m], 1])
+    slack = 1e-6  # the reference test's own barycentric slack
+    classes = {
+        # the reference's MT accepted a triangle the ray passes outside of, beyond its slack
+        "mt_hit_outside_beyond_slack": int(np.count_nonzero(bm < -slack)),
+        # the reference's MT missed while the ray passes inside the triangle the watertight test hit (a leak)
+        "mt_miss_inside": int(np.count_nonzero(~hm[idx] & (bw > 0))),
+        # the watertight test hit a triangle the FP64 ray passes outside of (its FP32 projection)
+        "wt_hit_outside_beyond_slack": int(np.count_nonzero(bw < -slack)),
+        # both within the slack of a shared edge: another of the triangles meeting there
+        "edge_ties": int(np.count_nonzero(((np.abs(bm) <= slack) | np.isnan(bm)) & ((np.abs(bw) <= slack) | np.isnan(bw)))),
+    }
+    depth = {"mt_outside_max": float(-np.nanmin(bm)) if np.any(bm < -slack) else 0.0,
+             "mt_leak_inside_max": float(np.nanmax(np.where(~hm[idx], bw, np.nan))) if np.any(~hm[idx] & (bw > 0))
+             else 0.0,
+             "wt_outside_max": float(-np.nanmin(bw)) if np.any(bw < -slack) else 0.0}
     same = hm & hw & (mt_hits[:, 1] == wt[:, 1])
     tm = mt_hits[same, 0].view(np.float32).astype(np.float64)
     tw = wt[same, 0].view(np.float32).astype(np.float64)
     return {"layout": args.layout, "eye_ms": round(eye_ms, 4), "ao_ms": round(ao_ms, 4),
             "mrays_s": round((n_eye + n_ao) / (eye_ms + ao_ms) / 1e3, 2),
             "eye_rays_differing_from_mt": int(idx.size), "eye_hits_mt": int(hm.sum()), "eye_hits_wt": int(hw.sum()),
-            "differing_by_edge_distance": bins,
+            "differing_by_class": classes, "barycentric_depth": depth,
             "same_triangle_t_max_rel_vs_mt": float((np.abs(tm - tw) / np.abs(tm)).max()) if tm.size else 0.0,
             "ao_rays_differing_from_mt": int(np.count_nonzero(wt_any != mt_any)),
-            "note": "edge distance = smallest FP64 barycentric (abs) of the ray against the triangle either test hit"}
+            "note": "barycentric = smallest FP64 barycentric of the ray against the triangle a test hit "
+                    "(negative: outside); MT accepts down to -1e-6"}
 
 
 # ---------------------------------------------------------------- served stream
@@ -1482,7 +1496,8 @@ def summarize(line: dict):
         wt = line["watertight"]
         cfg["watertight_mrays_s"] = wt["mrays_s"]
         cfg["watertight_eye_rays_differing_from_mt"] = wt["eye_rays_differing_from_mt"]
-        cfg["watertight_differing_beyond_1e-5_of_an_edge"] = wt["differing_by_edge_distance"]["gt_1e-5"]
+        for k, v in wt["differing_by_class"].items():
+            cfg[f"watertight_{k}"] = v
         cfg["watertight_ao_rays_differing_from_mt"] = wt["ao_rays_differing_from_mt"]
     if "frames" in line:
         cfg["frames_rtao_mrays_s"] = line["frames"]["rtao"]["mrays_s"]

@@ -97,18 +97,23 @@ __host__ __forceinline__ RayOrder ray_order(uint32_t n, int width)
 }
 
 // A lane's traversal stack: entries below `shared` in shared memory (entry k
-// of thread t at sh[k * THREADS]), the rest in the lane's spill array.
-template <int THREADS> struct Stack
+// of thread t at sh[k * THREADS]), the rest in the lane's spill array.  The
+// kernels without spill (SPILL = false: the whole depth bound in shared
+// memory) keep the plain shared-memory addressing.
+template <int THREADS, bool SPILL> struct Stack
 {
   uint32_t* sh;
-  uint32_t* spill;  // DEPTH - shared entries (local memory)
+  uint32_t* spill;  // DEPTH - shared entries (local memory); unused without SPILL
   int       shared;
   __device__ __forceinline__ void put(int k, uint32_t v)
   {
-    if (k < shared) sh[k * THREADS] = v;
+    if (!SPILL || k < shared) sh[k * THREADS] = v;
     else spill[k - shared] = v;
   }
-  __device__ __forceinline__ uint32_t get(int k) const { return k < shared ? sh[k * THREADS] : spill[k - shared]; }
+  __device__ __forceinline__ uint32_t get(int k) const
+  {
+    return (!SPILL || k < shared) ? sh[k * THREADS] : spill[k - shared];
+  }
 };
 
 // Shared-memory entries per lane for a requested short-stack size (0 or
@@ -531,8 +536,8 @@ template <int LAYOUT> struct EndBit
 // otherwise, -1 when the stack bound would be exceeded (reported).
 // One child pair of a binary tree: BVH2TraverseC32's decisions
 // (core/BVH2CommonRT.cpp:88-113).
-template <bool COUNT, int THREADS, int DEPTH, typename LaneT>
-__device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ recs, Stack<THREADS>& st,
+template <bool COUNT, int THREADS, int DEPTH, bool SPILL, typename LaneT>
+__device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ recs, Stack<THREADS, SPILL>& st,
                                           uint64_t& nPairs, uint32_t* errorWord)
 {
   const float4* p = reinterpret_cast<const float4*>(recs + L.cur);
@@ -563,8 +568,8 @@ __device__ __forceinline__ int visit_pair(LaneT& L, const PairRec* __restrict__ 
   return 0;
 }
 
-template <int LAYOUT, bool ANY, bool COUNT, int THREADS, int DEPTH, typename LaneT>
-__device__ __forceinline__ int visit_node(LaneT& L, Stack<THREADS>& st, uint64_t& nPairs, uint32_t* errorWord)
+template <int LAYOUT, bool ANY, bool COUNT, int THREADS, int DEPTH, bool SPILL, typename LaneT>
+__device__ __forceinline__ int visit_node(LaneT& L, Stack<THREADS, SPILL>& st, uint64_t& nPairs, uint32_t* errorWord)
 {
   if constexpr (LAYOUT != 0)
   {
@@ -633,7 +638,8 @@ __device__ __forceinline__ int visit_node(LaneT& L, Stack<THREADS>& st, uint64_t
     return 0;
   }
   else
-    return visit_pair<COUNT, THREADS, DEPTH>(L, reinterpret_cast<const PairRec*>(L.nodes), st, nPairs, errorWord);
+    return visit_pair<COUNT, THREADS, DEPTH, SPILL>(L, reinterpret_cast<const PairRec*>(L.nodes), st, nPairs,
+                                                    errorWord);
 }
 
 // One traversal step (an internal node, or a leaf followed by a pop).
@@ -660,8 +666,8 @@ __device__ __forceinline__ void tlas_begin(Lane& L)
 }
 
 // Pops the instance tree's stack; true when the ray is finished.
-template <int THREADS>
-__device__ __forceinline__ bool tlas_pop(Lane& L, const Stack<THREADS>& st)
+template <int THREADS, bool SPILL>
+__device__ __forceinline__ bool tlas_pop(Lane& L, const Stack<THREADS, SPILL>& st)
 {
   if (L.top == 0) return true;
   L.top--;
@@ -671,9 +677,9 @@ __device__ __forceinline__ bool tlas_pop(Lane& L, const Stack<THREADS>& st)
 
 // Enters the next instance (with triangles) of the current TLAS leaf run; when
 // the run is done, returns to the instance tree.  True when the ray is finished.
-template <int LAYOUT, int THREADS>
+template <int LAYOUT, int THREADS, bool SPILL>
 __device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
-                                          const Stack<THREADS>& st)
+                                          const Stack<THREADS, SPILL>& st)
 {
   while (L.tnext != kNoRay)
   {
@@ -690,12 +696,12 @@ __device__ __forceinline__ bool tlas_next(Lane& L, const InstanceDesc* __restric
   }
   L.inst = kTlasMode;
   world_ray(L);
-  return tlas_pop<THREADS>(L, st);
+  return tlas_pop<THREADS, SPILL>(L, st);
 }
 
-template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS, bool SPILL>
 __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ inst, const Tlas& tl,
-                                     Stack<THREADS>& st, uint64_t& nPairs, uint64_t& nTris, uint32_t* errorWord)
+                                     Stack<THREADS, SPILL>& st, uint64_t& nPairs, uint64_t& nTris, uint32_t* errorWord)
 {
   constexpr int DEPTH = StackDepth<LAYOUT, TLAS>::value;
   if (TLAS && L.inst == kTlasMode)
@@ -703,18 +709,18 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
     // instance tree: a pair of instance boxes, or a leaf (a run of instances)
     if ((L.cur & kLeafBit) == 0u)
     {
-      const int r = visit_pair<COUNT, THREADS, DEPTH>(L, tl.recs, st, nPairs, errorWord);
+      const int r = visit_pair<COUNT, THREADS, DEPTH, SPILL>(L, tl.recs, st, nPairs, errorWord);
       if (r < 0) return true;
-      return r == 1 ? tlas_pop<THREADS>(L, st) : false;
+      return r == 1 ? tlas_pop<THREADS, SPILL>(L, st) : false;
     }
-    if (L.cur == kEmptyRef) return tlas_pop<THREADS>(L, st);
+    if (L.cur == kEmptyRef) return tlas_pop<THREADS, SPILL>(L, st);
     L.tnext = L.cur & ~kLeafBit;
-    return tlas_next<LAYOUT, THREADS>(L, inst, tl, st);
+    return tlas_next<LAYOUT, THREADS, SPILL>(L, inst, tl, st);
   }
   bool pop;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, ANY, COUNT, THREADS, DEPTH>(L, st, nPairs, errorWord);
+    const int r = visit_node<LAYOUT, ANY, COUNT, THREADS, DEPTH, SPILL>(L, st, nPairs, errorWord);
     if (r < 0) return true;
     pop = (r == 1);
   }
@@ -733,7 +739,7 @@ __device__ __forceinline__ bool step(Lane& L, const InstanceDesc* __restrict__ i
       L.cur = st.get(L.top);
       return false;
     }
-    if (TLAS) return tlas_next<LAYOUT, THREADS>(L, inst, tl, st);
+    if (TLAS) return tlas_next<LAYOUT, THREADS, SPILL>(L, inst, tl, st);
     return !begin_instance<LAYOUT>(L, inst, L.inst + 1);
   }
   return false;
@@ -817,7 +823,7 @@ __device__ __forceinline__ void flush_counters(uint64_t nPairs, uint64_t nTris, 
 
 // Persistent warp pool.  Lanes run `steps` traversal steps between refills; a
 // warp refills when at least `refill` lanes are idle (or all are).
-template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS, bool SPILL>
 __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict__ rays, uint32_t n,
                                                         const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
                                                         void* out, unsigned long long* counters, uint32_t* errorWord,
@@ -825,8 +831,8 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
                                                         int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
-  uint32_t spill[StackDepth<LAYOUT, TLAS>::value];
-  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
+  uint32_t spill[SPILL ? StackDepth<LAYOUT, TLAS>::value : 1];
+  Stack<THREADS, SPILL> st{s_stack + threadIdx.x, spill, stackShared};
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ltMask = (1u << lane) - 1u;
   uint64_t nPairs = 0, nTris = 0;
@@ -866,7 +872,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
       for (int s = 0; s < steps; s++)
       {
         if (out_of_budget(L, errorWord) ||
-            step<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>(L, inst, tl, st, nPairs, nTris, errorWord))
+            step<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL>(L, inst, tl, st, nPairs, nTris, errorWord))
         {
           write_result<ANY>(L, inst, out);
           L.ray = kNoRay;
@@ -879,15 +885,15 @@ __global__ void __launch_bounds__(THREADS) k_trace_pool(const float4* __restrict
 }
 
 // One thread per ray.
-template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS, bool SPILL>
 __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict__ rays, uint32_t n,
                                                         const InstanceDesc* __restrict__ inst, Segments sg, Tlas tl,
                                                         void* out, unsigned long long* counters, uint32_t* errorWord,
                                                         int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
-  uint32_t spill[StackDepth<LAYOUT, TLAS>::value];
-  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
+  uint32_t spill[SPILL ? StackDepth<LAYOUT, TLAS>::value : 1];
+  Stack<THREADS, SPILL> st{s_stack + threadIdx.x, spill, stackShared};
   uint64_t nPairs = 0, nTris = 0;
   const uint32_t w = blockIdx.x * THREADS + threadIdx.x;
   const uint32_t i = w < order.nWork ? work_ray(order, w, n) : kNoRay;
@@ -900,7 +906,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_grid(const float4* __restrict
     else live = begin_instance<LAYOUT>(L, inst, first_instance(L, i, sg));
     if (live)
       while (!out_of_budget(L, errorWord) &&
-             !step<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>(L, inst, tl, st, nPairs, nTris, errorWord)) {}
+             !step<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL>(L, inst, tl, st, nPairs, nTris, errorWord)) {}
     write_result<ANY>(L, inst, out);
   }
   flush_counters<COUNT>(nPairs, nTris, counters);
@@ -944,14 +950,14 @@ __device__ __forceinline__ void start_ray_one(Lane1& L, uint32_t i, const float4
 }
 
 // One step of the single-instance kernel; true when the ray is finished.
-template <int LAYOUT, int TRI, bool ANY, int THREADS>
-__device__ __forceinline__ bool step_one(Lane1& L, Stack<THREADS>& st, uint32_t* errorWord)
+template <int LAYOUT, int TRI, bool ANY, int THREADS, bool SPILL>
+__device__ __forceinline__ bool step_one(Lane1& L, Stack<THREADS, SPILL>& st, uint32_t* errorWord)
 {
   constexpr int DEPTH = StackDepth<LAYOUT, false>::value;
   uint64_t none = 0;
   if ((L.cur & kLeafBit) == 0u)
   {
-    const int r = visit_node<LAYOUT, ANY, false, THREADS, DEPTH>(L, st, none, errorWord);
+    const int r = visit_node<LAYOUT, ANY, false, THREADS, DEPTH, SPILL>(L, st, none, errorWord);
     if (r < 0) return true;
     if (r == 0) return false;
   }
@@ -980,7 +986,7 @@ __device__ __forceinline__ void write_result_one(const Lane1& L, uint32_t instId
 }
 
 // Persistent warp pool over one instance (the refill rule of k_trace_pool).
-template <int LAYOUT, int TRI, bool ANY, int THREADS>
+template <int LAYOUT, int TRI, bool ANY, int THREADS, bool SPILL>
 __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict__ rays, uint32_t n,
                                                        const void* __restrict__ nodes, const TriRec* __restrict__ tris,
                                                        uint32_t instId, uint32_t geomId, void* out,
@@ -988,8 +994,8 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
                                                        int refill, int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
-  uint32_t spill[StackDepth<LAYOUT, false>::value];
-  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
+  uint32_t spill[SPILL ? StackDepth<LAYOUT, false>::value : 1];
+  Stack<THREADS, SPILL> st{s_stack + threadIdx.x, spill, stackShared};
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ltMask = (1u << lane) - 1u;
   Lane1 L;
@@ -1018,7 +1024,7 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
     {
       for (int s = 0; s < steps; s++)
       {
-        if (out_of_budget(L, errorWord) || step_one<LAYOUT, TRI, ANY, THREADS>(L, st, errorWord))
+        if (out_of_budget(L, errorWord) || step_one<LAYOUT, TRI, ANY, THREADS, SPILL>(L, st, errorWord))
         {
           write_result_one<ANY>(L, instId, geomId, out);
           L.ray = kNoRay;
@@ -1032,15 +1038,15 @@ __global__ void __launch_bounds__(THREADS) k_trace_one(const float4* __restrict_
 // One thread per ray over one instance: a warp's 32 consecutive rays end
 // together, so their results go out as one contiguous kilobyte (results
 // written in place over the host link want this).
-template <int LAYOUT, int TRI, bool ANY, int THREADS>
+template <int LAYOUT, int TRI, bool ANY, int THREADS, bool SPILL>
 __global__ void __launch_bounds__(THREADS)
     k_trace_one_grid(const float4* __restrict__ rays, uint32_t n, const void* __restrict__ nodes,
                      const TriRec* __restrict__ tris, uint32_t instId, uint32_t geomId, void* out, uint32_t* errorWord,
                      int stackShared, RayOrder order)
 {
   extern __shared__ uint32_t s_stack[];  // stackShared * THREADS entries
-  uint32_t spill[StackDepth<LAYOUT, false>::value];
-  Stack<THREADS> st{s_stack + threadIdx.x, spill, stackShared};
+  uint32_t spill[SPILL ? StackDepth<LAYOUT, false>::value : 1];
+  Stack<THREADS, SPILL> st{s_stack + threadIdx.x, spill, stackShared};
   const uint32_t w = blockIdx.x * THREADS + threadIdx.x;
   const uint32_t i = w < order.nWork ? work_ray(order, w, n) : kNoRay;
   if (i == kNoRay) return;
@@ -1048,7 +1054,7 @@ __global__ void __launch_bounds__(THREADS)
   L.nodes = nodes;
   L.tris = tris;
   start_ray_one(L, i, rays);
-  while (!out_of_budget(L, errorWord) && !step_one<LAYOUT, TRI, ANY, THREADS>(L, st, errorWord)) {}
+  while (!out_of_budget(L, errorWord) && !step_one<LAYOUT, TRI, ANY, THREADS, SPILL>(L, st, errorWord)) {}
   write_result_one<ANY>(L, instId, geomId, out);
 }
 
@@ -1060,7 +1066,7 @@ template <typename K> cudaError_t allow_smem(K kernel, size_t smem)
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-template <int LAYOUT, int TRI, bool ANY, int THREADS>
+template <int LAYOUT, int TRI, bool ANY, int THREADS, bool SPILL>
 cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   const uint32_t n = (uint32_t)a.n;
@@ -1088,16 +1094,17 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   }
   if (!c.persistent)
   {
-    cudaError_t e = allow_smem(k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, smem);
+    cudaError_t e = allow_smem(k_trace_one_grid<LAYOUT, TRI, ANY, THREADS, SPILL>, smem);
     if (e != cudaSuccess) return e;
     lc.gridDim = dim3((uint32_t)(((uint64_t)order.nWork + THREADS - 1) / THREADS));
-    return cudaLaunchKernelEx(&lc, k_trace_one_grid<LAYOUT, TRI, ANY, THREADS>, a.rays, n, nodes, d.tris, d.instId,
-                              d.geomId, a.hits, a.errorWord, shared, order);
+    return cudaLaunchKernelEx(&lc, k_trace_one_grid<LAYOUT, TRI, ANY, THREADS, SPILL>, a.rays, n, nodes, d.tris,
+                              d.instId, d.geomId, a.hits, a.errorWord, shared, order);
   }
-  cudaError_t e = allow_smem(k_trace_one<LAYOUT, TRI, ANY, THREADS>, smem);
+  cudaError_t e = allow_smem(k_trace_one<LAYOUT, TRI, ANY, THREADS, SPILL>, smem);
   if (e != cudaSuccess) return e;
   int perSM = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_one<LAYOUT, TRI, ANY, THREADS>, THREADS, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_one<LAYOUT, TRI, ANY, THREADS, SPILL>, THREADS,
+                                                    smem);
   if (e != cudaSuccess) return e;
   if (perSM < 1) perSM = 1;
   uint64_t blocks = (uint64_t)numSMs * perSM;
@@ -1106,8 +1113,19 @@ cudaError_t launch_one(const TraceArgs& a, const TraceConfig& c, int numSMs, cud
   e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   lc.gridDim = dim3((uint32_t)blocks);
-  return cudaLaunchKernelEx(&lc, k_trace_one<LAYOUT, TRI, ANY, THREADS>, a.rays, n, nodes, d.tris, d.instId, d.geomId,
-                            a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes, shared, order);
+  return cudaLaunchKernelEx(&lc, k_trace_one<LAYOUT, TRI, ANY, THREADS, SPILL>, a.rays, n, nodes, d.tris, d.instId,
+                            d.geomId, a.hits, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes, shared,
+                            order);
+}
+
+// The short-stack variant only when the requested size leaves part of the
+// depth bound to local memory.
+template <int LAYOUT, int TRI, bool ANY, int THREADS>
+cudaError_t launch_one_any_stack(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  constexpr int DEPTH = StackDepth<LAYOUT, false>::value;
+  return shared_entries<DEPTH>(c.stackEntries) < DEPTH ? launch_one<LAYOUT, TRI, ANY, THREADS, true>(a, c, numSMs, s)
+                                                       : launch_one<LAYOUT, TRI, ANY, THREADS, false>(a, c, numSMs, s);
 }
 
 template <int LAYOUT, int TRI>
@@ -1116,33 +1134,34 @@ cudaError_t trace_one(const TraceArgs& a, int kind, const TraceConfig& c, int nu
   switch (c.threadsPerBlock)
   {
     case 64:
-      return kind == 0 ? launch_one<LAYOUT, TRI, false, 64>(a, c, numSMs, s)
-                       : launch_one<LAYOUT, TRI, true, 64>(a, c, numSMs, s);
+      return kind == 0 ? launch_one_any_stack<LAYOUT, TRI, false, 64>(a, c, numSMs, s)
+                       : launch_one_any_stack<LAYOUT, TRI, true, 64>(a, c, numSMs, s);
     case 256:
-      return kind == 0 ? launch_one<LAYOUT, TRI, false, 256>(a, c, numSMs, s)
-                       : launch_one<LAYOUT, TRI, true, 256>(a, c, numSMs, s);
+      return kind == 0 ? launch_one_any_stack<LAYOUT, TRI, false, 256>(a, c, numSMs, s)
+                       : launch_one_any_stack<LAYOUT, TRI, true, 256>(a, c, numSMs, s);
     default:
-      return kind == 0 ? launch_one<LAYOUT, TRI, false, 128>(a, c, numSMs, s)
-                       : launch_one<LAYOUT, TRI, true, 128>(a, c, numSMs, s);
+      return kind == 0 ? launch_one_any_stack<LAYOUT, TRI, false, 128>(a, c, numSMs, s)
+                       : launch_one_any_stack<LAYOUT, TRI, true, 128>(a, c, numSMs, s);
   }
 }
 
-template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS>
+template <int LAYOUT, int TRI, bool ANY, bool COUNT, int THREADS, bool TLAS, bool SPILL>
 cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
   const uint32_t n = (uint32_t)a.n;
   const Segments sg{a.rayOffsets, a.segInst, a.nSeg, a.nInst};
   const Tlas tl{a.tlasRecs, a.tlasTris, a.nInst};
-  const int shared = shared_entries<StackDepth<LAYOUT, TLAS>::value>(c.stackEntries);
+  const int shared = SPILL ? shared_entries<StackDepth<LAYOUT, TLAS>::value>(c.stackEntries)
+                           : StackDepth<LAYOUT, TLAS>::value;
   const size_t smem = sizeof(uint32_t) * (size_t)shared * THREADS;
   const RayOrder order = ray_order(n, c.imageWidth);
   if (c.persistent && !COUNT)
   {
-    cudaError_t e = allow_smem(k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>, smem);
+    cudaError_t e = allow_smem(k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL>, smem);
     if (e != cudaSuccess) return e;
     int perSM = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>,
-                                                      THREADS, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &perSM, k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL>, THREADS, smem);
     if (e != cudaSuccess) return e;
     if (perSM < 1) perSM = 1;
     uint64_t blocks = (uint64_t)numSMs * perSM;
@@ -1150,38 +1169,48 @@ cudaError_t launch(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStr
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(a.rayCounter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+    k_trace_pool<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL><<<(uint32_t)blocks, THREADS, smem, s>>>(
         a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, a.rayCounter, c.stepsPerRefill, c.refillLanes,
         shared, order);
   }
   else
   {
-    cudaError_t e = allow_smem(k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS>, smem);
+    cudaError_t e = allow_smem(k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL>, smem);
     if (e != cudaSuccess) return e;
     const uint64_t blocks = ((uint64_t)order.nWork + THREADS - 1) / THREADS;
-    k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS><<<(uint32_t)blocks, THREADS, smem, s>>>(
+    k_trace_grid<LAYOUT, TRI, ANY, COUNT, THREADS, TLAS, SPILL><<<(uint32_t)blocks, THREADS, smem, s>>>(
         a.rays, n, a.inst, sg, tl, a.hits, a.counters, a.errorWord, shared, order);
   }
   return cudaGetLastError();
 }
 
+template <int LAYOUT, int TRI, bool ANY, int THREADS, bool TLAS>
+cudaError_t launch_any_stack(const TraceArgs& a, const TraceConfig& c, int numSMs, cudaStream_t s)
+{
+  constexpr int DEPTH = StackDepth<LAYOUT, TLAS>::value;
+  return shared_entries<DEPTH>(c.stackEntries) < DEPTH
+             ? launch<LAYOUT, TRI, ANY, false, THREADS, TLAS, true>(a, c, numSMs, s)
+             : launch<LAYOUT, TRI, ANY, false, THREADS, TLAS, false>(a, c, numSMs, s);
+}
+
 template <int LAYOUT, int TRI, bool TLAS>
 cudaError_t trace_tlas(const TraceArgs& a, int kind, int counting, const TraceConfig& c, int numSMs, cudaStream_t s)
 {
+  // counting runs: the whole stack in shared memory (the counts do not depend on it)
   if (counting)
-    return kind == 0 ? launch<LAYOUT, TRI, false, true, 128, TLAS>(a, c, numSMs, s)
-                     : launch<LAYOUT, TRI, true, true, 128, TLAS>(a, c, numSMs, s);
+    return kind == 0 ? launch<LAYOUT, TRI, false, true, 128, TLAS, false>(a, c, numSMs, s)
+                     : launch<LAYOUT, TRI, true, true, 128, TLAS, false>(a, c, numSMs, s);
   switch (c.threadsPerBlock)
   {
     case 64:
-      return kind == 0 ? launch<LAYOUT, TRI, false, false, 64, TLAS>(a, c, numSMs, s)
-                       : launch<LAYOUT, TRI, true, false, 64, TLAS>(a, c, numSMs, s);
+      return kind == 0 ? launch_any_stack<LAYOUT, TRI, false, 64, TLAS>(a, c, numSMs, s)
+                       : launch_any_stack<LAYOUT, TRI, true, 64, TLAS>(a, c, numSMs, s);
     case 256:
-      return kind == 0 ? launch<LAYOUT, TRI, false, false, 256, TLAS>(a, c, numSMs, s)
-                       : launch<LAYOUT, TRI, true, false, 256, TLAS>(a, c, numSMs, s);
+      return kind == 0 ? launch_any_stack<LAYOUT, TRI, false, 256, TLAS>(a, c, numSMs, s)
+                       : launch_any_stack<LAYOUT, TRI, true, 256, TLAS>(a, c, numSMs, s);
     default:
-      return kind == 0 ? launch<LAYOUT, TRI, false, false, 128, TLAS>(a, c, numSMs, s)
-                       : launch<LAYOUT, TRI, true, false, 128, TLAS>(a, c, numSMs, s);
+      return kind == 0 ? launch_any_stack<LAYOUT, TRI, false, 128, TLAS>(a, c, numSMs, s)
+                       : launch_any_stack<LAYOUT, TRI, true, 128, TLAS>(a, c, numSMs, s);
   }
 }
 

@@ -154,7 +154,7 @@ def test_trace_configs_give_identical_results(native, cfg):
     s, _ = _scene(v, idx)
     for kind in (0, 1):
         s.set_trace_config(kind, *cfg)
-        assert tuple(s.trace_config(kind).values()) == cfg
+        assert tuple(s.trace_config(kind).values())[:len(cfg)] == tuple(cfg)
     np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), o.trace(rays).view(np.uint32))
     np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), o.trace(rays, any_hit=True))
 
