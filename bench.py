@@ -753,7 +753,7 @@ def run_watertight(ctx, args, w, ao, mt_hits, mt_any, configs) -> dict:
 
 # ---------------------------------------------------------------- served stream
 
-def served_workload(args):
+def served_workload(args, rate: float, seconds: float):
     """64 resident scenes, the arrival trace, ray pools and upload scenes."""
     from heavyrt_gb300 import workload as wl
 
@@ -770,8 +770,8 @@ def served_workload(args):
     up_tris = wl.log_uniform_counts(seed, 2, 6, 100000, 1000000)
     uploads = [wl.soup(seed + 300 + i, int(n), -1.0, 1.0, 0.02) for i, n in enumerate(up_tris)]
     rng = np.random.default_rng(seed)
-    count = int(args.served_rate * args.served_seconds)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.served_rate, count))
+    count = int(rate * seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
     sizes = wl.log_uniform_counts(seed, 3, count, 1000, 1000000)
     target = rng.integers(0, len(scenes), count)
     kinds = rng.integers(0, 2, count)
@@ -800,7 +800,7 @@ def _latency_stats(lat_s, rays, span_s):
             "requests": int(len(lat))}
 
 
-def run_served(ctx, args) -> dict:
+def run_served(ctx, args, rate: float = None, seconds: float = None) -> dict:
     """Served stream: 64 resident scenes (soups and heightfields, log-uniform
     10k..2M triangles), Poisson arrivals, each request log-uniform 1k..1M rays
     against a uniformly chosen scene, half nearest / half any; 5% of requests
@@ -814,7 +814,9 @@ def run_served(ctx, args) -> dict:
     from heavyrt_gb300 import PinnedBuffer, SceneRT
     from heavyrt_gb300 import engine as E
 
-    W = served_workload(args)
+    rate = args.served_rate if rate is None else rate
+    seconds = args.served_seconds if seconds is None else seconds
+    W = served_workload(args, rate, seconds)
     arrivals, sizes, target, kinds, upload = W["arrivals"], W["sizes"], W["target"], W["kinds"], W["upload"]
     count = len(arrivals)
     pools = []
@@ -834,8 +836,8 @@ def run_served(ctx, args) -> dict:
         ai[:] = idx
         up_bufs.append((bv, bi, av, ai))
     W["uploads"] = [(av, ai) for _, _, av, ai in up_bufs]
-    result = {"workload": f"served: 64 resident scenes ({sum(W['tris'])} tris), Poisson {args.served_rate:.0f} req/s "
-                          f"for {args.served_seconds:.1f} s, 1k..1M rays per request, 5% uploads",
+    result = {"workload": f"served: 64 resident scenes ({sum(W['tris'])} tris), Poisson {rate:.0f} req/s "
+                          f"for {seconds:.1f} s, 1k..1M rays per request, 5% uploads",
               "requests": count, "rays": int(sizes.sum()), "uploads": int(upload.sum())}
 
     # ---- served
@@ -1428,6 +1430,9 @@ def run_engine(args):
     # the host link measured the same before and after
     if not args.no_served:
         line["served"] = run_served(ctx, args)
+        # the same stream at five times the arrival rate: requests queue while
+        # batches are on the GPU, so batches hold several requests
+        line["served_5x"] = run_served(ctx, args, 5 * args.served_rate, 1.0)
     if not args.no_batched:
         line["batched"] = run_batched(ctx, args)
         line["gpu_launches_batched_per_step"] = 2
@@ -1475,6 +1480,12 @@ def summarize(line: dict):
             cfg[f"served_plain_{k}"] = pl[k]
         cfg["served_mean_requests_per_batch"] = sv["mean_requests_per_batch"]
         cfg["served_engine_p99_ms"] = sv["engine_p99_ms"]
+    if "served_5x" in line:
+        sv, pl = line["served_5x"]["served"], line["served_5x"]["plain"]
+        for k in ("p50_ms", "p99_ms", "mrays_s"):
+            cfg[f"served_5x_{k}"] = sv[k]
+            cfg[f"served_5x_plain_{k}"] = pl[k]
+        cfg["served_5x_mean_requests_per_batch"] = sv["mean_requests_per_batch"]
     if "batched" in line:
         b = line["batched"]
         for k in ("batched_mrays_s", "plain_mrays_s", "speedup", "results_equal_plain"):

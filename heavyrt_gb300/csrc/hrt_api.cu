@@ -1437,6 +1437,7 @@ int hrt_geom_export(const hrt_scene* s, uint32_t geomId, int what, void* dst, ui
     case HRT_EXPORT_NODES4:
       size = (uint64_t)g.nNodes4 * (s->layout == HRT_LAYOUT_BVH4_F32 ? sizeof(Node4F32) : sizeof(Node4F16));
       break;
+    case HRT_EXPORT_PAIR_RECORDS: size = g.recs ? sizeof(PairRec) * (L > 1 ? L - 1 : (L ? 1 : 0)) : 0; break;
     default: return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "unknown export id");
   }
   if (sizeBytes) *sizeBytes = size;
@@ -1473,6 +1474,7 @@ int hrt_geom_export(const hrt_scene* s, uint32_t geomId, int what, void* dst, ui
     case HRT_EXPORT_PRIM_INDICES: HRT_CUDA(ctx, cudaMemcpy(dst, g.vals, size, cudaMemcpyDeviceToHost)); return HRT_OK;
     case HRT_EXPORT_SORTED_INDICES: HRT_CUDA(ctx, cudaMemcpy(dst, g.sortedIdx, size, cudaMemcpyDeviceToHost)); return HRT_OK;
     case HRT_EXPORT_NODES4: HRT_CUDA(ctx, cudaMemcpy(dst, g.nodes4, size, cudaMemcpyDeviceToHost)); return HRT_OK;
+    case HRT_EXPORT_PAIR_RECORDS: HRT_CUDA(ctx, cudaMemcpy(dst, g.recs, size, cudaMemcpyDeviceToHost)); return HRT_OK;
     default: break;
   }
   return HRT_ERR_INVALID_ARGUMENT;

@@ -41,6 +41,7 @@ EXPORT_PRIM_INDICES = 6
 EXPORT_SORTED_INDICES = 7
 EXPORT_MORTON_UNSORTED = 8
 EXPORT_NODES4 = 9
+EXPORT_PAIR_RECORDS = 10
 
 # node layouts (include/hrt.h); names accepted as CreateSceneRT's a_layoutName
 LAYOUT_BVH2, LAYOUT_BVH4_F32, LAYOUT_BVH4_F16, LAYOUT_BVH4_Q8 = 0, 1, 2, 3
@@ -66,6 +67,7 @@ _EXPORT_DTYPES = {
     EXPORT_PRIM_INDICES: np.uint32,
     EXPORT_SORTED_INDICES: np.uint32,
     EXPORT_NODES4: np.uint32,
+    EXPORT_PAIR_RECORDS: np.uint32,
 }
 
 

@@ -589,6 +589,11 @@ int hrt_geom_info(const hrt_scene* scene, uint32_t geomId, uint64_t out[4], floa
 #define HRT_EXPORT_SORTED_INDICES  7 /* uint32[3N] index buffer in sorted order (BVH2CommonRT_host.cpp:45-64) */
 #define HRT_EXPORT_MORTON_UNSORTED 8 /* uint2[N] (code, triId) before the sort (lbvh.cpp:259-287)           */
 #define HRT_EXPORT_NODES4          9 /* the 4-wide nodes of a BVH4 layout, raw (128 or 64 bytes each)      */
+#define HRT_EXPORT_PAIR_RECORDS   10 /* the binary layout's child-pair records, 64 bytes each: left child's
+                                        box (6 floats), right child's box, left ref, right ref (internal:
+                                        record index; leaf: 0x80000000 | first sorted triangle), 0, 0 --
+                                        the sibling pairs of the reference's LEFT_OFFSET array
+                                        (lbvh.cpp:492-729) in the LR tree's numbering                       */
 int hrt_geom_export(const hrt_scene* scene, uint32_t geomId, int what, void* dst, uint64_t capacityBytes,
                     uint64_t* sizeBytes);
 

@@ -481,3 +481,54 @@ def test_geom_boxes_and_info(native):
     info = s.geom_info(gid)
     assert info["tris"] == 1000 and info["leaves"] <= 1000 and info["build_ms"] > 0
     assert s.GetInstNum() == 1 and s.Name() == "GB300_LBVH"
+
+
+def _walk_pairs(recs, peach):
+    """Walks the engine's child-pair records and the reference's LEFT_OFFSET
+    (peach) array side by side from the root: record r of the binary layout
+    and the sibling pair at peach offset o hold the same two child boxes (bit
+    for bit), the same leaf starts, and internal children map to each other.
+    Returns the number of pairs compared."""
+    LEAF = 0x80000000
+    rec = recs.reshape(-1, 16)
+    boxes = rec[:, :12].view(np.float32)
+    refs = rec[:, 12:14]
+    pb = np.stack([peach["boxMin"], peach["boxMax"]], axis=1).reshape(-1, 6)  # min xyz, max xyz
+    seen = 0
+    todo = [(0, 0)]
+    while todo:
+        r, o = todo.pop()
+        seen += 1
+        for c in (0, 1):
+            eb = boxes[r, 6 * c:6 * c + 6]
+            ref = int(refs[r, c])
+            node_left = int(peach["leftOffset"][o + c])
+            if ref == 0xFFFFFFFF:  # a lone leaf's empty slot: the reference's dummy node
+                assert node_left == LEAF and int(peach["escapeIndex"][o + c]) == 0xFFFFFFFF
+                continue
+            np.testing.assert_array_equal(eb.view(np.uint32), pb[o + c].astype(np.float32).view(np.uint32))
+            if ref & LEAF:
+                assert node_left & LEAF
+                assert (node_left & 0x00FFFFFF) == (ref & 0x00FFFFFF)  # leaf start (sorted position)
+            else:
+                assert not (node_left & LEAF)
+                todo.append((ref, node_left))
+    return seen
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 257, 4097, 70001])
+def test_pair_records_are_the_reference_sibling_pairs(native, n):
+    """The binary layout's pair records hold the sibling pairs of the
+    reference's LEFT_OFFSET array (core/builders/lbvh.cpp:492-729, the
+    oracle's peach_convert): the same boxes and leaf starts, pair for pair,
+    reached through the same child links."""
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+
+    v, idx = wl.soup(700 + n, n, off=0.05)
+    o, _ = _oracle_expect(v, idx)
+    s, gid = _scene(v, idx)
+    recs = s.export(gid, E.EXPORT_PAIR_RECORDS)
+    peach = o.peach_nodes()
+    assert _walk_pairs(recs, peach) == max(o.n_leaves - 1, 1)
+    s.close()
