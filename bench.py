@@ -90,8 +90,9 @@ def parse():
     p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
     p.add_argument("--eye-order", default="tiles", choices=["tiles", "given"],
                    help="eye rays traced in 8x4 pixel tiles of the image (index arithmetic) or in the order given")
-    p.add_argument("--l2-persist", type=int, default=0, metavar="MIB",
-                   help="persisting-L2 window over the headline scene's nodes (MiB set aside; 0 none)")
+    p.add_argument("--l2-persist", type=int, default=64, metavar="MIB",
+                   help="persisting-L2 window over the headline scene's nodes (MiB set aside; 0 none) for the "
+                        "timed region and the end-to-end leg")
     p.add_argument("--no-l2-sweep", action="store_true", help="skip the persisting-L2 window sweep")
     p.add_argument("--no-oracle-check", action="store_true",
                    help="skip the check of every ray of the headline frame against the oracle")
@@ -645,7 +646,7 @@ def run_l2_window(scene, d_eye, d_ao, d_hits, d_any, args) -> dict:
         out["sweep"].append({"mib": mib, "eye_ms": round(e[0].elapsed_time(e[1]) / steps, 4),
                              "ao_ms": round(e[1].elapsed_time(e[2]) / steps, 4),
                              "results_equal": bool(torch.equal(d_hits, want_h) and torch.equal(d_any, want_a))})
-    scene.set_l2_persist(args.l2_persist)
+    scene.set_l2_persist(0)
     return out
 
 
@@ -1025,7 +1026,8 @@ def run_frames(ctx, args, w, trace_configs=None) -> dict:
     sc.AddInstance(g)
     sc.CommitScene()
     for kind, cfg in (trace_configs or {}).items():
-        sc.set_trace_config(kind, **cfg)
+        # the frames trace their eye rays in the renderer's own packed order
+        sc.set_trace_config(kind, **dict(cfg, imageWidth=0))
     f = Frame(ctx)
     f.set_normals(g, wl.vertex_normals(w.verts, w.idx))
     f.set_ao_tile(rtao_qmc_tile(R), R)
@@ -1304,6 +1306,10 @@ def run_engine(args):
     for b in (pin_eye, pin_ao, pin_hits, pin_any):
         b.free()
 
+    # the persisting-L2 set-aside ends with the headline scene's legs (the
+    # other sections run without it)
+    if args.l2_persist:
+        scene.set_l2_persist(0)
     # plain: the binary FP32 tree (the reference's decisions) with the default launch shape
     plain = None
     if not args.no_plain:
@@ -1409,6 +1415,7 @@ def run_engine(args):
         "clocks": clk,
     }
     line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
+    line["config"]["l2_persist_mib"] = args.l2_persist
     line["config"]["eye_ray_order"] = (f"8x4 pixel tiles of the {args.width}-wide image (index arithmetic, results "
                                        "in ray order)" if args.eye_order == "tiles" else "as given (row-major)")
     line["config"]["launch"] = tuned if tuned is not None else "default"
