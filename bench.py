@@ -89,7 +89,7 @@ def parse():
                    help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
     p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
     p.add_argument("--eye-order", default="tiles", choices=["tiles", "given"],
-                   help="eye rays traced in 8x4 pixel tiles of the image (index arithmetic) or in the order given")
+                   help="eye rays traced in 4x8 pixel tiles of the image (index arithmetic) or in the order given")
     p.add_argument("--l2-persist", type=int, default=64, metavar="MIB",
                    help="persisting-L2 window over the headline scene's nodes (MiB set aside; 0 none) for the "
                         "timed region and the end-to-end leg")
@@ -1160,7 +1160,7 @@ def run_engine(args):
     ao_bytes = node_bytes * ao_pairs + TRI_BYTES * ao_tris + RAY_BYTES * n_ao + 1 * n_ao
 
     # the eye rays are one row-major image: let the traversal take them in
-    # 8 x 4 pixel tiles (the autotuner keeps this property of the rays)
+    # 4 x 8 pixel tiles (the autotuner keeps this property of the rays)
     if args.eye_order == "tiles":
         scene.set_trace_config(0, imageWidth=args.width)
     tuned = None
@@ -1416,7 +1416,7 @@ def run_engine(args):
     }
     line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
     line["config"]["l2_persist_mib"] = args.l2_persist
-    line["config"]["eye_ray_order"] = (f"8x4 pixel tiles of the {args.width}-wide image (index arithmetic, results "
+    line["config"]["eye_ray_order"] = (f"4x8 pixel tiles of the {args.width}-wide image (index arithmetic, results "
                                        "in ray order)" if args.eye_order == "tiles" else "as given (row-major)")
     line["config"]["launch"] = tuned if tuned is not None else "default"
     if plain is not None:

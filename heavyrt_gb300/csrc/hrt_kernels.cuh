@@ -219,7 +219,7 @@ struct TraceConfig
   int refillLanes = 24;       // a warp refills when at least this many lanes are idle
   int stackEntries = 0;       // stack entries per lane in shared memory, the rest in local
                               // memory; 0 (or at least the depth bound): all in shared memory
-  int imageWidth = 0;         // > 0: rays form row-major images this wide, traced in 8 x 4 tiles
+  int imageWidth = 0;         // > 0: rays form row-major images this wide, traced in 4 x 8 tiles
 };
 
 // kind 0: nearest, 1: any.  counting = 1 also accumulates counters (node

@@ -262,8 +262,8 @@ typedef struct hrt_trace_config
   int refillLanes;     /* a warp refills when at least this many lanes are idle (1..32) */
   int stackEntries;    /* short-stack entries in shared memory (0..HRT_MAX_STACK_ENTRIES) */
   int imageWidth;      /* > 0: the rays form row-major images this many rays wide (as a
-                          renderer's eye rays do), and the traversal takes them in 8 x 4
-                          pixel tiles so that neighbouring pixels trace together; results
+                          renderer's eye rays do), and the traversal takes them in tiles of
+                          4 x 8 pixels so that neighbouring pixels trace together; results
                           still go to each ray's index.  0: rays taken in the order given */
 } hrt_trace_config;
 int hrt_scene_set_trace_config(hrt_scene* scene, int kind, const hrt_trace_config* config);

@@ -101,3 +101,21 @@ def test_adapter_scene_renders_frames_into_host_memory(native, tmp_path):
     np.testing.assert_array_equal(np.fromfile(tmp_path / "out.rtao", np.uint32), want["colors"])
     np.testing.assert_array_equal(np.fromfile(tmp_path / "out.eye", np.uint32), orc.eye_frame(b, p, wv, W, H))
     assert (want["colors"] != 0).any()
+
+
+def test_reference_eye_renderer_links_over_engine(host_libs):
+    """HeavyRT's eye-ray renderer (examples/01_eye_rays/eye_ray.cpp, its
+    sources unchanged) compiles and links with the engine's ISceneObject
+    adapter and the engine library (oracle/Makefile.ref render_engine_check).
+    Running it needs the reference sources and a CUDA device on one machine,
+    which this test does not assume."""
+    from heavyrt_gb300 import native_build
+
+    ref = native_build.reference_root()
+    if ref is None:
+        pytest.skip("HeavyRT sources not present on this machine")
+    native_build.build_engine()
+    r = subprocess.run(["make", "-s", "-f", "Makefile.ref", f"REF={ref}", "_ref/render_engine_check"],
+                       cwd=ROOT / "oracle", capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    assert (ROOT / "oracle" / "_ref" / "render_engine_check").exists()

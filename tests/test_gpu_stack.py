@@ -100,7 +100,7 @@ def test_stack_entries_out_of_range_refused(native):
 
 @pytest.mark.parametrize("layout", ["bvh2", "bvh4_f16"])
 def test_image_tile_order_gives_the_same_results(native, layout):
-    """Rays taken in 8 x 4 pixel tiles of row-major images (imageWidth): the
+    """Rays taken in 4 x 8 pixel tiles of row-major images (imageWidth): the
     results of the given order, for widths that divide the ray count and that
     do not, in the single-instance, two-level and segmented kernels."""
     import torch
