@@ -135,12 +135,43 @@ struct Tlas
   uint32_t       nInst;
 };
 
+struct WtRay
+{
+  int   kx, ky, kz;
+  float sx, sy, sz;
+};
+
+__device__ __forceinline__ float pick3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ void wt_setup(float dx, float dy, float dz, WtRay& w)
+{
+  const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+  w.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+  w.kx = w.kz == 2 ? 0 : w.kz + 1;
+  w.ky = w.kx == 2 ? 0 : w.kx + 1;
+  const float dk = pick3(dx, dy, dz, w.kz);
+  if (dk < 0.0f)
+  {
+    const int t = w.kx;
+    w.kx = w.ky;
+    w.ky = t;
+  }
+  w.sx = __fdiv_rn(pick3(dx, dy, dz, w.kx), dk);
+  w.sy = __fdiv_rn(pick3(dx, dy, dz, w.ky), dk);
+  w.sz = __fdiv_rn(1.0f, dk);
+}
+
+// A ray in the frame of the geometry being traversed.  `w` is the watertight
+// test's per-ray set-up; the Moller-Trumbore kernels never read it, so the
+// compiler drops its computation there.
 struct Ray
 {
   float ox, oy, oz, tNear;
   float dx, dy, dz;
   float ix, iy, iz;
+  WtRay w;
 };
+
 
 // SafeInverse, core/raytrace_common.h:57-65.
 __device__ __forceinline__ float safe_inv(float d)
@@ -227,6 +258,7 @@ __device__ __forceinline__ void make_ray(const InstanceDesc& d, const float4& po
   r.ix = safe_inv(r.dx);
   r.iy = safe_inv(r.dy);
   r.iz = safe_inv(r.dz);
+  wt_setup(r.dx, r.dy, r.dz, r.w);
 }
 
 // Moller-Trumbore leaf test over the leaf starting at sorted triangle j
@@ -287,32 +319,6 @@ __device__ __forceinline__ bool leaf_test(const TriRec* __restrict__ tris, uint3
 // exactly opposite signs on both sides: no ray passes between them.  Records
 // hold the vertices {A, B, C} (w: flags, triangle id, 0).  Outputs match the
 // Moller-Trumbore fields: u = the weight of C, v = the weight of B.
-struct WtRay
-{
-  int   kx, ky, kz;
-  float sx, sy, sz;
-};
-
-__device__ __forceinline__ float pick3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
-
-__device__ __forceinline__ void wt_setup(const Ray& r, WtRay& w)
-{
-  const float ax = fabsf(r.dx), ay = fabsf(r.dy), az = fabsf(r.dz);
-  w.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
-  w.kx = w.kz == 2 ? 0 : w.kz + 1;
-  w.ky = w.kx == 2 ? 0 : w.kx + 1;
-  const float dz = pick3(r.dx, r.dy, r.dz, w.kz);
-  if (dz < 0.0f)
-  {
-    const int t = w.kx;
-    w.kx = w.ky;
-    w.ky = t;
-  }
-  w.sx = __fdiv_rn(pick3(r.dx, r.dy, r.dz, w.kx), dz);
-  w.sy = __fdiv_rn(pick3(r.dx, r.dy, r.dz, w.ky), dz);
-  w.sz = __fdiv_rn(1.0f, dz);
-}
-
 // a*b - c*d with the rounding error of c*d restored (Kahan).
 __device__ __forceinline__ float diff_of_products(float a, float b, float c, float d)
 {
@@ -326,8 +332,7 @@ template <bool ANY, bool COUNT, uint32_t ENDBIT = 1u>
 __device__ __forceinline__ bool leaf_test_wt(const TriRec* __restrict__ tris, uint32_t j, const Ray& r, Hit& h,
                                              uint32_t instIndex, uint64_t& nTris)
 {
-  WtRay w;
-  wt_setup(r, w);
+  const WtRay& w = r.w;
   while (true)
   {
     const float4* q = reinterpret_cast<const float4*>(tris + j);
@@ -655,6 +660,7 @@ __device__ __forceinline__ void world_ray(Lane& L)
   L.r.ix = safe_inv(L.r.dx);
   L.r.iy = safe_inv(L.r.dy);
   L.r.iz = safe_inv(L.r.dz);
+  wt_setup(L.r.dx, L.r.dy, L.r.dz, L.r.w);
 }
 
 __device__ __forceinline__ void tlas_begin(Lane& L)
@@ -943,6 +949,7 @@ __device__ __forceinline__ void start_ray_one(Lane1& L, uint32_t i, const float4
   L.r.ix = safe_inv(di.x);
   L.r.iy = safe_inv(di.y);
   L.r.iz = safe_inv(di.z);
+  wt_setup(di.x, di.y, di.z, L.r.w);
   L.h.t = di.w;
   L.h.u = L.h.v = 0.0f;
   L.h.prim = L.h.inst = 0xFFFFFFFFu;
