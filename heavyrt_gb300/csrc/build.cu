@@ -208,17 +208,21 @@ __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict_
                                                      uint32_t* __restrict__ parent, uint32_t* __restrict__ rangeEnd)
 {
   const int L = (int)params->nLeaves;
-  // one node per lane, a warp's 32 consecutive nodes searched together
-  // (karras_node_warp); the loop bound is uniform over the warp
+  // one node per thread; a warp's 32 consecutive nodes exchange their codes
+  // for the direction test (karras_neighbours), so the loop bound is uniform
+  // over the warp
   const int lane = (int)(threadIdx.x & 31u);
   for (int base = (int)(blockIdx.x * kThreads + (threadIdx.x & ~31u)); base < L - 1; base += gridDim.x * kThreads)
   {
     const int i = base + lane;
     const bool active = i < L - 1;
-    uint32_t left = 0, right = 0;
-    int other = 0;
-    bc::karras_node_warp(codes, 0, L, i, active, left, right, other);
+    uint32_t ci;
+    int dPrev, dNext;
+    bc::karras_neighbours(codes, 0, L, i, active, ci, dPrev, dNext);
     if (!active) continue;
+    uint32_t left, right;
+    int other;
+    bc::karras_node(codes, L, i, ci, dPrev, dNext, left, right, other);
     lr[i].leftOffset = left;
     lr[i].escapeIndex = right;
     parent[left] = (uint32_t)i;

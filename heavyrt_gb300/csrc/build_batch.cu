@@ -293,8 +293,9 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
                                                          uint32_t* __restrict__ parent, uint32_t* __restrict__ rangeEnd)
 {
   const uint32_t Itot = counts[1];
-  // a warp's 32 consecutive internal nodes searched together (lanes may
-  // belong to different geometries); the loop bound is uniform over the warp
+  // one node per thread; a warp's 32 consecutive internal nodes exchange
+  // their codes for the direction test (lanes may belong to different
+  // geometries), so the loop bound is uniform over the warp
   const uint32_t lane = threadIdx.x & 31u;
   for (uint32_t base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < Itot; base += gridDim.x * kThreads)
   {
@@ -303,10 +304,13 @@ __global__ void __launch_bounds__(kThreads) k_seg_karras(const uint32_t* __restr
     const uint32_t s = active ? find_segment(intOffsets, G, j) : 0u;
     const int L = active ? (int)(leafOffsets[s + 1] - leafOffsets[s]) : 0;
     const int i = active ? (int)(j - intOffsets[s]) : 0;
-    uint32_t left = 0, right = 0;
-    int other = 0;
-    bc::karras_node_warp(compressed, active ? (int)leafOffsets[s] : 0, L, i, active, left, right, other);
+    uint32_t ci;
+    int dPrev, dNext;
+    bc::karras_neighbours(compressed, active ? (int)leafOffsets[s] : 0, L, i, active, ci, dPrev, dNext);
     if (!active) continue;
+    uint32_t left, right;
+    int other;
+    bc::karras_node(compressed + leafOffsets[s], L, i, ci, dPrev, dNext, left, right, other);
     const uint32_t nb = nodeOffsets[s];
     lr[nb + i].leftOffset = left;
     lr[nb + i].escapeIndex = right;

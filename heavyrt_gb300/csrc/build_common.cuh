@@ -105,97 +105,68 @@ __device__ __forceinline__ void zindex_scale(const float* mn, const float* mx, B
   }
 }
 
-// kernel1D_Karras12 (core/builders/lbvh.cpp:405-441) with its delta()
-// (:386-403: the codes are unique after compaction, so delta is the count of
-// leading zeros of their XOR, 32 for equal codes, -1 out of range): direction
-// from the neighbours' deltas, the range end by exponential then binary
-// search, the split by binary search; children in the LR numbering (internal
-// 0..L-2, leaves L-1..2L-2), `other` = the far end of the node's leaf range.
-// Computed by a whole warp at once, one node per lane, with the codes the
-// warp's lanes already hold exchanged by warp shuffles.
-// Lane l works on node i of a tree whose L codes start at absolute index
-// segBase of `all` (the lanes of a warp may work on different trees of a
-// segmented build); it holds its own node's code, all[segBase + i].  Each
-// delta() is a warp-collective probe: a code held by a lane of the warp comes
-// from that lane (__shfl_sync), any other from memory.  Most nodes are deep
-// and their searches stay within a few positions, so most probes never touch
-// memory.  The loops run until no lane needs another step (__any_sync), every
-// lane probing once per step; each lane's probe sequence and decisions are
-// the reference's.  Every lane of the warp must call this (active = false for
-// a lane without a node).
-struct WarpCodes
+// delta() of core/builders/lbvh.cpp:386-403 against a code held in a
+// register: the codes are unique after compaction, so this is the count of
+// leading zeros of their XOR (32 for equal codes, -1 out of range).
+__device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ c, int L, uint32_t ci, int j)
 {
-  const uint32_t* all;
-  uint32_t        mine;  // the code this lane holds
-  int             g;     // its absolute index (-1: none)
-  int             g0;    // lane 0's absolute index
-};
-
-__device__ __forceinline__ int warp_delta(const WarpCodes& w, uint32_t ci, int segBase, int L, int j)
-{
-  const bool in = j >= 0 && j < L;
-  const int gj = segBase + j;
-  const int off = gj - w.g0;
-  const int src = (in && off >= 0 && off < 32) ? off : 0;
-  const uint32_t c = __shfl_sync(0xFFFFFFFFu, w.mine, src);
-  const int gs = __shfl_sync(0xFFFFFFFFu, w.g, src);
-  if (!in) return -1;
-  const uint32_t cj = (gs == gj && off >= 0 && off < 32) ? c : __ldg(w.all + gj);
-  const uint32_t x = ci ^ cj;
+  if (j < 0 || j >= L) return -1;
+  const uint32_t x = ci ^ __ldg(c + j);
   return x == 0u ? 32 : __clz(x);
 }
 
-__device__ __forceinline__ void karras_node_warp(const uint32_t* __restrict__ all, int segBase, int L, int i,
-                                                 bool active, uint32_t& left, uint32_t& right, int& other)
+__device__ __forceinline__ int clz_delta(uint32_t a, uint32_t b)
 {
-  WarpCodes w;
-  w.all = all;
-  w.g = active ? segBase + i : -1;
-  w.mine = active ? __ldg(all + segBase + i) : 0u;
-  w.g0 = __shfl_sync(0xFFFFFFFFu, w.g, 0);
-  const uint32_t ci = w.mine;
-  const int dr = warp_delta(w, ci, segBase, L, active ? i + 1 : -1);
-  const int dlft = warp_delta(w, ci, segBase, L, active ? i - 1 : -1);
-  const int dl = dr - dlft;
+  const uint32_t x = a ^ b;
+  return x == 0u ? 32 : __clz(x);
+}
+
+// Node i's code and its neighbours' deltas, exchanged across the warp: lane l
+// handles absolute code index g (-1: no node); the neighbours' codes come
+// from the adjacent lanes by __shfl_up_sync / __shfl_down_sync when those
+// lanes hold indices g - 1 and g + 1 of the same tree, from memory otherwise
+// (the warp's first and last lanes, tree boundaries of a segmented build).
+// Every lane of the warp must call this.
+__device__ __forceinline__ void karras_neighbours(const uint32_t* __restrict__ all, int segBase, int L, int i,
+                                                  bool active, uint32_t& ci, int& dPrev, int& dNext)
+{
+  const int g = active ? segBase + i : -1;
+  ci = active ? __ldg(all + g) : 0u;
+  const uint32_t up = __shfl_up_sync(0xFFFFFFFFu, ci, 1);
+  const int gUp = __shfl_up_sync(0xFFFFFFFFu, g, 1);
+  const uint32_t down = __shfl_down_sync(0xFFFFFFFFu, ci, 1);
+  const int gDown = __shfl_down_sync(0xFFFFFFFFu, g, 1);
+  const int lane = (int)(threadIdx.x & 31u);
+  dPrev = -1;
+  dNext = -1;
+  if (!active) return;
+  if (i >= 1) dPrev = clz_delta(ci, (lane > 0 && gUp == g - 1) ? up : __ldg(all + g - 1));
+  if (i + 1 < L) dNext = clz_delta(ci, (lane < 31 && gDown == g + 1) ? down : __ldg(all + g + 1));
+}
+
+// kernel1D_Karras12 (core/builders/lbvh.cpp:405-441) for internal node i of a
+// tree over L unique codes c (ci = c[i], dPrev / dNext = its deltas to the
+// codes before and after it): direction from the neighbours' deltas, the
+// range end by exponential then binary search, the split by binary search;
+// children in the LR numbering (internal 0..L-2, leaves L-1..2L-2), `other` =
+// the far end of the node's leaf range.
+__device__ __forceinline__ void karras_node(const uint32_t* __restrict__ c, int L, int i, uint32_t ci, int dPrev,
+                                            int dNext, uint32_t& left, uint32_t& right, int& other)
+{
+  const int dl = dNext - dPrev;
   const int d = (dl > 0) - (dl < 0);
-  const int dmin = warp_delta(w, ci, segBase, L, active ? i - d : -1);
+  const int dmin = d > 0 ? dPrev : (d < 0 ? dNext : 32);  // delta(i, i - d)
   int lmax = 2;
-  bool go = active;
-  while (__any_sync(0xFFFFFFFFu, go))
-  {
-    const int dd = warp_delta(w, ci, segBase, L, go ? i + lmax * d : -1);
-    if (go)
-    {
-      if (dd > dmin) lmax <<= 1;
-      else go = false;
-    }
-  }
-  int l = 0, t = active ? lmax >> 1 : 0;
-  while (__any_sync(0xFFFFFFFFu, t > 0))
-  {
-    const bool on = t > 0;
-    const int dd = warp_delta(w, ci, segBase, L, on ? i + (l + t) * d : -1);
-    if (on)
-    {
-      if (dd > dmin) l += t;
-      t >>= 1;
-    }
-  }
+  while (karras_delta(c, L, ci, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t > 0; t >>= 1)
+    if (karras_delta(c, L, ci, i + (l + t) * d) > dmin) l += t;
   const int j = i + l * d;
-  const int dnode = warp_delta(w, ci, segBase, L, active ? j : -1);
-  int sp = 0;
-  t = active ? (l + 1) >> 1 : 0;
-  while (__any_sync(0xFFFFFFFFu, t > 0))
-  {
-    const bool on = t > 0;
-    const int dd = warp_delta(w, ci, segBase, L, on ? i + (sp + t) * d : -1);
-    if (on)
-    {
-      if (dd > dnode) sp += t;
-      t = (t == 1 ? 0 : (t + 1) >> 1);
-    }
-  }
-  const int gamma = i + sp * d + (d < 0 ? d : 0);
+  const int dnode = karras_delta(c, L, ci, j);
+  int s = 0;
+  for (int t = (l + 1) >> 1; t > 0; t = (t == 1 ? 0 : (t + 1) >> 1))
+    if (karras_delta(c, L, ci, i + (s + t) * d) > dnode) s += t;
+  const int gamma = i + s * d + (d < 0 ? d : 0);
   left = ((i < j ? i : j) == gamma) ? (uint32_t)(L - 1 + gamma) : (uint32_t)gamma;
   right = ((i > j ? i : j) == gamma + 1) ? (uint32_t)(L - 1 + gamma + 1) : (uint32_t)(gamma + 1);
   other = j;
