@@ -145,3 +145,29 @@ def test_image_tile_order_gives_the_same_results(native, layout):
                 outs.append(out.cpu().numpy())
             np.testing.assert_array_equal(outs[0], outs[1])
         s.close()
+
+
+def test_l2_persisting_window_keeps_results(native):
+    """A persisting-L2 window over a single-instance scene's nodes
+    (HRT_OPTION_L2_PERSIST) changes no result; out-of-range sizes are refused;
+    turning it off restores the context's set-aside."""
+    from heavyrt_gb300 import HrtError, SceneRT
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(13, 128, 128)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 160, 90),
+                           wl.rays_at_triangles(4, v, idx, 4000, jitter=0.02)])
+    for layout in ("bvh2", "bvh4_f16"):
+        s = SceneRT(layout=layout)
+        gid = s.AddGeom_Triangles3f(v, v.shape[0], idx, idx.size, vByteStride=16)
+        s.AddInstance(gid)
+        s.CommitScene()
+        ref = s.RayQuery_NearestHit(rays).view(np.uint32)
+        ref_any = s.RayQuery_AnyHit(rays)
+        for mib in (1, 64, 0):
+            s.set_l2_persist(mib)
+            np.testing.assert_array_equal(s.RayQuery_NearestHit(rays).view(np.uint32), ref)
+            np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), ref_any)
+        with pytest.raises(HrtError):
+            s.set_l2_persist(-1)
+        s.close()
