@@ -88,6 +88,10 @@ def parse():
     p.add_argument("--only-build-batched", type=int, default=0, metavar="K",
                    help="only K segmented builds of the 256-soup batch, BVH4 FP16 merge 1 (its launch list)")
     p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
+    p.add_argument("--morton-frame", default="cubic", choices=["cubic", "per_axis"],
+                   help="Morton grid of the headline scene: cubic cells (engine option) or the reference's per-axis grid")
+    p.add_argument("--no-frame-compare", action="store_true",
+                   help="skip timing the headline layout on the reference's per-axis grid")
     p.add_argument("--eye-order", default="tiles", choices=["tiles", "given"],
                    help="eye rays traced in 4x8 pixel tiles of the image (index arithmetic) or in the order given")
     p.add_argument("--l2-persist", type=int, default=64, metavar="MIB",
@@ -488,6 +492,16 @@ def run_batched(ctx, args, tune: bool = True) -> dict:
 
 # ---------------------------------------------------------------- quantised nodes
 
+def to_original(hits, prim_indices):
+    """Hit records (uint32 [n, 8]) with primId (a position in the tree's sorted
+    order) replaced by the original triangle index, so that the hits of trees
+    with different sorted orders compare."""
+    h = np.array(hits, dtype=np.uint32, copy=True).reshape(-1, 8)
+    m = h[:, 1] != 0xFFFFFFFF
+    h[m, 1] = np.asarray(prim_indices, np.uint32)[h[m, 1]]
+    return h
+
+
 def hit_diff(hits, ref, name: str) -> dict:
     """Nearest-hit records (uint32 [n, 8]) against a reference set: mismatches
     (hit/miss differs, or t beyond 1e-5 relative: must be 0), ties resolved to
@@ -633,6 +647,14 @@ def run_precision(ctx, args) -> dict:
     return res
 
 
+def apply_frame(scene, args):
+    """The headline scene's Morton grid (before its first geometry)."""
+    from heavyrt_gb300 import engine as E
+
+    if args.morton_frame == "cubic":
+        scene.set_morton_frame(E.MORTON_CUBIC)
+
+
 def run_l2_window(scene, d_eye, d_ao, d_hits, d_any, args) -> dict:
     """The headline scene's eye and AO launches with a persisting-L2 window
     over its node array (hrt OPTION_L2_PERSIST) of 0 / 16 / 32 / 64 MiB set
@@ -699,6 +721,7 @@ def run_watertight(ctx, args, w, ao, mt_hits, mt_any, configs) -> dict:
     sc = SceneRT(ctx, layout=args.layout, triangle_test=E.TRI_WATERTIGHT)
     if args.layout != "bvh2":
         sc.set_bvh4_merge(args.merge)
+    apply_frame(sc, args)
     g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
     sc.AddInstance(g)
     sc.CommitScene()
@@ -1014,6 +1037,7 @@ def run_builds(ctx, args, w):
         s = SceneRT(ctx, layout=args.layout)
         if args.layout != "bvh2":
             s.set_bvh4_merge(args.merge)
+        apply_frame(s, args)
         g = s.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
         s.AddInstance(g)
         s.CommitScene()
@@ -1055,6 +1079,7 @@ def run_frames(ctx, args, w, trace_configs=None) -> dict:
     sc = SceneRT(ctx, layout=args.layout)
     if args.layout != "bvh2":
         sc.set_bvh4_merge(args.merge)
+    apply_frame(sc, args)
     g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
     sc.AddInstance(g)
     sc.CommitScene()
@@ -1151,16 +1176,19 @@ def run_engine(args):
             print(json.dumps({"frames": run_frames(ctx, args, w)}), flush=True)
         return 0
 
-    def make_scene(layout):
+    def make_scene(layout, frame=True):
         sc = SceneRT(ctx, layout=layout)
         if layout != "bvh2":
             sc.set_bvh4_merge(args.merge)
+        if frame:
+            apply_frame(sc, args)
         g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
         sc.AddInstance(g)
         sc.CommitScene()
         return sc, g
 
     scene, gid = make_scene(args.layout)
+    prim_idx = scene.export(gid, E.EXPORT_PRIM_INDICES)
     if args.l2_persist:
         scene.set_l2_persist(args.l2_persist)
     info = scene.geom_info(gid)
@@ -1346,7 +1374,7 @@ def run_engine(args):
     # plain: the binary FP32 tree (the reference's decisions) with the default launch shape
     plain = None
     if not args.no_plain:
-        ps, _ = make_scene("bvh2")
+        ps, _ = make_scene("bvh2", frame=False)  # the reference's grid and decisions
         p_hits = torch.empty_like(d_hits)
         p_any = torch.empty_like(d_any)
         for _ in range(3):
@@ -1363,8 +1391,8 @@ def run_engine(args):
         torch.cuda.synchronize()
         pe_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in pe)
         pa_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in pe)
-        hp = p_hits.cpu().numpy().view(np.uint32)
-        hq = d_hits.cpu().numpy().view(np.uint32)
+        hp = to_original(p_hits.cpu().numpy().view(np.uint32), ps.export(0, E.EXPORT_PRIM_INDICES))
+        hq = to_original(d_hits.cpu().numpy().view(np.uint32), prim_idx)
         plain = {"layout": LAYOUT_DESC["bvh2"], "eye_ms": round(pe_ms, 4), "ao_ms": round(pa_ms, 4),
                  "mrays_s": round((n_eye + n_ao) / (pe_ms + pa_ms) / 1e3, 2),
                  **hit_diff(hq, hp, "plain"),
@@ -1390,6 +1418,43 @@ def run_engine(args):
                 "ao_node_pairs_per_ray": round(pp_ao / n_ao, 3), "ao_tris_per_ray": round(pt_ao / n_ao, 3),
                 "at_plain_rate_gb_s": round((blb_eye * n_eye + blb_ao * n_ao) / ((pe_ms + pa_ms) * 1e-3) / 1e9, 1)}
         ps.close()
+
+    # the headline layout on the reference's per-axis Morton grid, same launch shapes
+    frame_cmp = None
+    if args.morton_frame == "cubic" and not args.no_frame_compare and not args.ncu:
+        fs, _ = make_scene(args.layout, frame=False)
+        for k in (0, 1):
+            fs.set_trace_config(k, **scene.trace_config(k))
+        if args.l2_persist:
+            fs.set_l2_persist(args.l2_persist)  # as the headline's legs had it
+        f_hits = torch.empty_like(d_hits)
+        f_any = torch.empty_like(d_any)
+        for _ in range(3):
+            fs.query_device(0, d_eye.data_ptr(), n_eye, f_hits.data_ptr(), sh)
+            fs.query_device(1, d_ao.data_ptr(), n_ao, f_any.data_ptr(), sh)
+        torch.cuda.synchronize()
+        fe = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        for k in range(args.steps):
+            fe[k][0].record(stream)
+            fs.query_device(0, d_eye.data_ptr(), n_eye, f_hits.data_ptr(), sh)
+            fe[k][1].record(stream)
+            fs.query_device(1, d_ao.data_ptr(), n_ao, f_any.data_ptr(), sh)
+            fe[k][2].record(stream)
+        torch.cuda.synchronize()
+        if args.l2_persist:
+            fs.set_l2_persist(0)
+        fe_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in fe)
+        fa_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in fe)
+        fp, ft = fs.query_counters(1, d_ao.data_ptr(), n_ao, sh)
+        frame_cmp = {"frame": "per_axis (the reference's ZIndexMultCoeff grid)", "eye_ms": round(fe_ms, 4),
+                     "ao_ms": round(fa_ms, 4), "mrays_s": round((n_eye + n_ao) / (fe_ms + fa_ms) / 1e3, 2),
+                     "node_fetches_per_ao_ray": round(fp / n_ao, 3), "tri_tests_per_ao_ray": round(ft / n_ao, 3),
+                     **hit_diff(to_original(d_hits.cpu().numpy().view(np.uint32), prim_idx),
+                                to_original(f_hits.cpu().numpy().view(np.uint32),
+                                            fs.export(0, E.EXPORT_PRIM_INDICES)), "per_axis"),
+                     "anyhit_mismatch_vs_per_axis": int(np.count_nonzero(f_any.cpu().numpy() != d_any.cpu().numpy()))}
+        fs.close()
+        del f_hits, f_any
 
     # roofline of the dominant kernel
     eye_avg, ao_avg = statistics.mean(eye_ms), statistics.mean(ao_ms)
@@ -1449,6 +1514,13 @@ def run_engine(args):
     }
     line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
     line["config"]["l2_persist_mib"] = args.l2_persist
+    line["config"]["morton_frame"] = args.morton_frame
+    line["config"]["node_pairs_note"] = "node fetches / triangle tests per ray of the headline's own tree"
+    line["config"]["tri_tests_per_ao_ray"] = round(ao_tris / n_ao, 3) if n_ao else None
+    if frame_cmp is not None:
+        line["per_axis_frame"] = frame_cmp
+        for k in ("mrays_s", "eye_ms", "ao_ms", "node_fetches_per_ao_ray"):
+            line["config"][f"per_axis_frame_{k}"] = frame_cmp[k]
     line["config"]["eye_ray_order"] = (f"4x8 pixel tiles of the {args.width}-wide image (index arithmetic, results "
                                        "in ray order)" if args.eye_order == "tiles" else "as given (row-major)")
     line["config"]["launch"] = tuned if tuned is not None else "default"
@@ -1491,9 +1563,11 @@ def run_engine(args):
             # every ray of the frame against the oracle (after the timed region):
             # the timed layout's device-resident eye hits and AO flags, and the
             # AO flags the e2e leg wrote into host memory
-            want = o.trace(w.eye_rays).view(np.uint32).reshape(-1, 8)
+            # primIds compared as original triangle indices (the headline's
+            # tree may sort the triangles differently from the reference's)
+            want = to_original(o.trace(w.eye_rays).view(np.uint32).reshape(-1, 8), o.prim_indices())
             want_any = o.trace(ao, any_hit=True)
-            got = d_hits.cpu().numpy().view(np.uint32)
+            got = to_original(d_hits.cpu().numpy().view(np.uint32), prim_idx)
             cfg = line["config"]
             cfg["oracle_checked_rays"] = int(n_eye + n_ao)
             dd = hit_diff(got, want, "oracle")

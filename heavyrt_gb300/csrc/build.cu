@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kThreads) k_box_partial(const float4* __restri
 // Final box and ZIndexMultCoeff on the box widened by 1e-4
 // (core/builders/lbvh.cpp:41-51,263).
 __global__ void __launch_bounds__(kThreads) k_box_final(const float4* __restrict__ partial, uint32_t nPartial,
-                                                         BuildParams* params)
+                                                         BuildParams* params, int cubic)
 {
   float mn[4] = {1e10f, 1e10f, 1e10f, 1e10f}, mx[4] = {-1e10f, -1e10f, -1e10f, -1e10f};
   for (uint32_t b = threadIdx.x; b < nPartial; b += kThreads)
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kThreads) k_box_final(const float4* __restrict
   if (threadIdx.x != 0) return;
   for (int w = 1; w < kThreads / 32; w++)
     for (int k = 0; k < 4; k++) { mn[k] = lm_min(mn[k], smn[w][k]); mx[k] = lm_max(mx[k], smx[w][k]); }
-  bc::zindex_scale(mn, mx, params);
+  bc::zindex_scale(mn, mx, params, cubic);
 }
 
 // ---------------------------------------------------------------- Morton codes
@@ -401,7 +401,7 @@ cudaError_t build_lbvh(const BuildBuffers& b, int numSMs, cudaStream_t s)
   uint32_t pb = grid_for(b.nVerts, numSMs, 4);
   if (pb > 1024) pb = 1024;
   k_box_partial<<<pb, kThreads, 0, s>>>(b.verts, b.nVerts, partial);
-  k_box_final<<<1, kThreads, 0, s>>>(partial, pb, b.params);
+  k_box_final<<<1, kThreads, 0, s>>>(partial, pb, b.params, b.mortonCubic);
   // 2. Morton codes
   k_morton<<<(N + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.verts, b.idx, N, b.nVerts, b.params, b.keys, b.vals, err);
   cudaError_t e = cudaMemcpyAsync(b.keysUnsorted, b.keys, sizeof(uint32_t) * N, cudaMemcpyDeviceToDevice, s);
@@ -445,7 +445,7 @@ cudaError_t refit_lbvh(const BuildBuffers& b, BuildParams* boxOut, int numSMs, c
   uint32_t pb = grid_for(b.nVerts, numSMs, 4);
   if (pb > 1024) pb = 1024;
   k_box_partial<<<pb, kThreads, 0, s>>>(b.verts, b.nVerts, partial);
-  k_box_final<<<1, kThreads, 0, s>>>(partial, pb, boxOut);
+  k_box_final<<<1, kThreads, 0, s>>>(partial, pb, boxOut, b.mortonCubic);
   const uint32_t g = grid_for(N, numSMs, 8);
   k_leaves<<<g, kThreads, 0, s>>>(b.verts, b.idx, b.vals, b.runStarts, N, b.nVerts, b.params, b.lr, b.tris, b.sortedIdx,
                                   err, b.vertexRecords);

@@ -69,7 +69,8 @@ __global__ void __launch_bounds__(kThreads) k_seg_box_partial(const float4* __re
 }
 
 __global__ void __launch_bounds__(kThreads) k_seg_box_final(const uint32_t* __restrict__ chunkOffsets, uint32_t G,
-                                                            const float4* __restrict__ partial, BuildParams* params)
+                                                            const float4* __restrict__ partial, BuildParams* params,
+                                                            int cubic)
 {
   for (uint32_t s = blockIdx.x * kThreads + threadIdx.x; s < G; s += gridDim.x * kThreads)
   {
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_seg_box_final(const uint32_t* __re
       mn[0] = lm_min(mn[0], a.x); mn[1] = lm_min(mn[1], a.y); mn[2] = lm_min(mn[2], a.z); mn[3] = lm_min(mn[3], a.w);
       mx[0] = lm_max(mx[0], b.x); mx[1] = lm_max(mx[1], b.y); mx[2] = lm_max(mx[2], b.z); mx[3] = lm_max(mx[3], b.w);
     }
-    bc::zindex_scale(mn, mx, &params[s]);
+    bc::zindex_scale(mn, mx, &params[s], cubic);
     params[s].nLeaves = 0;
     params[s].error = 0;
   }
@@ -487,7 +488,8 @@ cudaError_t build_lbvh_batch(const BatchBuffers& b, int numSMs, cudaStream_t s)
 
   if (b.nBoxChunks) k_seg_box_partial<<<b.nBoxChunks, kThreads, 0, s>>>(b.verts, b.vertOffsets, b.boxChunkOffsets, G,
                                                                          b.boxPartial);
-  k_seg_box_final<<<(G + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.boxChunkOffsets, G, b.boxPartial, b.params);
+  k_seg_box_final<<<(G + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.boxChunkOffsets, G, b.boxPartial, b.params,
+                                                                      b.mortonCubic);
   k_seg_morton<<<(N + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.verts, b.idx, b.vertOffsets, b.triOffsets, G, N,
                                                                    b.params, b.keys, b.vals, b.errorWord);
   cudaError_t e = cudaMemcpyAsync(b.keysUnsorted, b.keys, sizeof(uint32_t) * N, cudaMemcpyDeviceToDevice, s);

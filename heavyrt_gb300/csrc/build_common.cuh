@@ -90,17 +90,28 @@ __device__ __forceinline__ uint32_t morton_code(const float4& a, const float4& b
 }
 
 // ZIndexMultCoeff on the box widened by 1e-4 (core/builders/lbvh.cpp:41-51,263).
-__device__ __forceinline__ void zindex_scale(const float* mn, const float* mx, BuildParams* params)
+// cubic = 1 (the engine's HRT_MORTON_CUBIC frame, no reference counterpart):
+// x, y and z share the scale of the longest widened extent, so a cell of the
+// Morton grid is a cube and a flat scene (a heightfield) does not spend a
+// third of the code's bits splitting its thin axis; the codes are still
+// 3 x 10 bits in [0, 1023] per axis.
+__device__ __forceinline__ void zindex_scale(const float* mn, const float* mx, BuildParams* params, int cubic = 0)
 {
+  float ext[4];
   for (int c = 0; c < 4; c++)
   {
     params->bmin[c] = mn[c];
     params->bmax[c] = mx[c];
     const float lo = __fsub_rn(mn[c], 1e-4f);
     const float hi = __fadd_rn(mx[c], 1e-4f);
-    const float ext = __fsub_rn(hi, lo);
-    float inv = __fdiv_rn(1.0f, ext);
-    if (c < 3 && fabsf(ext) < 1e-20f) inv = 0.0f;
+    ext[c] = __fsub_rn(hi, lo);
+  }
+  const float emax = lm_max(ext[0], lm_max(ext[1], ext[2]));
+  for (int c = 0; c < 4; c++)
+  {
+    const float e = (cubic && c < 3) ? emax : ext[c];
+    float inv = __fdiv_rn(1.0f, e);
+    if (c < 3 && fabsf(e) < 1e-20f) inv = 0.0f;
     params->scale[c] = __fmul_rn(1024.0f, inv);
   }
 }

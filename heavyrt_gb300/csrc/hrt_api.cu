@@ -211,6 +211,8 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
   b.params = g.params;
   b.scratch = scratch;
   b.vertexRecords = triTest == HRT_TRI_WATERTIGHT;
+  b.mortonCubic = s->mortonFrame == HRT_MORTON_CUBIC && &g != &s->tlas;
+  g.mortonFrame = b.mortonCubic ? HRT_MORTON_CUBIC : HRT_MORTON_PER_AXIS;
 
   cudaEvent_t e0, e1;
   HRT_CUDA(ctx, cudaEventCreate(&e0));
@@ -330,6 +332,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
   b.G = G;
   b.nTris = (uint32_t)N;
   b.vertexRecords = s->triTest == HRT_TRI_WATERTIGHT;
+  b.mortonCubic = s->mortonFrame == HRT_MORTON_CUBIC;
   // scene-box chunks of each geometry's vertices
   std::vector<uint32_t> hChunk(G + 1, 0);
   for (uint32_t i = 0; i < G; i++) hChunk[i + 1] = hChunk[i] + (hv[i + 1] - hv[i] + kBatchBoxChunk - 1) / kBatchBoxChunk;
@@ -479,6 +482,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
     g.shared = true;
     g.bvh4Merge = s->bvh4Merge;
     g.triTest = s->triTest;
+    g.mortonFrame = s->mortonFrame;
     g.nTris = Ni;
     g.nVerts = hv[i + 1] - hv[i];
     g.nLeaves = Li;
@@ -672,6 +676,7 @@ int refit_geometry(hrt_scene* s, Geom& g, const float* vpos, const uint32_t* idx
   b.params = g.params;
   b.scratch = scratch;
   b.vertexRecords = g.triTest == HRT_TRI_WATERTIGHT;
+  b.mortonCubic = g.mortonFrame == HRT_MORTON_CUBIC;  // only the vertex box is recomputed
   cudaEvent_t e0, e1;
   HRT_CUDA(ctx, cudaEventCreate(&e0));
   HRT_CUDA(ctx, cudaEventCreate(&e1));
@@ -1521,6 +1526,11 @@ int hrt_scene_set_option(hrt_scene* s, int option, int value)
       s->l2PersistMB = value;
       return HRT_OK;
     }
+    case HRT_OPTION_MORTON_FRAME:
+      if (value != HRT_MORTON_PER_AXIS && value != HRT_MORTON_CUBIC)
+        return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown Morton frame");
+      s->mortonFrame = value;
+      return HRT_OK;
     case HRT_OPTION_TRIANGLE_TEST:
       if (value != HRT_TRI_MOLLER_TRUMBORE && value != HRT_TRI_WATERTIGHT)
         return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown triangle test");

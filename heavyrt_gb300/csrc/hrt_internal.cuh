@@ -51,6 +51,7 @@ struct Geom
   bool         shared = false;    // arrays point into a batch allocation (hrt_add_geoms_triangles3f_batched)
   int          bvh4Merge = 0;     // leaf merge bound the 4-wide nodes were built with
   int          triTest = 0;       // triangle records for HRT_TRI_* (1: vertices, for the watertight test)
+  int          mortonFrame = 0;   // HRT_MORTON_* the tree was built in (a refit keeps it)
 };
 
 struct Instance
@@ -79,6 +80,7 @@ struct hrt_scene
   int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
   int                   useTlas = 1;    // HRT_OPTION_TLAS
   int                   triTest = 0;    // HRT_OPTION_TRIANGLE_TEST
+  int                   mortonFrame = 0;  // HRT_OPTION_MORTON_FRAME
   int                   l2PersistMB = 0;  // HRT_OPTION_L2_PERSIST
   size_t                singleNodeBytes = 0;  // node array of the single instance's geometry
   Geom                  tlas;           // instance tree of the committed scene (nTris = 0: none)

@@ -52,6 +52,7 @@ struct BuildBuffers
   BuildParams* params;        // device
   void*      scratch;         // build_scratch_bytes(nTris)
   int        vertexRecords = 0;  // 1: triangle records hold {A, B, C} (watertight test), else {A, B-A, C-A}
+  int        mortonCubic = 0;    // 1: one Morton scale for x, y, z (that of the longest axis)
 };
 size_t build_scratch_bytes(uint32_t nTris);
 // Runs the whole LBVH build asynchronously on `stream`.  Errors found on the
@@ -111,6 +112,7 @@ struct BatchBuffers
   uint32_t        nBoxChunks;
   float4*         boxPartial;       // 2 * nBoxChunks
   int             vertexRecords = 0;  // as BuildBuffers::vertexRecords
+  int             mortonCubic = 0;    // as BuildBuffers::mortonCubic
 };
 constexpr uint32_t kBatchBoxChunk = 8192;
 size_t build_batch_scratch_bytes(uint32_t nTris, uint32_t G);

@@ -45,7 +45,8 @@ EXPORT_PAIR_RECORDS = 10
 
 # node layouts (include/hrt.h); names accepted as CreateSceneRT's a_layoutName
 LAYOUT_BVH2, LAYOUT_BVH4_F32, LAYOUT_BVH4_F16, LAYOUT_BVH4_Q8 = 0, 1, 2, 3
-OPTION_BVH4_MERGE, OPTION_TLAS, OPTION_TRIANGLE_TEST, OPTION_L2_PERSIST = 1, 2, 3, 4
+OPTION_BVH4_MERGE, OPTION_TLAS, OPTION_TRIANGLE_TEST, OPTION_L2_PERSIST, OPTION_MORTON_FRAME = 1, 2, 3, 4, 5
+MORTON_PER_AXIS, MORTON_CUBIC = 0, 1
 TRI_MOLLER_TRUMBORE, TRI_WATERTIGHT = 0, 1
 TRI_TEST_NAMES = {"mt": TRI_MOLLER_TRUMBORE, "moller_trumbore": TRI_MOLLER_TRUMBORE, "watertight": TRI_WATERTIGHT}
 LAYOUT_NAMES = {"": LAYOUT_BVH2, "bvh2": LAYOUT_BVH2, "bvh4": LAYOUT_BVH4_F32, "bvh4_f32": LAYOUT_BVH4_F32,
@@ -337,6 +338,10 @@ class SceneRT:
     def set_l2_persist(self, mib: int):
         """Keep the node array in L2 for queries (persisting set-aside of `mib` MiB; 0 off)."""
         self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_L2_PERSIST, int(mib)), "set_option")
+
+    def set_morton_frame(self, frame: int):
+        """MORTON_PER_AXIS (the reference's grid) or MORTON_CUBIC, for geometry added afterwards."""
+        self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_MORTON_FRAME, int(frame)), "set_option")
 
     def set_triangle_test(self, test: int):
         """TRI_MOLLER_TRUMBORE (the reference's test) or TRI_WATERTIGHT; before the first geometry."""

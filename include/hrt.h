@@ -157,6 +157,21 @@ int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
  *                          set-aside).  0 (default): no window.  Results
  *                          never depend on it. */
 #define HRT_OPTION_L2_PERSIST 4
+/*   HRT_OPTION_MORTON_FRAME  the grid the Morton codes of geometry added
+ *                          afterwards are quantised on:
+ *     HRT_MORTON_PER_AXIS  (default) HeavyRT's ZIndexMultCoeff
+ *                          (core/builders/lbvh.cpp:41-51): each axis of the
+ *                          scene box divided into 1024 cells; the build is
+ *                          the reference's bit for bit;
+ *     HRT_MORTON_CUBIC     one scale for all three axes, that of the longest
+ *                          extent (cubic cells), so a flat or elongated scene
+ *                          does not split its short axes as often as its long
+ *                          ones.  The same LBVH otherwise; a different tree, so
+ *                          hits equal the reference's except at ties within
+ *                          1e-5 relative t. */
+#define HRT_OPTION_MORTON_FRAME 5
+#define HRT_MORTON_PER_AXIS     0
+#define HRT_MORTON_CUBIC        1
 int hrt_scene_set_option(hrt_scene* scene, int option, int value);
 
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */

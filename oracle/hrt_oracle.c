@@ -90,15 +90,24 @@ static void aabb_from_vertices(const float* v4, uint32_t nV, float bmin[4], floa
     }
 }
 
-/* ZIndexMultCoeff on the biased box, core/builders/lbvh.cpp:41-51 and :263. */
-static void zindex_scale(const float bmin[4], const float bmax[4], float scale[4])
+/* ZIndexMultCoeff on the biased box, core/builders/lbvh.cpp:41-51 and :263.
+ * cubic != 0 restates the engine's HRT_MORTON_CUBIC frame (no reference
+ * counterpart): x, y and z take the scale of the longest biased extent. */
+static void zindex_scale(const float bmin[4], const float bmax[4], float scale[4], int cubic)
 {
+  float ext[4];
   for (int c = 0; c < 4; c++)
   {
     const float lo = bmin[c] - 1e-4f;
     const float hi = bmax[c] + 1e-4f;
-    float inv = 1.0f / (hi - lo);
-    if (c < 3 && fabsf(hi - lo) < 1e-20f) inv = 0.0f;
+    ext[c] = hi - lo;
+  }
+  const float emax = fmax_lm(ext[0], fmax_lm(ext[1], ext[2]));
+  for (int c = 0; c < 4; c++)
+  {
+    const float e = (cubic && c < 3) ? emax : ext[c];
+    float inv = 1.0f / e;
+    if (c < 3 && fabsf(e) < 1e-20f) inv = 0.0f;
     scale[c] = 1024.0f * inv;
   }
 }
@@ -479,7 +488,15 @@ static void peach_convert(ora_bvh* B)
 /* Whole build: scene box, Morton codes, stable sort, run compaction, leaves,
  * Karras hierarchy, refit, peach relayout; then the per-geometry arrays that
  * BVH2CommonRT::AddGeom_Triangles3f keeps (core/BVH2CommonRT_host.cpp:45-98). */
+ora_bvh* ora_build_frame(const float* v4, uint32_t nV, const uint32_t* idx, uint32_t nIdx, int cubic);
+
 ora_bvh* ora_build(const float* v4, uint32_t nV, const uint32_t* idx, uint32_t nIdx)
+{
+  return ora_build_frame(v4, nV, idx, nIdx, 0);
+}
+
+/* The same build on the engine's cubic Morton grid when cubic != 0. */
+ora_bvh* ora_build_frame(const float* v4, uint32_t nV, const uint32_t* idx, uint32_t nIdx, int cubic)
 {
   ora_bvh* B = (ora_bvh*)calloc(1, sizeof(ora_bvh));
   const uint32_t N = nIdx / 3;
@@ -496,7 +513,7 @@ ora_bvh* ora_build(const float* v4, uint32_t nV, const uint32_t* idx, uint32_t n
   if (N == 0) return B;
 
   aabb_from_vertices(B->verts, nV, B->bmin, B->bmax);
-  zindex_scale(B->bmin, B->bmax, B->scale);
+  zindex_scale(B->bmin, B->bmax, B->scale, cubic);
   B->pairsUnsorted = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (size_t)N);
   morton_codes(B->verts, idx, N, B->bmin, B->scale, B->pairsUnsorted);
   B->pairsSorted = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (size_t)N);

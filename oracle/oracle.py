@@ -36,6 +36,8 @@ def lib() -> C.CDLL:
         vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
         L.ora_build.restype = vp
         L.ora_build.argtypes = [vp, u32, vp, u32]
+        L.ora_build_frame.restype = vp
+        L.ora_build_frame.argtypes = [vp, u32, vp, u32, i32]
         L.ora_free.argtypes = [vp]
         for f in ("ora_num_tris", "ora_num_leaves", "ora_num_nodes"):
             getattr(L, f).restype = u32
@@ -67,10 +69,13 @@ def _p(a):
 class OracleBVH:
     """LBVH built by the C restatement: stage arrays + peach layout + traversal."""
 
-    def __init__(self, verts: np.ndarray, idx: np.ndarray):
+    def __init__(self, verts: np.ndarray, idx: np.ndarray, cubic: bool = False):
+        """cubic=True builds on the engine's cubic Morton grid instead of the
+        reference's per-axis one."""
         self._v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 4)
         self._i = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1)
-        self._h = C.c_void_p(lib().ora_build(_p(self._v), self._v.shape[0], _p(self._i), self._i.size))
+        self._h = C.c_void_p(lib().ora_build_frame(_p(self._v), self._v.shape[0], _p(self._i), self._i.size,
+                                                   1 if cubic else 0))
         self.n_tris = lib().ora_num_tris(self._h)
         self.n_leaves = lib().ora_num_leaves(self._h)
         self.n_nodes = lib().ora_num_nodes(self._h)
