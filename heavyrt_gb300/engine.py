@@ -100,7 +100,7 @@ class ServerConfig(C.Structure):
 
     _fields_ = [("memoryBudget", C.c_uint64), ("slotRays", C.c_uint64), ("slots", C.c_uint32),
                 ("maxScenes", C.c_uint32), ("maxBatchRequests", C.c_uint32), ("layout", C.c_int),
-                ("bvh4Merge", C.c_int)]
+                ("bvh4Merge", C.c_int), ("mortonFrame", C.c_int)]
 
 
 class RequestInfo(C.Structure):
@@ -576,12 +576,13 @@ class Server:
     memory-budget admission, continuous batching of ray requests."""
 
     def __init__(self, ctx: Context | None = None, memory_budget: int = 0, slot_rays: int = 0, slots: int = 0,
-                 max_scenes: int = 0, max_batch_requests: int = 0, layout=LAYOUT_BVH2, bvh4_merge: int = 0):
+                 max_scenes: int = 0, max_batch_requests: int = 0, layout=LAYOUT_BVH2, bvh4_merge: int = 0,
+                 morton_frame: int = MORTON_PER_AXIS):
         self.ctx = ctx or default_context()
         if isinstance(layout, str):
             layout = LAYOUT_NAMES[layout.lower()]
         cfg = ServerConfig(memory_budget, slot_rays, slots, max_scenes, max_batch_requests, int(layout),
-                           int(bvh4_merge))
+                           int(bvh4_merge), int(morton_frame))
         self._h = C.c_void_p()
         self.ctx.check(lib().hrt_server_create(self.ctx.handle, C.byref(cfg), C.byref(self._h)), "hrt_server_create")
 

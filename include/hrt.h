@@ -382,6 +382,7 @@ typedef struct hrt_server_config
   uint32_t maxBatchRequests; /* requests per batch; 0 = 1024                               */
   int      layout;           /* HRT_LAYOUT_* of every scene                                */
   int      bvh4Merge;        /* HRT_OPTION_BVH4_MERGE value for 4-wide layouts             */
+  int      mortonFrame;      /* HRT_MORTON_* grid of every scene's build                   */
 } hrt_server_config;
 
 /* Result of one request; times in seconds since the server was created. */

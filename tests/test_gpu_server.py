@@ -222,3 +222,33 @@ def test_request_errors(native):
     t = srv.submit(sid, 0, rays.ctypes.data, 0, out.ctypes.data)  # empty request
     assert srv.wait(t)[0] == 0
     srv.close()
+
+
+def test_cubic_morton_frame_scenes(native):
+    """A server configured with the cubic Morton frame builds every scene on
+    that grid: binary-layout hits are the oracle's on the same grid bit for bit,
+    any-hit flags are the reference's; a frame out of range is refused."""
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    with pytest.raises(E.HrtError):
+        E.Server(slot_rays=4096, slots=1, morton_frame=7)
+    srv = E.Server(slot_rays=1 << 18, slots=2, morton_frame=E.MORTON_CUBIC)
+    scenes = _scenes()[:2] + _scenes()[4:]
+    ids = [srv.add_scene(v, idx, evictable=False) for v, idx in scenes]
+    assert all(srv.scene_state(i, timeout=120) == E.SCENE_READY for i in ids)
+    for k, (v, idx) in enumerate(scenes):
+        rays = np.concatenate([wl.rays_at_triangles(40 + k, v, idx, 3000, jitter=0.03), wl.sphere_rays(k, 1000)])
+        oc = orc.OracleBVH(v, idx, cubic=True)
+        want = oc.trace(rays).view(np.uint32).reshape(-1, 8).copy()
+        hit = want[:, 1] != MISS
+        want[hit, 2] = ids[k] & 0xFFFF
+        want[hit, 3] = ids[k] & 0xFFFF
+        out = _out(0, len(rays))
+        assert srv.wait(srv.submit_array(ids[k], 0, rays, out))[0] == 0
+        np.testing.assert_array_equal(out, want, err_msg=f"scene {k}")
+        flags = _out(1, len(rays))
+        assert srv.wait(srv.submit_array(ids[k], 1, rays, flags))[0] == 0
+        np.testing.assert_array_equal(flags.astype(bool), orc.OracleBVH(v, idx).trace(rays, any_hit=True))
+    srv.close()
