@@ -90,8 +90,15 @@ def parse():
     p.add_argument("--no-watertight", action="store_true", help="skip the watertight triangle-test measurement")
     p.add_argument("--morton-frame", default="cubic", choices=["cubic", "per_axis"],
                    help="Morton grid of the headline scene: cubic cells (engine option) or the reference's per-axis grid")
+    p.add_argument("--bvh4-collapse", default="largest_first", choices=["largest_first", "even_depth"],
+                   help="4-wide collapse of the headline scene: largest subtrees opened first (engine option) or "
+                        "the reference's even-depth rule")
+    p.add_argument("--split", default="replicas", choices=["replicas", "rays"],
+                   help="N > 1: every rank traces the whole frame (replicas, weak scaling) or its share of the "
+                        "frame's eye and AO rays, results gathered on rank 0 through host memory (strong scaling)")
     p.add_argument("--no-frame-compare", action="store_true",
-                   help="skip timing the headline layout on the reference's per-axis grid")
+                   help="skip timing the headline layout on the reference's own tree (per-axis grid, even-depth "
+                        "collapse) and with the even-depth collapse alone")
     p.add_argument("--eye-order", default="tiles", choices=["tiles", "given"],
                    help="eye rays traced in 4x8 pixel tiles of the image (index arithmetic) or in the order given")
     p.add_argument("--l2-persist", type=int, default=64, metavar="MIB",
@@ -647,12 +654,15 @@ def run_precision(ctx, args) -> dict:
     return res
 
 
-def apply_frame(scene, args):
-    """The headline scene's Morton grid (before its first geometry)."""
+def apply_frame(scene, args, collapse=True):
+    """The headline scene's build options (before its first geometry): its
+    Morton grid and, for 4-wide layouts, its collapse rule."""
     from heavyrt_gb300 import engine as E
 
     if args.morton_frame == "cubic":
         scene.set_morton_frame(E.MORTON_CUBIC)
+    if collapse and args.bvh4_collapse == "largest_first":
+        scene.set_bvh4_collapse(E.BVH4_COLLAPSE_LARGEST_FIRST)
 
 
 def run_l2_window(scene, d_eye, d_ao, d_hits, d_any, args) -> dict:
@@ -1176,12 +1186,14 @@ def run_engine(args):
             print(json.dumps({"frames": run_frames(ctx, args, w)}), flush=True)
         return 0
 
-    def make_scene(layout, frame=True):
+    def make_scene(layout, frame=True, collapse=True):
         sc = SceneRT(ctx, layout=layout)
         if layout != "bvh2":
             sc.set_bvh4_merge(args.merge)
         if frame:
-            apply_frame(sc, args)
+            apply_frame(sc, args, collapse)
+        elif collapse and args.bvh4_collapse == "largest_first":
+            sc.set_bvh4_collapse(E.BVH4_COLLAPSE_LARGEST_FIRST)
         g = sc.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
         sc.AddInstance(g)
         sc.CommitScene()
@@ -1201,7 +1213,25 @@ def run_engine(args):
 
     eye_hits = scene.RayQuery_NearestHit(w.eye_rays)
     ao = ao_from_hits(w, eye_hits, scene.export(gid, E.EXPORT_SORTED_INDICES))
+    frame_eye, frame_ao = w.eye_rays, ao
+    frame_rays = frame_eye.shape[0] + frame_ao.shape[0]
+    split = args.split == "rays" and world > 1
+    if split:
+        # this rank's share of the frame: whole 8-row bands of the image (the
+        # tile order stays within the share) and a run of AO rays
+        e0, e1 = replicas.partition(frame_eye.shape[0], rk, align=8 * args.width)
+        a0, a1 = replicas.partition(frame_ao.shape[0], rk, align=16)
+        w.eye_rays = np.ascontiguousarray(frame_eye[e0:e1])
+        ao = np.ascontiguousarray(frame_ao[a0:a1])
+        # sections that make or trace whole frames of their own stay out
+        args.no_frames = args.no_watertight = args.no_l2_sweep = args.no_frame_compare = args.no_plain = True
+        args.no_served = args.no_batched = args.no_precision = True
     n_eye, n_ao = w.eye_rays.shape[0], ao.shape[0]
+
+    def job_rate(local_units, ms):
+        """Whole-job units per second: the frame over the slowest rank's time
+        when the ranks split it, every replica's units otherwise."""
+        return frame_rays / (ms * 1e-3) if split else replicas.job_throughput(rk, local_units, ms)
 
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
@@ -1273,7 +1303,7 @@ def run_engine(args):
     total_ms = replicas.max_over_ranks(rk, total_ms, "cuda")  # the slowest replica's time
     ms_per_step = total_ms / args.steps
     rays_per_step = n_eye + n_ao
-    value = replicas.job_throughput(rk, rays_per_step, ms_per_step) / 1e6
+    value = job_rate(rays_per_step, ms_per_step) / 1e6
     if args.ncu:
         print(json.dumps({"ncu_run": True, "ms_per_step": ms_per_step, "value": value}), flush=True)
         return 0
@@ -1318,54 +1348,74 @@ def run_engine(args):
 
     e2e_async_s = time_steps(e2e_step)
     e2e_s = time_steps(e2e_step_sync)
-    e2e_value = replicas.job_throughput(rk, rays_per_step, 1e3 * e2e_s) / 1e6
-    e2e_async_value = replicas.job_throughput(rk, rays_per_step, 1e3 * e2e_async_s) / 1e6
+    e2e_value = job_rate(rays_per_step, 1e3 * e2e_s) / 1e6
+    e2e_async_value = job_rate(rays_per_step, 1e3 * e2e_async_s) / 1e6
     got_any = pin_any.array(np.uint8)[:n_ao].copy()
 
-    # the same frame with its rays made on the device: camera parameters in,
-    # eye hits and AO flags out (no ray crosses the host link)
-    pp = w.params
-    cap = n_eye * pp["ao_per_hit"]
-    g_eye = torch.empty((n_eye, 8), dtype=torch.float32, device="cuda")
-    g_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
-    g_ao = torch.empty((cap, 8), dtype=torch.float32, device="cuda")
-    g_any = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    # split frame: every rank's results gathered on rank 0 through host
+    # memory (after the timed region) and compared with rank 0 tracing the
+    # whole frame itself
+    split_check = None
+    if split:
+        grp = replicas.host_group(rk)
+        all_hits = replicas.gather_rows(rk, d_hits.cpu().numpy().view(np.uint32), grp)
+        all_any = replicas.gather_rows(rk, got_any, grp)
+        if rank == 0:
+            f_hits = scene.RayQuery_NearestHit(frame_eye).view(np.uint32).reshape(-1, 8)
+            f_any = scene.RayQuery_AnyHit(frame_ao).astype(np.uint8)
+            split_check = {"ranks": world, "gathered_rays": int(all_hits.shape[0] + all_any.shape[0]),
+                           "frame_rays": int(frame_rays),
+                           "nearest_mismatch": int(np.count_nonzero(np.any(all_hits != f_hits, axis=1))),
+                           "anyhit_mismatch": int(np.count_nonzero(all_any != f_any))}
 
-    copy_stream = torch.cuda.Stream()
-    eye_done = torch.cuda.Event()
+    raygen_e2e = None
+    if not split:
+        # the same frame with its rays made on the device: camera parameters in,
+        # eye hits and AO flags out (no ray crosses the host link)
+        pp = w.params
+        cap = n_eye * pp["ao_per_hit"]
+        g_eye = torch.empty((n_eye, 8), dtype=torch.float32, device="cuda")
+        g_hits = torch.empty((n_eye, 8), dtype=torch.int32, device="cuda")
+        g_ao = torch.empty((cap, 8), dtype=torch.float32, device="cuda")
+        g_any = torch.empty(cap, dtype=torch.uint8, device="cuda")
 
-    def raygen_step():
-        # the eye hits go home on a second stream while the AO rays are made
-        # and traced; the AO flags are written straight into page-locked host memory
-        ctx.gen_pinhole_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, args.width, args.height, 0.0, 1e9,
-                             g_eye.data_ptr(), sh)
-        scene.query_device(0, g_eye.data_ptr(), n_eye, g_hits.data_ptr(), sh)
-        eye_done.record(stream)
-        copy_stream.wait_event(eye_done)
-        with torch.cuda.stream(copy_stream):
-            pin_hits_d.copy_(g_hits, non_blocking=True)
-        k = scene.gen_ao_rays(pp["ao_seed"], g_eye.data_ptr(), g_hits.data_ptr(), n_eye, pp["ao_per_hit"],
-                              pp["ao_length"], pp["ao_offset"], g_ao.data_ptr(), cap, 0, sh)
-        scene.query_device(1, g_ao.data_ptr(), k, pin_any_d.data_ptr(), sh)
-        torch.cuda.synchronize()
-        return k
+        copy_stream = torch.cuda.Stream()
+        eye_done = torch.cuda.Event()
 
-    pin_hits_d = torch.empty((n_eye, 8), dtype=torch.int32).pin_memory()
-    pin_any_d = torch.empty(cap, dtype=torch.uint8).pin_memory()
-    for _ in range(3):
-        n_ao_dev = raygen_step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        n_ao_dev = raygen_step()
-    rg_s = replicas.max_over_ranks(rk, (time.perf_counter() - t0) / args.steps, "cuda")
-    raygen_e2e = {"value": round(replicas.job_throughput(rk, n_eye + n_ao_dev, 1e3 * rg_s) / 1e6, 3), "unit": UNIT,
-                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(32 * n_eye + n_ao_dev),
-                  "ao_rays": int(n_ao_dev), "ao_rays_equal_host_count": bool(n_ao_dev == n_ao),
-                  "anyhit_equal_host_frame": bool(np.array_equal(pin_any_d[:n_ao_dev].numpy(), got_any))
-                  if n_ao_dev == n_ao else False}
-    del g_eye, g_hits, g_ao, g_any
+        def raygen_step():
+            # the eye hits go home on a second stream while the AO rays are made
+            # and traced; the AO flags are written straight into page-locked host memory
+            ctx.gen_pinhole_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, args.width, args.height, 0.0, 1e9,
+                                 g_eye.data_ptr(), sh)
+            scene.query_device(0, g_eye.data_ptr(), n_eye, g_hits.data_ptr(), sh)
+            eye_done.record(stream)
+            copy_stream.wait_event(eye_done)
+            with torch.cuda.stream(copy_stream):
+                pin_hits_d.copy_(g_hits, non_blocking=True)
+            k = scene.gen_ao_rays(pp["ao_seed"], g_eye.data_ptr(), g_hits.data_ptr(), n_eye, pp["ao_per_hit"],
+                                  pp["ao_length"], pp["ao_offset"], g_ao.data_ptr(), cap, 0, sh)
+            scene.query_device(1, g_ao.data_ptr(), k, pin_any_d.data_ptr(), sh)
+            torch.cuda.synchronize()
+            return k
+
+        pin_hits_d = torch.empty((n_eye, 8), dtype=torch.int32).pin_memory()
+        pin_any_d = torch.empty(cap, dtype=torch.uint8).pin_memory()
+        for _ in range(3):
+            n_ao_dev = raygen_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            n_ao_dev = raygen_step()
+        rg_s = replicas.max_over_ranks(rk, (time.perf_counter() - t0) / args.steps, "cuda")
+        raygen_e2e = {"value": round(replicas.job_throughput(rk, n_eye + n_ao_dev, 1e3 * rg_s) / 1e6, 3), "unit": UNIT,
+                      "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(32 * n_eye + n_ao_dev),
+                      "ao_rays": int(n_ao_dev), "ao_rays_equal_host_count": bool(n_ao_dev == n_ao),
+                      "anyhit_equal_host_frame": bool(np.array_equal(pin_any_d[:n_ao_dev].numpy(), got_any))
+                      if n_ao_dev == n_ao else False}
+        del g_eye, g_hits, g_ao, g_any
     for b in (pin_eye, pin_ao, pin_hits, pin_any):
         b.free()
+    if split:
+        raygen_e2e = {"skipped": "the ranks split the frame's rays; device ray generation makes whole frames"}
 
     # the persisting-L2 set-aside ends with the headline scene's legs (the
     # other sections run without it)
@@ -1419,10 +1469,9 @@ def run_engine(args):
                 "at_plain_rate_gb_s": round((blb_eye * n_eye + blb_ao * n_ao) / ((pe_ms + pa_ms) * 1e-3) / 1e9, 1)}
         ps.close()
 
-    # the headline layout on the reference's per-axis Morton grid, same launch shapes
-    frame_cmp = None
-    if args.morton_frame == "cubic" and not args.no_frame_compare and not args.ncu:
-        fs, _ = make_scene(args.layout, frame=False)
+    # the headline layout on other trees over the same triangles, same launch shapes
+    def compare_tree(label, frame, collapse):
+        fs, _ = make_scene(args.layout, frame=frame, collapse=collapse)
         for k in (0, 1):
             fs.set_trace_config(k, **scene.trace_config(k))
         if args.l2_persist:
@@ -1446,15 +1495,25 @@ def run_engine(args):
         fe_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in fe)
         fa_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in fe)
         fp, ft = fs.query_counters(1, d_ao.data_ptr(), n_ao, sh)
-        frame_cmp = {"frame": "per_axis (the reference's ZIndexMultCoeff grid)", "eye_ms": round(fe_ms, 4),
-                     "ao_ms": round(fa_ms, 4), "mrays_s": round((n_eye + n_ao) / (fe_ms + fa_ms) / 1e3, 2),
-                     "node_fetches_per_ao_ray": round(fp / n_ao, 3), "tri_tests_per_ao_ray": round(ft / n_ao, 3),
-                     **hit_diff(to_original(d_hits.cpu().numpy().view(np.uint32), prim_idx),
-                                to_original(f_hits.cpu().numpy().view(np.uint32),
-                                            fs.export(0, E.EXPORT_PRIM_INDICES)), "per_axis"),
-                     "anyhit_mismatch_vs_per_axis": int(np.count_nonzero(f_any.cpu().numpy() != d_any.cpu().numpy()))}
+        out = {"tree": label, "eye_ms": round(fe_ms, 4), "ao_ms": round(fa_ms, 4),
+               "mrays_s": round((n_eye + n_ao) / (fe_ms + fa_ms) / 1e3, 2),
+               "node_fetches_per_ao_ray": round(fp / n_ao, 3), "tri_tests_per_ao_ray": round(ft / n_ao, 3),
+               **hit_diff(to_original(d_hits.cpu().numpy().view(np.uint32), prim_idx),
+                          to_original(f_hits.cpu().numpy().view(np.uint32), fs.export(0, E.EXPORT_PRIM_INDICES)),
+                          "other"),
+               "anyhit_mismatch_vs_other": int(np.count_nonzero(f_any.cpu().numpy() != d_any.cpu().numpy()))}
         fs.close()
         del f_hits, f_any
+        return out
+
+    tree_cmp = {}
+    if not args.no_frame_compare and not args.ncu:
+        if args.morton_frame == "cubic" or (args.layout != "bvh2" and args.bvh4_collapse == "largest_first"):
+            tree_cmp["reference_tree"] = compare_tree(
+                "the reference's tree: per-axis ZIndexMultCoeff grid"
+                + (", even-depth BVH2ToBVH4 collapse" if args.layout != "bvh2" else ""), False, False)
+        if args.morton_frame == "cubic" and args.layout != "bvh2" and args.bvh4_collapse == "largest_first":
+            tree_cmp["even_depth_collapse"] = compare_tree("cubic grid, even-depth collapse", True, False)
 
     # roofline of the dominant kernel
     eye_avg, ao_avg = statistics.mean(eye_ms), statistics.mean(ao_ms)
@@ -1485,9 +1544,10 @@ def run_engine(args):
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "strong" if split else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w.name, "tris": int(w.idx.size // 3), "eye_rays": int(n_eye), "ao_rays": int(n_ao),
-                   "layout": LAYOUT_DESC[args.layout], "parallelism": f"replicas{world}",
+                   "layout": LAYOUT_DESC[args.layout],
+                   "parallelism": f"rays_split{world}" if split else f"replicas{world}",
                    "l2": f"inputs larger than L2: rays {(d_eye.nbytes + d_ao.nbytes) / 1e6:.0f} MB, "
                          f"BVH+triangles {info['bytes'] / 1e6:.0f} MB",
                    "build_ms_median": round(statistics.median(build_ms), 3),
@@ -1515,15 +1575,19 @@ def run_engine(args):
     line["config"]["bvh4_merge"] = args.merge if args.layout != "bvh2" else None
     line["config"]["l2_persist_mib"] = args.l2_persist
     line["config"]["morton_frame"] = args.morton_frame
+    line["config"]["bvh4_collapse"] = args.bvh4_collapse if args.layout != "bvh2" else None
     line["config"]["node_pairs_note"] = "node fetches / triangle tests per ray of the headline's own tree"
     line["config"]["tri_tests_per_ao_ray"] = round(ao_tris / n_ao, 3) if n_ao else None
-    if frame_cmp is not None:
-        line["per_axis_frame"] = frame_cmp
+    for name, cmp in tree_cmp.items():
+        line[name] = cmp
         for k in ("mrays_s", "eye_ms", "ao_ms", "node_fetches_per_ao_ray"):
-            line["config"][f"per_axis_frame_{k}"] = frame_cmp[k]
+            line["config"][f"{name}_{k}"] = cmp[k]
     line["config"]["eye_ray_order"] = (f"4x8 pixel tiles of the {args.width}-wide image (index arithmetic, results "
                                        "in ray order)" if args.eye_order == "tiles" else "as given (row-major)")
     line["config"]["launch"] = tuned if tuned is not None else "default"
+    if split:
+        line["split_check"] = split_check
+        line["config"]["frame_rays"] = int(frame_rays)
     if plain is not None:
         line["plain"] = plain
         line["speedup_vs_plain"] = round(line["value"] / plain["mrays_s"], 3)

@@ -10,6 +10,15 @@
 // adjacent).  The root always stays a node.  With this rule the 4-wide nodes
 // are exactly the binary internal nodes at even depth that are not merged.
 //
+// Largest-first rule (a build option): a 4-wide node starts from its binary
+// node's two children and twice opens the internal slot with the most leaves
+// under it (the leftmost of equals) into that slot's two children, in place.
+// The slots' shapes alone decide, so a refit (same topology) keeps the tree.
+// Which binary nodes become 4-wide nodes then depends on the choices above
+// them: the roles are found top down, one 4-wide level per launch, each level
+// a frontier list built with atomics (the roles do not depend on the order
+// within a level; the numbering is the same Karras-order scan as before).
+//
 // Quantised boxes only ever contain the FP32 box they stand for, so a
 // traversal of the quantised tree visits every node the FP32 tree would and
 // can only add visits; the triangle test is unchanged.
@@ -60,26 +69,191 @@ __device__ __forceinline__ void node_range(const BVHNode32* __restrict__ lr, con
   end = (lb + 1 < L) ? runStarts[lb + 1] : nTris;
 }
 
-// Role of internal node i: 1 = 4-wide node, 2 = merged leaf, 0 = absorbed.
+// Whether internal node i, due to become a 4-wide node, becomes one leaf instead.
 // mergeMode 0: merge when both children are leaves (the reference's rule);
 // mergeMode M > 0: merge when the subtree holds at most M triangles.
+__device__ __forceinline__ bool merges(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
+                                       uint32_t L, uint32_t nTris, int mergeMode, uint32_t i)
+{
+  if (i == 0) return false;  // the root stays a node
+  if (mergeMode == 0) return lr[i].leftOffset + 1u >= L && lr[i].escapeIndex + 1u >= L;
+  if (mergeMode == 1) return false;  // an internal node holds two leaves at least, so two triangles
+  uint32_t st, en;
+  node_range(lr, runStarts, L, nTris, i, st, en);
+  return en - st <= (uint32_t)mergeMode;
+}
+
+// Role of internal node i under the even-depth rule: 1 = 4-wide node, 2 =
+// merged leaf, 0 = absorbed.
 __device__ __forceinline__ uint8_t node_role(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
                                              uint32_t L, uint32_t nTris, uint8_t depth, int mergeMode, uint32_t i)
 {
   if ((depth & 1u) != 0u) return 0;
-  bool merge;
-  if (mergeMode == 0)
-    merge = lr[i].leftOffset + 1u >= L && lr[i].escapeIndex + 1u >= L;
-  else if (mergeMode == 1)
-    merge = false;  // an internal node holds two leaves at least, so two triangles
-  else
-  {
-    uint32_t st, en;
-    node_range(lr, runStarts, L, nTris, i, st, en);
-    merge = en - st <= (uint32_t)mergeMode;
-  }
-  return (i != 0 && merge) ? 2 : 1;
+  return merges(lr, runStarts, L, nTris, mergeMode, i) ? 2 : 1;
 }
+
+constexpr int kCollapseLargestFirst = 1;  // HRT_BVH4_COLLAPSE_LARGEST_FIRST
+
+// The binary nodes that become the slots of the 4-wide node of internal node
+// i (L >= 2), left to right; returns their count (2..4).  Even depth: each
+// child's two children, or the child itself when it is a leaf.  Largest
+// first: the two children, then twice the internal slot with the largest
+// descendant count (most leaves; the leftmost of equals) replaced in place by
+// its two children.
+__device__ __forceinline__ int collapse_slots(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ lrCount,
+                                              uint32_t L, int collapse, uint32_t i, uint32_t (&cand)[4])
+{
+  const uint32_t k0 = lr[i].leftOffset, k1 = lr[i].escapeIndex;
+  if (collapse != kCollapseLargestFirst)
+  {
+    const bool in0 = k0 + 1u < L, in1 = k1 + 1u < L;
+    const uint32_t a0 = in0 ? lr[k0].leftOffset : k0, b0 = in0 ? lr[k0].escapeIndex : 0u;
+    const uint32_t a1 = in1 ? lr[k1].leftOffset : k1, b1 = in1 ? lr[k1].escapeIndex : 0u;
+    cand[0] = a0;
+    cand[1] = in0 ? b0 : a1;
+    cand[2] = in0 ? a1 : b1;
+    cand[3] = b1;
+    return (in0 ? 2 : 1) + (in1 ? 2 : 1);
+  }
+  cand[0] = k0;
+  cand[1] = k1;
+  cand[2] = cand[3] = 0u;
+  int n = 2;
+#pragma unroll
+  for (int it = 0; it < 2; it++)
+  {
+    int best = -1;
+    uint32_t bestCount = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (k < n && cand[k] + 1u < L)
+      {
+        const uint32_t c = lrCount[cand[k]];
+        if (best < 0 || c > bestCount)
+        {
+          best = k;
+          bestCount = c;
+        }
+      }
+    if (best < 0) break;
+    uint32_t x = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (k == best) x = cand[k];
+    const uint32_t left = lr[x].leftOffset, right = lr[x].escapeIndex;
+    // slots after `best` move one place right; `best` becomes the two children
+#pragma unroll
+    for (int k = 3; k >= 1; k--)
+      if (k >= best + 2 && k <= n) cand[k] = cand[k - 1];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+    {
+      if (k == best) cand[k] = left;
+      if (k == best + 1) cand[k] = right;
+    }
+    n++;
+  }
+  return n;
+}
+
+// Appends each lane's `cnt` entries (up to four, in `item`) to a list with one
+// atomic per warp; all 32 lanes call it together.  Entries at or past `cap`
+// are dropped and reported.
+__device__ __forceinline__ void warp_append(const uint32_t (&item)[4], int cnt, uint32_t* __restrict__ list,
+                                            uint32_t* count, uint32_t cap, uint32_t* errorWord)
+{
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t incl = (uint32_t)cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(count, total);
+  base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - (uint32_t)cnt;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (k < cnt)
+    {
+      if (base + k < cap)
+        list[base + k] = item[k];
+      else
+        atomicOr(errorWord, kErrLayout);
+    }
+}
+
+// One level of the largest-first roles: every 4-wide node of this level
+// (frontIn) marks its internal slots as 4-wide nodes (appended to frontOut)
+// or merged leaves.  role is zeroed beforehand and the root marked.  The
+// loop runs over warp-uniform bases so that whole warps append together.
+__global__ void __launch_bounds__(kThreads)
+    k_roles_level(const BuildParams* __restrict__ params, const BVHNode32* __restrict__ lr,
+                  const uint32_t* __restrict__ lrCount, const uint32_t* __restrict__ runStarts, uint32_t nTris,
+                  int mergeMode, const uint32_t* __restrict__ frontIn, const uint32_t* __restrict__ countIn,
+                  uint32_t* __restrict__ frontOut, uint32_t* countOut, uint8_t* __restrict__ role, uint32_t* errorWord)
+{
+  const uint32_t L = params->nLeaves;
+  const uint32_t cap = L > 0 ? L - 1 : 0u;  // internal nodes, each a slot of one 4-wide node at most
+  const uint32_t n = min(*countIn, cap);    // a count past the entries written is an error already reported
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warpBase = (blockIdx.x * kThreads + threadIdx.x) & ~31u;
+  for (uint32_t b0 = warpBase; b0 < n; b0 += gridDim.x * kThreads)
+  {
+    const uint32_t f = b0 + lane;
+    uint32_t next[4] = {0u, 0u, 0u, 0u};
+    int cnt = 0;
+    if (f < n)
+    {
+      uint32_t cand[4];
+      const int nc = collapse_slots(lr, lrCount, L, kCollapseLargestFirst, frontIn[f], cand);
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+      {
+        if (k >= nc) break;
+        const uint32_t c = cand[k];
+        if (c + 1u >= L) continue;  // a leaf slot
+        const bool m = merges(lr, runStarts, L, nTris, mergeMode, c);
+        role[c] = m ? 2 : 1;
+        if (!m)
+        {
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            if (j == cnt) next[j] = c;
+          cnt++;
+        }
+      }
+    }
+    warp_append(next, cnt, frontOut, countOut, cap, errorWord);
+  }
+}
+
+// The root as the first level (L >= 2), every other level empty.
+__global__ void k_roles_level_init(const BuildParams* __restrict__ params, uint32_t* __restrict__ front,
+                                   uint32_t* __restrict__ counts, int levels, uint8_t* __restrict__ role)
+{
+  const uint32_t L = params->nLeaves;
+  for (int k = threadIdx.x; k <= levels; k += blockDim.x) counts[k] = (k == 0 && L >= 2) ? 1u : 0u;
+  if (threadIdx.x == 0 && L >= 2)
+  {
+    front[0] = 0;
+    role[0] = 1;
+  }
+}
+
+// A frontier left after the last level would mean a tree deeper than the
+// depth bound: reported, never silently cut.
+__global__ void k_roles_level_check(const uint32_t* __restrict__ counts, int levels, uint32_t* errorWord)
+{
+  if (counts[levels] != 0u) atomicOr(errorWord, kErrLayout);
+}
+
+// Depth bound of the largest-first levels: every 4-wide level descends at
+// least one binary level, and a tree of distinct 30-bit codes is at most 31
+// binary levels deep.
+constexpr int kCollapseLevels = 34;
 
 __global__ void __launch_bounds__(kThreads) k_roles(const BuildParams* __restrict__ params,
                                                     const BVHNode32* __restrict__ lr,
@@ -345,9 +519,10 @@ __device__ __forceinline__ void write_node4(int format, void* __restrict__ nodes
 // 4-wide node indexOf(child) of another role-1 node.  With one leaf (L == 1)
 // the node holds that leaf alone.  Returns the number of used slots.
 template <typename IndexOf>
-__device__ __forceinline__ int node4_slots(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ runStarts,
-                                           uint32_t L, uint32_t nTris, const uint8_t* __restrict__ role,
-                                           IndexOf indexOf, uint32_t i, TriRec* __restrict__ tris, Slot (&slot)[4])
+__device__ __forceinline__ int node4_slots(const BVHNode32* __restrict__ lr, const uint32_t* __restrict__ lrCount,
+                                           const uint32_t* __restrict__ runStarts, uint32_t L, uint32_t nTris,
+                                           int collapse, const uint8_t* __restrict__ role, IndexOf indexOf, uint32_t i,
+                                           TriRec* __restrict__ tris, Slot (&slot)[4])
 {
   if (L == 1u)
   {
@@ -356,14 +531,8 @@ __device__ __forceinline__ int node4_slots(const BVHNode32* __restrict__ lr, con
     slot[0].ref = kLeafBit | runStarts[0];
     return 1;
   }
-  // the children of each internal child (or the leaf child itself), left
-  // child's first, at fixed positions so that the slots stay in registers
-  const uint32_t k0 = lr[i].leftOffset, k1 = lr[i].escapeIndex;
-  const bool in0 = k0 + 1u < L, in1 = k1 + 1u < L;
-  const uint32_t a0 = in0 ? lr[k0].leftOffset : k0, b0 = in0 ? lr[k0].escapeIndex : 0u;
-  const uint32_t a1 = in1 ? lr[k1].leftOffset : k1, b1 = in1 ? lr[k1].escapeIndex : 0u;
-  const uint32_t cand[4] = {a0, in0 ? b0 : a1, in0 ? a1 : b1, b1};
-  const int nc = (in0 ? 2 : 1) + (in1 ? 2 : 1);
+  uint32_t cand[4];
+  const int nc = collapse_slots(lr, lrCount, L, collapse, i, cand);
 #pragma unroll
   for (int k = 0; k < 4; k++)
   {
@@ -399,9 +568,11 @@ __device__ __forceinline__ int node4_slots(const BVHNode32* __restrict__ lr, con
 
 __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restrict__ params,
                                                     const BVHNode32* __restrict__ lr,
+                                                    const uint32_t* __restrict__ lrCount,
                                                     const uint32_t* __restrict__ runStarts, uint32_t nTris,
-                                                    const uint8_t* __restrict__ role, const uint32_t* __restrict__ index,
-                                                    int format, void* __restrict__ nodes, uint32_t maxNodes,
+                                                    int collapse, const uint8_t* __restrict__ role,
+                                                    const uint32_t* __restrict__ index, int format,
+                                                    void* __restrict__ nodes, uint32_t maxNodes,
                                                     TriRec* __restrict__ tris, uint32_t* errorWord)
 {
   const uint32_t L = params->nLeaves;
@@ -421,7 +592,8 @@ __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restric
       }
     }
     Slot slot[4];
-    const int ns = node4_slots(lr, runStarts, L, nTris, role, [&](uint32_t c) { return index[c]; }, i, tris, slot);
+    const int ns = node4_slots(lr, lrCount, runStarts, L, nTris, collapse, role, [&](uint32_t c) { return index[c]; },
+                               i, tris, slot);
     write_node4(format, nodes, outIdx, slot, ns, errorWord);
   }
 }
@@ -433,6 +605,7 @@ __global__ void __launch_bounds__(kThreads) k_emit4(const BuildParams* __restric
 struct SegTree
 {
   const BVHNode32* lr;
+  const uint32_t*  lrCount;
   const uint32_t*  runStarts;
   const uint32_t*  parent;
   TriRec*          tris;
@@ -444,6 +617,7 @@ __device__ __forceinline__ SegTree seg_tree(const Bvh4Batch& b, uint32_t seg)
   SegTree t;
   t.seg = seg;
   t.lr = b.lr + b.nodeOffsets[seg];
+  t.lrCount = b.lrCount + b.nodeOffsets[seg];
   t.parent = b.parent + b.nodeOffsets[seg];
   t.runStarts = b.runStarts + b.leafOffsets[seg];
   t.tris = b.tris + b.triOffsets[seg];
@@ -460,6 +634,63 @@ __global__ void __launch_bounds__(kThreads) k_seg4_depth_roles(Bvh4Batch b, uint
     const SegTree t = seg_tree(b, bc::find_segment(b.intOffsets, b.G, j));
     const uint32_t i = j - t.intBase;
     role[j] = node_role(t.lr, t.runStarts, t.L, t.nTris, node_depth(t.parent, t.L, i), b.mergeMode, i);
+  }
+}
+
+// Largest-first roles of a batch: the geometries' roots as the first level
+// (batch-wide internal node indices), then one launch per level.
+__global__ void __launch_bounds__(kThreads) k_seg4_roles_init(Bvh4Batch b, uint32_t* __restrict__ front,
+                                                              uint32_t* counts, int levels, uint8_t* __restrict__ role)
+{
+  const uint32_t tid = blockIdx.x * kThreads + threadIdx.x;
+  if (tid == 0)
+    for (int k = 1; k <= levels; k++) counts[k] = 0u;
+  for (uint32_t seg = tid; seg < b.G; seg += gridDim.x * kThreads)
+    if (b.leafOffsets[seg + 1] - b.leafOffsets[seg] >= 2u)
+    {
+      const uint32_t j = b.intOffsets[seg];
+      role[j] = 1;
+      front[atomicAdd(counts, 1u)] = j;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_seg4_roles_level(Bvh4Batch b, uint32_t nInt, const uint32_t* __restrict__ frontIn,
+                       const uint32_t* __restrict__ countIn, uint32_t* __restrict__ frontOut, uint32_t* countOut,
+                       uint8_t* __restrict__ role, uint32_t* errorWord)
+{
+  const uint32_t n = min(*countIn, nInt);
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warpBase = (blockIdx.x * kThreads + threadIdx.x) & ~31u;
+  for (uint32_t b0 = warpBase; b0 < n; b0 += gridDim.x * kThreads)
+  {
+    const uint32_t f = b0 + lane;
+    uint32_t next[4] = {0u, 0u, 0u, 0u};
+    int cnt = 0;
+    if (f < n)
+    {
+      const uint32_t j = frontIn[f];
+      const SegTree t = seg_tree(b, bc::find_segment(b.intOffsets, b.G, j));
+      uint32_t cand[4];
+      const int nc = collapse_slots(t.lr, t.lrCount, t.L, kCollapseLargestFirst, j - t.intBase, cand);
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+      {
+        if (k >= nc) break;
+        const uint32_t c = cand[k];
+        if (c + 1u >= t.L) continue;
+        const bool m = merges(t.lr, t.runStarts, t.L, t.nTris, b.mergeMode, c);
+        role[t.intBase + c] = m ? 2 : 1;
+        if (!m)
+        {
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            if (q == cnt) next[q] = t.intBase + c;
+          cnt++;
+        }
+      }
+    }
+    warp_append(next, cnt, frontOut, countOut, nInt, errorWord);
   }
 }
 
@@ -541,7 +772,7 @@ __global__ void __launch_bounds__(kThreads) k_seg4_emit(Bvh4Batch b, uint32_t nI
     Slot slot[4];
     const uint8_t* roleSeg = role + t.intBase;
     const uint32_t* rankSeg = rank + t.intBase;
-    const int ns = node4_slots(t.lr, t.runStarts, t.L, t.nTris, roleSeg,
+    const int ns = node4_slots(t.lr, t.lrCount, t.runStarts, t.L, t.nTris, b.collapse, roleSeg,
                                [&](uint32_t c) { return rankSeg[c] - r0; }, i, t.tris, slot);
     write_node4(format, nodes, outIdx, slot, ns, errorWord);
   }
@@ -555,69 +786,124 @@ inline uint32_t grid_for(uint64_t n, int numSMs)
   return g == 0 ? 1u : (uint32_t)g;
 }
 
+// Blocks for level `lvl` of the largest-first roles: the level holds at most
+// roots * 4^lvl entries (and never more than the internal nodes); the loop
+// strides over larger levels, so two blocks per SM suffice.
+inline uint32_t level_grid(int lvl, uint64_t roots, uint64_t nInternal, int numSMs)
+{
+  uint64_t most = roots;
+  for (int k = 0; k < lvl && most < nInternal; k++) most *= 4;
+  if (most > nInternal) most = nInternal;
+  uint64_t g = (most + kThreads - 1) / kThreads;
+  const uint64_t cap = (uint64_t)numSMs * 2;
+  if (g > cap) g = cap;
+  return g == 0 ? 1u : (uint32_t)g;
+}
+
 }  // namespace
 
+// Scratch: total (256 B), depth and role (N B each), index (4N B; also the
+// first frontier of the largest-first roles), scan tile status, the second
+// frontier (4N B) and the level counts.
 size_t bvh4_scratch_bytes(uint32_t nTris)
 {
   const size_t n = nTris ? nTris : 1;
   const size_t tiles = (n + kScanTile - 1) / kScanTile;
-  return 256 + ((2 * n + 255) / 256) * 256 + ((4 * n + 255) / 256) * 256 + 4 * (tiles + 8);
+  return 256 + ((2 * n + 255) / 256) * 256 + ((4 * n + 255) / 256) * 256 + ((4 * (tiles + 8) + 255) / 256) * 256 +
+         ((4 * n + 255) / 256) * 256 + 4 * (kCollapseLevels + 1);
 }
+
+namespace
+{
+struct SingleScratch
+{
+  uint32_t *total, *index, *tiles, *front2, *levelCounts;
+  uint8_t *depth, *role;
+};
+SingleScratch single_scratch(void* scratch, uint32_t N)
+{
+  const size_t n = N ? N : 1;
+  const size_t tiles = (n + kScanTile - 1) / kScanTile;
+  char* p = (char*)scratch;
+  SingleScratch q;
+  q.total = (uint32_t*)p;
+  q.depth = (uint8_t*)(p + 256);
+  q.role = q.depth + N;
+  q.index = (uint32_t*)(p + 256 + ((2 * n + 255) / 256) * 256);
+  q.tiles = (uint32_t*)((char*)q.index + ((4 * n + 255) / 256) * 256);
+  q.front2 = (uint32_t*)((char*)q.tiles + ((4 * (tiles + 8) + 255) / 256) * 256);
+  q.levelCounts = (uint32_t*)((char*)q.front2 + ((4 * n + 255) / 256) * 256);
+  return q;
+}
+}  // namespace
 
 cudaError_t bvh4_plan(const Bvh4Buffers& b, int numSMs, cudaStream_t s)
 {
   const uint32_t N = b.nTris;
-  char* p = (char*)b.scratch;
-  uint32_t* total = (uint32_t*)p;
-  uint8_t* depth = (uint8_t*)(p + 256);
-  uint8_t* role = depth + N;
-  uint32_t* index = (uint32_t*)(p + 256 + ((2 * (size_t)N + 255) / 256) * 256);
-  uint32_t* tiles = index + ((4 * (size_t)N + 255) / 256) * 64;
+  const SingleScratch q = single_scratch(b.scratch, N);
   const size_t nTiles = ((size_t)N + kScanTile - 1) / kScanTile;
-  cudaError_t e = cudaMemsetAsync(total, 0, 4, s);
+  cudaError_t e = cudaMemsetAsync(q.total, 0, 4, s);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(tiles, 0, 4 * (nTiles + 8), s);
+  e = cudaMemsetAsync(q.tiles, 0, 4 * (nTiles + 8), s);
   if (e != cudaSuccess) return e;
   const uint32_t g = grid_for(N, numSMs);
-  k_depth<<<g, kThreads, 0, s>>>(b.params, b.parent, depth);
-  k_roles<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, N, depth, b.mergeMode, role);
-  k_scan_roles<<<(uint32_t)(nTiles ? nTiles : 1), kThreads, 0, s>>>(b.params, 0u, role, index, tiles + 4, tiles, total,
-                                                                      &b.params->error);
-  return cudaMemcpyAsync(b.hostNodeCount, total, 4, cudaMemcpyDeviceToHost, s);
+  if (b.collapse == kCollapseLargestFirst)
+  {
+    e = cudaMemsetAsync(q.role, 0, N ? N : 1, s);
+    if (e != cudaSuccess) return e;
+    k_roles_level_init<<<1, 64, 0, s>>>(b.params, q.index, q.levelCounts, kCollapseLevels, q.role);
+    for (int lvl = 0; lvl < kCollapseLevels; lvl++)
+    {
+      uint32_t* in = (lvl & 1) ? q.front2 : q.index;
+      uint32_t* out = (lvl & 1) ? q.index : q.front2;
+      k_roles_level<<<level_grid(lvl, 1, N, numSMs), kThreads, 0, s>>>(
+          b.params, b.lr, b.lrCount, b.runStarts, N, b.mergeMode, in, q.levelCounts + lvl, out,
+          q.levelCounts + lvl + 1, q.role, &b.params->error);
+    }
+    k_roles_level_check<<<1, 1, 0, s>>>(q.levelCounts, kCollapseLevels, &b.params->error);
+  }
+  else
+  {
+    k_depth<<<g, kThreads, 0, s>>>(b.params, b.parent, q.depth);
+    k_roles<<<g, kThreads, 0, s>>>(b.params, b.lr, b.runStarts, N, q.depth, b.mergeMode, q.role);
+  }
+  k_scan_roles<<<(uint32_t)(nTiles ? nTiles : 1), kThreads, 0, s>>>(b.params, 0u, q.role, q.index, q.tiles + 4,
+                                                                      q.tiles, q.total, &b.params->error);
+  return cudaMemcpyAsync(b.hostNodeCount, q.total, 4, cudaMemcpyDeviceToHost, s);
 }
 
 cudaError_t bvh4_emit(const Bvh4Buffers& b, int format, void* nodes, uint32_t maxNodes, int numSMs, cudaStream_t s)
 {
   const uint32_t N = b.nTris;
-  char* p = (char*)b.scratch;
-  uint8_t* depth = (uint8_t*)(p + 256);
-  uint8_t* role = depth + N;
-  uint32_t* index = (uint32_t*)(p + 256 + ((2 * (size_t)N + 255) / 256) * 256);
-  k_emit4<<<grid_for(N, numSMs), kThreads, 0, s>>>(b.params, b.lr, b.runStarts, N, role, index, format, nodes,
-                                                   maxNodes, b.tris, &b.params->error);
+  const SingleScratch q = single_scratch(b.scratch, N);
+  k_emit4<<<grid_for(N, numSMs), kThreads, 0, s>>>(b.params, b.lr, b.lrCount, b.runStarts, N, b.collapse, q.role,
+                                                   q.index, format, nodes, maxNodes, b.tris, &b.params->error);
   return cudaGetLastError();
 }
 
-// Batch scratch: total (256 B), role (nInt B), rank (4 nInt B), per-geometry
-// rootRank, count4, node4Off (4 (3G + 1) B), scan tile status.
+// Batch scratch: total (256 B), role (nInt B), rank (4 nInt B; also the
+// first frontier of the largest-first roles), per-geometry rootRank, count4,
+// node4Off (4 (3G + 1) B), scan tile status, the second frontier (4 nInt B)
+// and the level counts.
 size_t bvh4_batch_scratch_bytes(uint32_t nInt, uint32_t G)
 {
   const size_t n = nInt ? nInt : 1;
   const size_t tiles = (n + kScanTile - 1) / kScanTile;
   return 256 + ((n + 255) / 256) * 256 + ((4 * n + 255) / 256) * 256 + ((4 * (3 * (size_t)G + 1) + 255) / 256) * 256 +
-         4 * (tiles + 8);
+         ((4 * (tiles + 8) + 255) / 256) * 256 + ((4 * n + 255) / 256) * 256 + 4 * (kCollapseLevels + 1);
 }
 
 namespace
 {
 struct BatchScratch
 {
-  uint32_t *total, *rank, *rootRank, *count4, *node4Off, *tiles;
+  uint32_t *total, *rank, *rootRank, *count4, *node4Off, *tiles, *front2, *levelCounts;
   uint8_t* role;
 };
 BatchScratch batch_scratch(void* scratch, uint32_t nInt, uint32_t G)
 {
   const size_t n = nInt ? nInt : 1;
+  const size_t tiles = (n + kScanTile - 1) / kScanTile;
   char* p = (char*)scratch;
   BatchScratch q;
   q.total = (uint32_t*)p;
@@ -627,6 +913,8 @@ BatchScratch batch_scratch(void* scratch, uint32_t nInt, uint32_t G)
   q.count4 = q.rootRank + G;
   q.node4Off = q.count4 + G;
   q.tiles = (uint32_t*)((char*)q.rootRank + ((4 * (3 * (size_t)G + 1) + 255) / 256) * 256);
+  q.front2 = (uint32_t*)((char*)q.tiles + ((4 * (tiles + 8) + 255) / 256) * 256);
+  q.levelCounts = (uint32_t*)((char*)q.front2 + ((4 * n + 255) / 256) * 256);
   return q;
 }
 }  // namespace
@@ -642,7 +930,24 @@ cudaError_t bvh4_plan_batch(const Bvh4Batch& b, uint32_t nInt, void* scratch, ui
   if (e != cudaSuccess) return e;
   if (nInt)
   {
-    k_seg4_depth_roles<<<grid_for(nInt, numSMs), kThreads, 0, s>>>(b, nInt, q.role);
+    if (b.collapse == kCollapseLargestFirst)
+    {
+      e = cudaMemsetAsync(q.role, 0, nInt, s);
+      if (e != cudaSuccess) return e;
+      e = cudaMemsetAsync(q.levelCounts, 0, 4, s);
+      if (e != cudaSuccess) return e;
+      k_seg4_roles_init<<<grid_for(b.G, numSMs), kThreads, 0, s>>>(b, q.rank, q.levelCounts, kCollapseLevels, q.role);
+      for (int lvl = 0; lvl < kCollapseLevels; lvl++)
+      {
+        uint32_t* in = (lvl & 1) ? q.front2 : q.rank;
+        uint32_t* out = (lvl & 1) ? q.rank : q.front2;
+        k_seg4_roles_level<<<level_grid(lvl, b.G, nInt, numSMs), kThreads, 0, s>>>(
+            b, nInt, in, q.levelCounts + lvl, out, q.levelCounts + lvl + 1, q.role, errorWord);
+      }
+      k_roles_level_check<<<1, 1, 0, s>>>(q.levelCounts, kCollapseLevels, errorWord);
+    }
+    else
+      k_seg4_depth_roles<<<grid_for(nInt, numSMs), kThreads, 0, s>>>(b, nInt, q.role);
     k_scan_roles<<<(uint32_t)nTiles, kThreads, 0, s>>>(nullptr, nInt, q.role, q.rank, q.tiles + 4, q.tiles, q.total,
                                                        errorWord);
   }

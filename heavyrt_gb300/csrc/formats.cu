@@ -166,7 +166,9 @@ int hrt_geom_save(const hrt_scene* s, uint32_t geomId, const char* path)
   BlobHeader h;
   std::memcpy(h.magic, kBlobMagic, 8);
   h.layout = (uint32_t)s->layout | ((uint32_t)g.triTest << 8);  // triangle-record form in bits 8..15
-  h.merge = (uint32_t)g.bvh4Merge;
+  // merge bound in bits 0..7, collapse rule in 8..15, Morton frame in 16..23
+  // (what a refit of the restored geometry rebuilds with)
+  h.merge = (uint32_t)g.bvh4Merge | ((uint32_t)g.bvh4Collapse << 8) | ((uint32_t)g.mortonFrame << 16);
   h.nTris = g.nTris;
   h.nVerts = g.nVerts;
   h.nLeaves = g.nLeaves;
@@ -205,7 +207,9 @@ int hrt_geom_load(hrt_scene* s, const char* path, uint32_t* geomId)
   if ((int)h.layout != s->layout) return fail(ctx, HRT_ERR_STATE, "the blob was built for another node layout");
   if (triTest != s->triTest) return fail(ctx, HRT_ERR_STATE, "the blob was built for another triangle test");
   if (h.nTris > HRT_MAX_TRIS_PER_GEOM || h.nLeaves > h.nTris || (h.nTris && !h.nLeaves) ||
-      (h.layout != HRT_LAYOUT_BVH2 && h.nTris && !h.nNodes4))
+      (h.layout != HRT_LAYOUT_BVH2 && h.nTris && !h.nNodes4) || (h.merge & 0xFFu) > 64u ||
+      ((h.merge >> 8) & 0xFFu) > (uint32_t)HRT_BVH4_COLLAPSE_LARGEST_FIRST ||
+      ((h.merge >> 16) & 0xFFu) > (uint32_t)HRT_MORTON_CUBIC || (h.merge >> 24) != 0u)
     return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "inconsistent BVH blob header");
   cudaSetDevice(ctx->device);
   Geom g;
@@ -213,7 +217,9 @@ int hrt_geom_load(hrt_scene* s, const char* path, uint32_t* geomId)
   g.nVerts = h.nVerts;
   g.nLeaves = h.nLeaves;
   g.nNodes4 = h.nNodes4;
-  g.bvh4Merge = (int)h.merge;
+  g.bvh4Merge = (int)(h.merge & 0xFFu);
+  g.bvh4Collapse = (int)((h.merge >> 8) & 0xFFu);
+  g.mortonFrame = (int)((h.merge >> 16) & 0xFFu);
   g.triTest = triTest;
   g.host = h.params;
   for (int c = 0; c < 4; c++)

@@ -235,8 +235,11 @@ int build_geometry(hrt_scene* s, Geom& g, const float* vpos, uint64_t nVert, con
     b4.tris = g.tris;
     b4.scratch = scratch4;
     b4.mergeMode = s->bvh4Merge;
+    b4.lrCount = g.lrCount;
+    b4.collapse = s->bvh4Collapse;
     b4.hostNodeCount = &count4;
     g.bvh4Merge = s->bvh4Merge;
+    g.bvh4Collapse = s->bvh4Collapse;
     HRT_CUDA(ctx, bvh4_plan(b4, ctx->numSMs, st));
     HRT_CUDA(ctx, cudaStreamSynchronize(st));
     if (count4 == 0) count4 = 1;  // a single leaf still gets a root node
@@ -421,7 +424,9 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
     q.intOffsets = b.intOffsets;
     q.nodeOffsets = b.nodeOffsets;
     q.triOffsets = b.triOffsets;
+    q.lrCount = b.lrCount;
     q.mergeMode = s->bvh4Merge;
+    q.collapse = s->bvh4Collapse;
     HRT_CUDA(ctx, cudaMallocAsync(&scratch4, bvh4_batch_scratch_bytes(nInt, G), st));
     uint32_t* hostCounts = nullptr;
     HRT_CUDA(ctx, cudaMallocHost((void**)&hostCounts, sizeof(uint32_t) * (2 * (size_t)G + 1)));
@@ -481,6 +486,7 @@ int build_batch(hrt_scene* s, uint32_t G, const float* vpos, const uint64_t* vOf
     const uint32_t Li = hLeaf[i + 1] - hLeaf[i];
     g.shared = true;
     g.bvh4Merge = s->bvh4Merge;
+    g.bvh4Collapse = s->bvh4Collapse;
     g.triTest = s->triTest;
     g.mortonFrame = s->mortonFrame;
     g.nTris = Ni;
@@ -697,6 +703,8 @@ int refit_geometry(hrt_scene* s, Geom& g, const float* vpos, const uint32_t* idx
     b4.tris = g.tris;
     b4.scratch = scratch4;
     b4.mergeMode = g.bvh4Merge;
+    b4.lrCount = g.lrCount;
+    b4.collapse = g.bvh4Collapse;
     b4.hostNodeCount = &count4;
     HRT_CUDA(ctx, bvh4_plan(b4, ctx->numSMs, st));
     HRT_CUDA(ctx, cudaStreamSynchronize(st));
@@ -1531,6 +1539,11 @@ int hrt_scene_set_option(hrt_scene* s, int option, int value)
         return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown Morton frame");
       s->mortonFrame = value;
       return HRT_OK;
+    case HRT_OPTION_BVH4_COLLAPSE:
+      if (value != HRT_BVH4_COLLAPSE_EVEN_DEPTH && value != HRT_BVH4_COLLAPSE_LARGEST_FIRST)
+        return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown BVH4 collapse rule");
+      s->bvh4Collapse = value;
+      return HRT_OK;
     case HRT_OPTION_TRIANGLE_TEST:
       if (value != HRT_TRI_MOLLER_TRUMBORE && value != HRT_TRI_WATERTIGHT)
         return fail(s->ctx, HRT_ERR_INVALID_ARGUMENT, "unknown triangle test");
@@ -1686,7 +1699,7 @@ int hrt_scene_autotune(hrt_scene* s, const hrt_query_desc* q, int repeats, hrt_t
     c.persistent = 0;
     grid.push_back(c);
     for (int steps : {4, 8, 16, 32, 64})
-      for (int lanes : {8, 16, 24, 28, 32})
+      for (int lanes : {2, 4, 8, 16, 24, 28, 32})
       {
         c.persistent = 1;
         c.stepsPerRefill = steps;

@@ -50,6 +50,7 @@ struct Geom
   uint32_t     nNodes4 = 0;
   bool         shared = false;    // arrays point into a batch allocation (hrt_add_geoms_triangles3f_batched)
   int          bvh4Merge = 0;     // leaf merge bound the 4-wide nodes were built with
+  int          bvh4Collapse = 0;  // HRT_BVH4_COLLAPSE_* the 4-wide nodes were built with (a refit keeps it)
   int          triTest = 0;       // triangle records for HRT_TRI_* (1: vertices, for the watertight test)
   int          mortonFrame = 0;   // HRT_MORTON_* the tree was built in (a refit keeps it)
 };
@@ -78,6 +79,7 @@ struct hrt_scene
   bool                  committed = false;
   int                   layout = HRT_LAYOUT_BVH2;
   int                   bvh4Merge = 0;  // HRT_OPTION_BVH4_MERGE
+  int                   bvh4Collapse = 0;  // HRT_OPTION_BVH4_COLLAPSE
   int                   useTlas = 1;    // HRT_OPTION_TLAS
   int                   triTest = 0;    // HRT_OPTION_TRIANGLE_TEST
   int                   mortonFrame = 0;  // HRT_OPTION_MORTON_FRAME

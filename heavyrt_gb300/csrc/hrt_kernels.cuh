@@ -128,7 +128,9 @@ struct Bvh4Buffers
   const uint32_t*  runStarts;       // L
   const uint32_t*  parent;          // 2L-1
   TriRec*          tris;            // N; bit 1 of a.w marks 4-wide leaf ends
+  const uint32_t*  lrCount;         // 2L-1 descendant node counts (the largest-first collapse opens by them)
   int              mergeMode;       // 0: merge two leaf children (reference rule); M > 0: merge subtrees of <= M triangles
+  int              collapse;        // HRT_BVH4_COLLAPSE_*
   void*            scratch;         // bvh4_scratch_bytes(nTris)
   uint32_t*        hostNodeCount;   // host word receiving the node count (0 when L == 1)
 };
@@ -158,7 +160,9 @@ struct Bvh4Batch
   const uint32_t*  intOffsets;
   const uint32_t*  nodeOffsets;
   const uint32_t*  triOffsets;
+  const uint32_t*  lrCount;  // indexed like lr
   int              mergeMode;
+  int              collapse;  // HRT_BVH4_COLLAPSE_*
 };
 size_t bvh4_batch_scratch_bytes(uint32_t nInt, uint32_t G);
 cudaError_t bvh4_plan_batch(const Bvh4Batch& b, uint32_t nInt, void* scratch, uint32_t* hostCount4,

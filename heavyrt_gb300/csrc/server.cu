@@ -502,7 +502,8 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
   if (c.maxBatchRequests == 0) c.maxBatchRequests = 1024;
   if (c.maxScenes > (1u << kSlotBits) || c.slots > 16 || c.slotRays > 0xFFFFFFFFull ||
       c.layout < HRT_LAYOUT_BVH2 || c.layout > HRT_LAYOUT_BVH4_Q8 || c.bvh4Merge < 0 || c.bvh4Merge > 64 ||
-      (c.mortonFrame != HRT_MORTON_PER_AXIS && c.mortonFrame != HRT_MORTON_CUBIC))
+      (c.mortonFrame != HRT_MORTON_PER_AXIS && c.mortonFrame != HRT_MORTON_CUBIC) ||
+      (c.bvh4Collapse != HRT_BVH4_COLLAPSE_EVEN_DEPTH && c.bvh4Collapse != HRT_BVH4_COLLAPSE_LARGEST_FIRST))
     return fail(ctx, HRT_ERR_INVALID_ARGUMENT, "server configuration out of range");
   const uint64_t staging = (uint64_t)c.slots * slot_bytes(c);
   if (staging + sizeof(InstanceDesc) * (uint64_t)c.maxScenes > c.memoryBudget)
@@ -517,6 +518,7 @@ int hrt_server_create(hrt_context* ctx, const hrt_server_config* config, hrt_ser
   S->proto.layout = c.layout;
   S->proto.bvh4Merge = c.bvh4Merge;
   S->proto.mortonFrame = c.mortonFrame;
+  S->proto.bvh4Collapse = c.bvh4Collapse;
   for (int k = 0; k < 2; k++)
   {
     S->trace[k].threadsPerBlock = 256;  // segmented batches: fastest shape of the batched-scene sweep

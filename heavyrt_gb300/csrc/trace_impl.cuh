@@ -287,7 +287,7 @@ __device__ __forceinline__ bool leaf_test(const TriRec* __restrict__ tris, uint3
     const float qy = __fsub_rn(__fmul_rn(tz, e1.x), __fmul_rn(tx, e1.z));
     const float qz = __fsub_rn(__fmul_rn(tx, e1.y), __fmul_rn(ty, e1.x));
     const float det = __fadd_rn(__fadd_rn(__fmul_rn(e1.x, px), __fmul_rn(e1.y, py)), __fmul_rn(e1.z, pz));
-    const float invDet = __fdiv_rn(1.0f, det);
+    const float invDet = __frcp_rn(det);  // correctly rounded: the value of 1.0f / det
     const float v = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(tx, px), __fmul_rn(ty, py)), __fmul_rn(tz, pz)), invDet);
     const float u = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(qx, r.dx), __fmul_rn(qy, r.dy)), __fmul_rn(qz, r.dz)), invDet);
     const float t = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(e2.x, qx), __fmul_rn(e2.y, qy)), __fmul_rn(e2.z, qz)), invDet);
@@ -359,7 +359,7 @@ __device__ __forceinline__ bool leaf_test_wt(const TriRec* __restrict__ tris, ui
     {
       const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, __fmul_rn(w.sz, az)), __fmul_rn(V, __fmul_rn(w.sz, bz))),
                                 __fmul_rn(W, __fmul_rn(w.sz, cz)));
-      const float inv = __fdiv_rn(1.0f, det);
+      const float inv = __frcp_rn(det);
       const float t = __fmul_rn(T, inv);
       if (t > r.tNear && t < h.t)
       {

@@ -46,7 +46,9 @@ EXPORT_PAIR_RECORDS = 10
 # node layouts (include/hrt.h); names accepted as CreateSceneRT's a_layoutName
 LAYOUT_BVH2, LAYOUT_BVH4_F32, LAYOUT_BVH4_F16, LAYOUT_BVH4_Q8 = 0, 1, 2, 3
 OPTION_BVH4_MERGE, OPTION_TLAS, OPTION_TRIANGLE_TEST, OPTION_L2_PERSIST, OPTION_MORTON_FRAME = 1, 2, 3, 4, 5
+OPTION_BVH4_COLLAPSE = 6
 MORTON_PER_AXIS, MORTON_CUBIC = 0, 1
+BVH4_COLLAPSE_EVEN_DEPTH, BVH4_COLLAPSE_LARGEST_FIRST = 0, 1
 TRI_MOLLER_TRUMBORE, TRI_WATERTIGHT = 0, 1
 TRI_TEST_NAMES = {"mt": TRI_MOLLER_TRUMBORE, "moller_trumbore": TRI_MOLLER_TRUMBORE, "watertight": TRI_WATERTIGHT}
 LAYOUT_NAMES = {"": LAYOUT_BVH2, "bvh2": LAYOUT_BVH2, "bvh4": LAYOUT_BVH4_F32, "bvh4_f32": LAYOUT_BVH4_F32,
@@ -100,7 +102,7 @@ class ServerConfig(C.Structure):
 
     _fields_ = [("memoryBudget", C.c_uint64), ("slotRays", C.c_uint64), ("slots", C.c_uint32),
                 ("maxScenes", C.c_uint32), ("maxBatchRequests", C.c_uint32), ("layout", C.c_int),
-                ("bvh4Merge", C.c_int), ("mortonFrame", C.c_int)]
+                ("bvh4Merge", C.c_int), ("mortonFrame", C.c_int), ("bvh4Collapse", C.c_int)]
 
 
 class RequestInfo(C.Structure):
@@ -343,6 +345,11 @@ class SceneRT:
         """MORTON_PER_AXIS (the reference's grid) or MORTON_CUBIC, for geometry added afterwards."""
         self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_MORTON_FRAME, int(frame)), "set_option")
 
+    def set_bvh4_collapse(self, rule: int):
+        """BVH4_COLLAPSE_EVEN_DEPTH (the reference's BVH2ToBVH4 rule) or
+        BVH4_COLLAPSE_LARGEST_FIRST, for geometry added afterwards."""
+        self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_BVH4_COLLAPSE, int(rule)), "set_option")
+
     def set_triangle_test(self, test: int):
         """TRI_MOLLER_TRUMBORE (the reference's test) or TRI_WATERTIGHT; before the first geometry."""
         self.ctx.check(lib().hrt_scene_set_option(self._h, OPTION_TRIANGLE_TEST, int(test)), "set_option")
@@ -577,12 +584,12 @@ class Server:
 
     def __init__(self, ctx: Context | None = None, memory_budget: int = 0, slot_rays: int = 0, slots: int = 0,
                  max_scenes: int = 0, max_batch_requests: int = 0, layout=LAYOUT_BVH2, bvh4_merge: int = 0,
-                 morton_frame: int = MORTON_PER_AXIS):
+                 morton_frame: int = MORTON_PER_AXIS, bvh4_collapse: int = BVH4_COLLAPSE_EVEN_DEPTH):
         self.ctx = ctx or default_context()
         if isinstance(layout, str):
             layout = LAYOUT_NAMES[layout.lower()]
         cfg = ServerConfig(memory_budget, slot_rays, slots, max_scenes, max_batch_requests, int(layout),
-                           int(bvh4_merge), int(morton_frame))
+                           int(bvh4_merge), int(morton_frame), int(bvh4_collapse))
         self._h = C.c_void_p()
         self.ctx.check(lib().hrt_server_create(self.ctx.handle, C.byref(cfg), C.byref(self._h)), "hrt_server_create")
 

@@ -172,6 +172,25 @@ int hrt_scene_get_layout(const hrt_scene* scene, int* layout);
 #define HRT_OPTION_MORTON_FRAME 5
 #define HRT_MORTON_PER_AXIS     0
 #define HRT_MORTON_CUBIC        1
+/*   HRT_OPTION_BVH4_COLLAPSE  which binary nodes a 4-wide node of geometry
+ *                          added afterwards takes as its (up to) four slots:
+ *     HRT_BVH4_COLLAPSE_EVEN_DEPTH  (default) BVH2ToBVH4's rule
+ *                          (core/builders/cbvh.cpp:226-311): the grandchildren,
+ *                          so the 4-wide nodes are the binary nodes at even
+ *                          depth;
+ *     HRT_BVH4_COLLAPSE_LARGEST_FIRST  start from the two children and twice
+ *                          open the internal slot with the most leaves under
+ *                          it (the leftmost of equals) into its two children,
+ *                          so big subtrees descend faster and small ones are
+ *                          not split early.  It depends on the tree's shape
+ *                          alone, so a refit keeps it.  The merge option
+ *                          applies to the internal slots left after the
+ *                          openings.  Another 4-wide tree over the same
+ *                          binary tree: hits equal the reference's except at
+ *                          ties within 1e-5 relative t. */
+#define HRT_OPTION_BVH4_COLLAPSE          6
+#define HRT_BVH4_COLLAPSE_EVEN_DEPTH      0
+#define HRT_BVH4_COLLAPSE_LARGEST_FIRST   1
 int hrt_scene_set_option(hrt_scene* scene, int option, int value);
 
 /* ISceneObject::ClearGeom (core/CrossRT.h:82): drops every geometry and instance. */
@@ -345,7 +364,7 @@ int hrt_graph_destroy(hrt_graph* graph);
 /* Launch-shape autotuner: times `query` (repeats timed runs after one
  * warm-up) under every trace configuration of a fixed grid (64/128/256
  * threads; one ray per thread, or the persistent pool with 4..64 steps per
- * refill and 8..32 idle lanes to refill), then the best of those with 16, 24,
+ * refill and 2..32 idle lanes to refill), then the best of those with 16, 24,
  * 32, 48 and 64 shared-memory stack entries; sets the fastest as the scene's
  * configuration for query->kind, and returns it with its mean time in ms.
  * Synchronous; overwrites query->out (with identical results). */
@@ -383,6 +402,7 @@ typedef struct hrt_server_config
   int      layout;           /* HRT_LAYOUT_* of every scene                                */
   int      bvh4Merge;        /* HRT_OPTION_BVH4_MERGE value for 4-wide layouts             */
   int      mortonFrame;      /* HRT_MORTON_* grid of every scene's build                   */
+  int      bvh4Collapse;     /* HRT_BVH4_COLLAPSE_* rule of every scene's 4-wide nodes     */
 } hrt_server_config;
 
 /* Result of one request; times in seconds since the server was created. */

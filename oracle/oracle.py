@@ -152,6 +152,126 @@ class OracleBVH:
             pass
 
 
+# ---------------------------------------------------------------- 4-wide collapse
+
+LEAF_BIT, EMPTY_REF = 0x80000000, 0xFFFFFFFF
+COLLAPSE_EVEN_DEPTH, COLLAPSE_LARGEST_FIRST = 0, 1
+
+
+def collapse4(lr: np.ndarray, counts: np.ndarray, run_starts: np.ndarray, n_tris: int, merge: int = 0,
+              rule: int = COLLAPSE_EVEN_DEPTH) -> np.ndarray:
+    """The 4-wide nodes of a binary LBVH (lr_nodes / lr_counts / run_starts of
+    this module's OracleBVH) as uint32 [n, 32] FP32 node records: lo x, y, z,
+    hi x, y, z (four floats each, one per slot), the four slot refs, padding.
+
+    rule COLLAPSE_EVEN_DEPTH is BVH2ToBVH4 (core/builders/cbvh.cpp:226-311): a
+    4-wide node's slots are its binary node's grandchildren (a leaf child
+    stands for itself), so the 4-wide nodes are the internal nodes at even
+    depth.  COLLAPSE_LARGEST_FIRST starts from the two children and twice
+    opens the internal slot with the largest descendant count (the leftmost
+    of equals).  merge 0: an internal slot whose two children are leaves
+    becomes one leaf; M > 0: a slot over at most M triangles does (1 never).
+    A leaf slot refers to its first sorted triangle (LEAF_BIT set), an internal
+    slot to the 4-wide node it becomes, numbered in binary-node order; unused
+    slots are EMPTY_REF with zero boxes.  Pure Python: small trees only."""
+    L = len(run_starts)
+    left = lr["leftOffset"].astype(np.int64)
+    right = lr["escapeIndex"].astype(np.int64)
+    bmin, bmax = lr["boxMin"], lr["boxMax"]
+
+    def is_leaf(n):
+        return n >= L - 1
+
+    def tri_range(n):
+        a = b = n
+        while not is_leaf(a):
+            a = left[a]
+        while not is_leaf(b):
+            b = right[b]
+        la, lb = a - (L - 1), b - (L - 1)
+        return int(run_starts[la]), int(run_starts[lb + 1]) if lb + 1 < L else n_tris
+
+    def merges(n):
+        if n == 0:
+            return False
+        if merge == 0:
+            return is_leaf(left[n]) and is_leaf(right[n])
+        if merge == 1:
+            return False
+        st, en = tri_range(n)
+        return en - st <= merge
+
+    def slots(n):
+        if rule == COLLAPSE_EVEN_DEPTH:
+            out = []
+            for c in (left[n], right[n]):
+                out += [c] if is_leaf(c) else [left[c], right[c]]
+            return out
+        out = [left[n], right[n]]
+        for _ in range(2):
+            best = None
+            for k, c in enumerate(out):
+                if not is_leaf(c) and (best is None or counts[c] > counts[out[best]]):
+                    best = k
+            if best is None:
+                break
+            c = out[best]
+            out[best:best + 1] = [left[c], right[c]]
+        return out
+
+    def record(sl, index, role):
+        w = np.zeros(32, np.uint32)
+        box = np.zeros((6, 4), np.float32)
+        refs = [EMPTY_REF] * 4
+        for k, c in enumerate(sl):
+            box[0:3, k] = bmin[c]
+            box[3:6, k] = bmax[c]
+            if is_leaf(c):
+                refs[k] = LEAF_BIT | int(run_starts[c - (L - 1)])
+            elif role[c] == 2:
+                refs[k] = LEAF_BIT | tri_range(c)[0]
+            else:
+                refs[k] = int(index[c])
+        w[0:24] = box.reshape(-1).view(np.uint32)
+        w[24:28] = refs
+        return w
+
+    if L == 1:
+        w = np.zeros(32, np.uint32)
+        box = np.zeros((6, 4), np.float32)
+        box[0:3, 0], box[3:6, 0] = bmin[0], bmax[0]
+        w[0:24] = box.reshape(-1).view(np.uint32)
+        w[24:28] = [LEAF_BIT | int(run_starts[0]), EMPTY_REF, EMPTY_REF, EMPTY_REF]
+        return w.reshape(1, 32)
+    role = np.zeros(L - 1, np.uint8)
+    if rule == COLLAPSE_EVEN_DEPTH:
+        depth = np.zeros(L - 1, np.int64)
+        stack = [(0, 0)]  # internal nodes are not stored parent first: walk down from the root
+        while stack:
+            n, d = stack.pop()
+            depth[n] = d
+            for c in (left[n], right[n]):
+                if not is_leaf(c):
+                    stack.append((c, d + 1))
+        for n in range(L - 1):
+            if depth[n] % 2 == 0:
+                role[n] = 2 if merges(n) else 1
+    else:
+        role[0] = 1
+        frontier = [0]
+        while frontier:
+            nxt = []
+            for b in frontier:
+                for c in slots(b):
+                    if not is_leaf(c):
+                        role[c] = 2 if merges(c) else 1
+                        if role[c] == 1:
+                            nxt.append(c)
+            frontier = nxt
+    index = np.cumsum(role == 1) - (role == 1)
+    return np.stack([record(slots(n), index, role) for n in range(L - 1) if role[n] == 1])
+
+
 # ---------------------------------------------------------------- reference checker
 
 def eye_rays(proj_inv: np.ndarray, world_view_inv: np.ndarray, width: int, height: int, t_near: float = 0.0,

@@ -1,0 +1,170 @@
+"""The two 4-wide collapse rules (HRT_OPTION_BVH4_COLLAPSE): the engine's
+4-wide nodes equal the restatement oracle/oracle.py collapse4 applied to the
+oracle's own binary tree, word for word (FP32 layout; the quantised layouts'
+slot references), for every merge mode; hits of both rules against the oracle
+(hit/miss and any-hit exact, another triangle only at a tie within 1e-5
+relative t); segmented batches, refits and blobs keep the rule."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+MISS = 0xFFFFFFFF
+RULES = [0, 1]  # even depth (the reference's), largest first
+
+
+def _scene(v, idx, layout, merge, rule, instance=True):
+    from heavyrt_gb300 import SceneRT
+
+    s = SceneRT(layout=layout)
+    s.set_bvh4_merge(merge)
+    s.set_bvh4_collapse(rule)
+    gid = s.AddGeom_Triangles3f(v, v.shape[0], idx, idx.size, vByteStride=16)
+    if instance:
+        s.AddInstance(gid)
+        s.CommitScene()
+    return s, gid
+
+
+def _u32(h):
+    return np.ascontiguousarray(h).view(np.uint32).reshape(-1, 8)
+
+
+def _within_tolerance(got, want, err=""):
+    g, w = _u32(got), _u32(want)
+    np.testing.assert_array_equal(g[:, 3] != MISS, w[:, 3] != MISS, err_msg=err)
+    same = g[:, 1] == w[:, 1]
+    np.testing.assert_array_equal(g[same], w[same], err_msg=err)
+    tg = g[~same, 0].view(np.float32).astype(np.float64)
+    tw = w[~same, 0].view(np.float32).astype(np.float64)
+    assert np.all(np.abs(tg - tw) <= 1e-5 * np.abs(tw)), err
+    assert np.count_nonzero(~same) <= max(2, g.shape[0] // 100000), err
+
+
+def _meshes():
+    from heavyrt_gb300 import workload as wl
+
+    g = dict(np.load(GOLDEN / "golden_duplicates40x5.npz"))
+    hv, hidx, _ = wl.heightfield(21, 64, 48)
+    sv, sidx = wl.soup(22, 5000, -1.0, 1.0, 0.03)
+    out = [("duplicates", g["verts"], g["idx"]), ("heightfield64", hv, hidx), ("soup5000", sv, sidx)]
+    for n in (1, 2, 3, 5):
+        out.append((f"soup{n}", sv, sidx[: 3 * n]))
+    return out
+
+
+@pytest.mark.parametrize("merge", [0, 1, 4])
+def test_nodes_equal_the_restatement(native, merge):
+    from heavyrt_gb300 import engine as E
+    from oracle import oracle as orc
+
+    for name, v, idx in _meshes():
+        o = orc.OracleBVH(v, idx)
+        for rule in RULES:
+            want = orc.collapse4(o.lr_nodes(), o.lr_counts(), o.run_starts(), o.n_tris, merge, rule)
+            s, gid = _scene(v, idx, "bvh4", merge, rule, instance=False)
+            got = s.export(gid, E.EXPORT_NODES4).view(np.uint32).reshape(-1, 32)
+            np.testing.assert_array_equal(got, want, err_msg=f"{name} merge {merge} rule {rule}")
+            s.close()
+            for layout in ("bvh4_f16", "bvh4_q8"):  # same structure, quantised boxes
+                s, gid = _scene(v, idx, layout, merge, rule, instance=False)
+                got = s.export(gid, E.EXPORT_NODES4).view(np.uint32).reshape(-1, 16)
+                np.testing.assert_array_equal(got[:, 12:16], want[:, 24:28], err_msg=f"{name} {layout}")
+                s.close()
+        o.close()
+
+
+def test_hits_of_both_rules_vs_oracle(native):
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    hv, hidx, _ = wl.heightfield(31, 256, 256)
+    sv, sidx = wl.soup(32, 30000, -1.0, 1.0, 0.03)
+    cases = [("heightfield256", hv, hidx,
+              np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 240, 135),
+                              wl.rays_at_triangles(3, hv, hidx, 20000, jitter=0.01)])),
+             ("soup30000", sv, sidx,
+              np.concatenate([wl.rays_at_triangles(4, sv, sidx, 20000, jitter=0.02), wl.sphere_rays(5, 5000)]))]
+    for name, v, idx, rays in cases:
+        o = orc.OracleBVH(v, idx)
+        want, want_any = o.trace(rays), o.trace(rays, any_hit=True)
+        for rule in RULES:
+            for layout in ("bvh4", "bvh4_f16", "bvh4_q8"):
+                for merge in (0, 1):
+                    s, _ = _scene(v, idx, layout, merge, rule)
+                    _within_tolerance(s.RayQuery_NearestHit(rays), want, f"{name} {layout} rule {rule}")
+                    np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), want_any, err_msg=f"{name} {layout}")
+                    s.close()
+        o.close()
+
+
+def test_largest_first_fetches_fewer_nodes(native):
+    """On the heightfield, the largest-first nodes are fetched less often than
+    the even-depth ones by nearest and any-hit rays alike."""
+    import torch
+
+    from heavyrt_gb300 import workload as wl
+
+    v, idx, _ = wl.heightfield(5, 256, 256)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 128, 72),
+                           wl.rays_at_triangles(4, v, idx, 5000, jitter=0.01)])
+    dr = torch.from_numpy(rays).cuda()
+    fetched = {}
+    for rule in RULES:
+        s, _ = _scene(v, idx, "bvh4_f16", 1, rule)
+        fetched[rule] = [s.query_counters(kind, dr.data_ptr(), rays.shape[0])[0] for kind in (0, 1)]
+        s.close()
+    assert fetched[1][0] < fetched[0][0] and fetched[1][1] < fetched[0][1], fetched
+
+
+def test_batch_refit_and_blob_keep_the_rule(native, tmp_path):
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    scenes = [wl.soup(800 + k, n, off=0.03) for k, n in enumerate((3000, 700, 1, 2))]
+    for merge in (0, 1):
+        s = SceneRT(layout="bvh4")
+        s.set_bvh4_merge(merge)
+        s.set_bvh4_collapse(E.BVH4_COLLAPSE_LARGEST_FIRST)
+        ids = s.add_geoms_batched([v for v, _ in scenes], [i for _, i in scenes])
+        for gid, (v, i) in zip(ids, scenes):
+            o = orc.OracleBVH(v, i)
+            want = orc.collapse4(o.lr_nodes(), o.lr_counts(), o.run_starts(), o.n_tris, merge, 1)
+            got = s.export(gid, E.EXPORT_NODES4).view(np.uint32).reshape(-1, 32)
+            np.testing.assert_array_equal(got, want, err_msg=f"batch merge {merge} geometry {gid}")
+            o.close()
+        s.close()
+
+    # refit: the same rule over the moved boxes (topology and leaf counts unchanged)
+    v, i = scenes[0]
+    moved = v.copy()
+    moved[:, :3] += np.random.default_rng(3).uniform(-0.01, 0.01, (v.shape[0], 3)).astype(np.float32)
+    s, gid = _scene(v, i, "bvh4", 0, 1)
+    s.UpdateGeom_Triangles3f(gid, moved, moved.shape[0], i, i.size, E.BUILD_REFIT, 16)
+    s.CommitScene()
+    lr = s.export(gid, E.EXPORT_LR_NODES).view(orc.NODE_DTYPE)
+    want = orc.collapse4(lr, s.export(gid, E.EXPORT_LR_COUNTS), s.export(gid, E.EXPORT_RUN_STARTS), i.size // 3, 0, 1)
+    np.testing.assert_array_equal(s.export(gid, E.EXPORT_NODES4).view(np.uint32).reshape(-1, 32), want)
+
+    # blob: a restored geometry refits with the rule (and frame) it was built with
+    path = tmp_path / "lf.blob"
+    s.save_geom(gid, path)
+    r = SceneRT(layout="bvh4")
+    gid2 = r.load_geom(path)
+    back = moved.copy()
+    back[:, :3] -= 0.002
+    for sc, g in ((s, gid), (r, gid2)):
+        sc.UpdateGeom_Triangles3f(g, back, back.shape[0], i, i.size, E.BUILD_REFIT, 16)
+    np.testing.assert_array_equal(r.export(gid2, E.EXPORT_NODES4), s.export(gid, E.EXPORT_NODES4))
+    s.close()
+    r.close()
+
+    # the option's values
+    t = SceneRT(layout="bvh4")
+    with pytest.raises(E.HrtError):
+        t.set_bvh4_collapse(2)
+    t.close()

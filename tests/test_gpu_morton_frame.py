@@ -102,9 +102,10 @@ def test_cubic_frame_build_and_hits_vs_oracle(native):
             s.close()
 
 
-def test_cubic_frame_batch_refit_and_default(native):
+def test_cubic_frame_batch_refit_and_default(native, tmp_path):
     """Segmented builds keep the frame per geometry (equal to single builds),
-    a refit keeps the build's frame, and the default frame is the reference's."""
+    a refit keeps the build's frame (also after a blob round trip), and the
+    default frame is the reference's."""
     import torch
 
     from heavyrt_gb300 import SceneRT
@@ -146,6 +147,16 @@ def test_cubic_frame_batch_refit_and_default(native):
     assert np.all(np.abs(tg - tw) <= 1e-5 * np.abs(tw))
     assert np.count_nonzero(got[:, 0] != want[:, 0]) <= 2
     np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), fresh.trace(rays, any_hit=True))
+    # a geometry restored from a blob refits on the grid it was built on
+    blob = tmp_path / "cubic.blob"
+    s.save_geom(gid, blob)
+    r = SceneRT()
+    gid2 = r.load_geom(blob)
+    for sc, g in ((s, gid), (r, gid2)):
+        sc.UpdateGeom_Triangles3f(g, v, v.shape[0], i, i.size, E.BUILD_REFIT, 16)
+    np.testing.assert_array_equal(r.export(gid2, E.EXPORT_SCENE_BOX), s.export(gid, E.EXPORT_SCENE_BOX))
+    np.testing.assert_array_equal(r.export(gid2, E.EXPORT_SCENE_BOX).view(np.uint32)[8:11], before)
+    r.close()
     s.close()
 
     d = SceneRT()

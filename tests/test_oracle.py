@@ -283,3 +283,71 @@ def test_oracle_watertight_agrees_with_mt_away_from_edges(host_libs):
         prim = np.where(hm[only], mt["primId"][only], wt["primId"][only])
         b, _ = _bary64(rays[only], v, si[prim])
         assert np.all(np.abs(b).min(axis=1) < 1e-5)
+
+
+def _collapse_walk(nodes, n_tris, run_starts):
+    """Walks 4-wide nodes from node 0: every node reached once, the leaf
+    starts reached, and the deepest 4-wide level."""
+    from oracle import oracle as orc
+
+    seen, starts, depth = set(), [], 0
+    stack = [(0, 1)]
+    while stack:
+        n, d = stack.pop()
+        assert n not in seen
+        seen.add(n)
+        depth = max(depth, d)
+        for ref in nodes[n, 24:28]:
+            ref = int(ref)
+            if ref == orc.EMPTY_REF:
+                continue
+            if ref & orc.LEAF_BIT:
+                starts.append(ref & ~orc.LEAF_BIT)
+            else:
+                stack.append((ref, d + 1))
+    return seen, sorted(starts), depth
+
+
+@pytest.mark.parametrize("merge", [0, 1, 4])
+def test_collapse4_rules_cover_every_run(host_libs, merge):
+    """Both collapse rules of the 4-wide restatement reach every node once and
+    start a leaf at run starts only, every run start once when nothing merges;
+    the even-depth rule's nodes are the internal nodes at even depth; child
+    boxes lie inside the box of their slot in the parent."""
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    hv, hidx, _ = wl.heightfield(5, 40, 30)
+    sv, sidx = wl.soup(6, 3000, off=0.05)
+    for v, idx in ((hv, hidx), (sv, sidx), (sv[:3], sidx[:3]), (sv[:12], sidx[:6])):
+        o = orc.OracleBVH(v, idx)
+        lr, cnt, rs = o.lr_nodes(), o.lr_counts(), o.run_starts()
+        out = {}
+        for rule in (orc.COLLAPSE_EVEN_DEPTH, orc.COLLAPSE_LARGEST_FIRST):
+            nodes = orc.collapse4(lr, cnt, rs, o.n_tris, merge, rule)
+            seen, starts, depth = _collapse_walk(nodes, o.n_tris, rs)
+            assert seen == set(range(len(nodes)))
+            assert set(starts) <= set(int(x) for x in rs) and len(set(starts)) == len(starts)
+            if merge == 1:
+                assert starts == sorted(int(x) for x in rs)
+            # slot boxes of a child node enclose nothing outside the parent's slot box
+            for n in range(len(nodes)):
+                box = nodes[n, 0:24].view(np.float32).reshape(6, 4)
+                for k, ref in enumerate(nodes[n, 24:28]):
+                    ref = int(ref)
+                    if ref == orc.EMPTY_REF or ref & orc.LEAF_BIT:
+                        continue
+                    cb = nodes[ref, 0:24].view(np.float32).reshape(6, 4)
+                    used = nodes[ref, 24:28] != orc.EMPTY_REF
+                    assert np.all(cb[0:3, used] >= box[0:3, k:k + 1]) and np.all(cb[3:6, used] <= box[3:6, k:k + 1])
+            out[rule] = (len(nodes), depth)
+        if o.n_leaves > 1 and merge == 1:
+            left, right = lr["leftOffset"].astype(int), lr["escapeIndex"].astype(int)
+            L = o.n_leaves
+            even, stack = 0, [(0, 0)]
+            while stack:
+                n, d = stack.pop()
+                even += d % 2 == 0
+                stack += [(c, d + 1) for c in (left[n], right[n]) if c < L - 1]
+            assert out[orc.COLLAPSE_EVEN_DEPTH][0] == even
+        o.close()

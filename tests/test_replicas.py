@@ -59,3 +59,56 @@ def test_single_process_defaults(monkeypatch):
     replicas.barrier(r)
     assert replicas.max_over_ranks(r, 4.25) == 4.25
     assert replicas.job_throughput(r, 500.0, 2.0) == pytest.approx(250000.0)
+
+
+def test_partition_covers_in_order():
+    from heavyrt_gb300 import replicas
+
+    for n in (0, 1, 7, 1000, 2073600):
+        for world in (1, 2, 3, 8):
+            for align in (1, 16, 15360):
+                shares = [replicas.partition(n, replicas.Rank(k, world, k), align) for k in range(world)]
+                assert shares[0][0] == 0 and shares[-1][1] == n
+                for (a0, a1), (b0, b1) in zip(shares, shares[1:]):
+                    assert a1 == b0 and a0 <= a1
+                for k, (a0, a1) in enumerate(shares):
+                    assert (a0 % align == 0 or a0 == n) and (a1 % align == 0 or a1 == n)
+                blocks = [-(-(a1 - a0) // align) for a0, a1 in shares]
+                assert max(blocks) - min(blocks) <= 1
+
+
+def _split_main(rank, world, port, out_dir):
+    import numpy as np
+
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "RANK": str(rank),
+                       "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank)})
+    from heavyrt_gb300 import replicas
+
+    r = replicas.from_env()
+    replicas.init(r, "gloo")
+    grp = replicas.host_group(r)
+    n, width = 1003, 17
+    rays = np.arange(n * 8, dtype=np.float32).reshape(n, 8)
+    a0, a1 = replicas.partition(n, r, align=width)
+    # a stand-in for the traced result of each ray: records derived from it
+    hits = (rays[a0:a1, :4].view(np.uint32) ^ np.uint32(0x5A5A5A5A)).copy()
+    flags = (np.arange(a0, a1) % 3 == 0).astype(np.uint8)
+    got = replicas.gather_rows(r, hits, grp)
+    got_flags = replicas.gather_rows(r, flags, grp)
+    if r.leader:
+        want = rays[:, :4].view(np.uint32) ^ np.uint32(0x5A5A5A5A)
+        ok = np.array_equal(got, want) and np.array_equal(got_flags, (np.arange(n) % 3 == 0).astype(np.uint8))
+        (open(os.path.join(out_dir, "split.txt"), "w")).write("ok" if ok else "mismatch")
+    else:
+        assert got is None
+    replicas.finish(r)
+
+
+def test_split_batch_gathers_in_order(tmp_path):
+    """Three gloo ranks each take their share of one ray batch; rank 0 gets
+    every rank's result rows back in ray order."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    mp.start_processes(_split_main, args=(3, _free_port(), str(tmp_path)), nprocs=3, join=True, start_method="spawn")
+    assert (tmp_path / "split.txt").read_text() == "ok"
