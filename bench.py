@@ -392,15 +392,15 @@ def run_batched(ctx, args, tune: bool = True) -> dict:
     if tune and not args.ncu:
         tr = AT.tune_batch(ctx, w.verts, w.idx, d_rays.data_ptr(), n, d_offs.data_ptr(), d_seg.data_ptr(), G,
                            d_hits.data_ptr(), d_any.data_ptr())
-        layout, merge = tr.layout, tr.merge
+        layout, merge, collapse = tr.layout, tr.merge, tr.collapse
     else:
-        tr, layout, merge = None, "bvh4_f16", 1
+        tr, layout, merge, collapse = None, "bvh4_f16", 1, AT.EVEN
 
     # batched build: repeated for timing (GPU time of the whole batch)
     b_ms, b_wall = [], []
     for _ in range(1 if args.ncu else 3):
         t0 = time.perf_counter()
-        scene, ids = AT.build_batch(ctx, w.verts, w.idx, layout, merge)
+        scene, ids = AT.build_batch(ctx, w.verts, w.idx, layout, merge, collapse)
         b_wall.append(time.perf_counter() - t0)
         b_ms.append(scene.geom_info(ids[0])["build_ms"])
         if _ < (0 if args.ncu else 2):
@@ -479,7 +479,9 @@ def run_batched(ctx, args, tune: bool = True) -> dict:
     rays2 = 2 * n  # each ray is traced twice: nearest and any
     out = {
         "workload": w.name, "scenes": G, "tris": w.params["tris"], "rays": n,
-        "structure": {"layout": layout, "bvh4_merge": merge},
+        "structure": {"layout": layout, "bvh4_merge": merge,
+                      "bvh4_collapse": ("largest_first" if collapse == AT.LARGEST else "even_depth")
+                      if layout != "bvh2" else None},
         "launch": tr.configs if tr is not None else None,
         "tuning_table_ms": tr.table if tr is not None else None,
         "batched_mrays_s": round(rays2 / batched_ms / 1e3, 2), "batched_ms": round(batched_ms, 4),
@@ -898,7 +900,11 @@ def run_served(ctx, args, rate: float = None, seconds: float = None) -> dict:
               "requests": count, "rays": int(sizes.sum()), "uploads": int(upload.sum())}
 
     # ---- served
-    srv = E.Server(ctx, memory_budget=150 * 10**9, layout="bvh4_f16", bvh4_merge=1)
+    # the headline's tree options for every scene the server builds
+    srv = E.Server(ctx, memory_budget=150 * 10**9, layout="bvh4_f16", bvh4_merge=1,
+                   morton_frame=E.MORTON_CUBIC if args.morton_frame == "cubic" else E.MORTON_PER_AXIS,
+                   bvh4_collapse=(E.BVH4_COLLAPSE_LARGEST_FIRST if args.bvh4_collapse == "largest_first"
+                                  else E.BVH4_COLLAPSE_EVEN_DEPTH))
     t0 = time.perf_counter()
     ids = [srv.add_scene(v, idx, evictable=False) for v, idx in W["scenes"]]
     for i in ids:
