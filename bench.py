@@ -560,7 +560,9 @@ def run_precision(ctx, args) -> dict:
     decisions), BVH4 with FP32 boxes, FP16 boxes and 8-bit offsets.  Nearest
     hits of the quantised layouts are compared with the FP32-node build (same
     tree) and with the binary tree, any-hit flags with both, and the hit
-    distance with an FP64 evaluation on 1M sampled eye rays per scene."""
+    distance with an FP64 evaluation on 1M sampled eye rays per scene.  All of
+    it twice: with the reference's Moller-Trumbore test, and with the FP32
+    watertight test the configuration names (same rays)."""
     import torch
 
     from heavyrt_gb300 import SceneRT
@@ -572,15 +574,14 @@ def run_precision(ctx, args) -> dict:
     layouts = [("bvh2", None), ("bvh4", 1), ("bvh4_f16", 1), ("bvh4_q8", 1)]
     res = {"note": "mismatch = hit/miss differs or t differs by more than 1e-5 relative (must be 0); tie = another "
                    "triangle at a t within 1e-5 relative (exact = the same t), resolved by visit order", "scenes": {}}
-    for scene_name in ("heightfield", "soup"):
-        w = wl.config2(scene_name, args.width, args.height, args.soup_tris)
-        d_eye = torch.from_numpy(w.eye_rays).cuda()
-        n_eye = len(w.eye_rays)
-        ref_hits = ref_any = ao = d_ao = None
-        out = {}
-        sc_res = {"workload": w.name, "tris": int(w.params["tris"])}
+
+    def trace_layouts(w, d_eye, n_eye, tri_test, ao, d_ao):
+        """Every layout with one triangle test; AO rays from the first
+        (binary) layout's primary hits unless given.  Returns the layouts'
+        entries, the AO rays (host, device) and the binary tree's FP64 t error."""
+        out, ref_hits, ref_any, t_err = {}, None, None, None
         for layout, merge in layouts:
-            sc = SceneRT(ctx, layout=layout)
+            sc = SceneRT(ctx, layout=layout, triangle_test=tri_test)
             if merge is not None:
                 sc.set_bvh4_merge(merge)
             g = sc.AddGeom_Triangles3f(w.verts, len(w.verts), w.idx, w.idx.size, vByteStride=16)
@@ -591,15 +592,15 @@ def run_precision(ctx, args) -> dict:
             sc.query_device(0, d_eye.data_ptr(), n_eye, d_hits.data_ptr(), sh)
             torch.cuda.synchronize()
             hits = d_hits.cpu().numpy().view(np.uint32)
-            if ao is None:
-                # AO rays from the binary FP32 tree's primary hits (same input for every layout)
+            if t_err is None:
                 si = sc.export(g, E.EXPORT_SORTED_INDICES)
-                ao = wl.frame_ao_rays(w, hits.view(np.float32), si)
-                d_ao = torch.from_numpy(ao).cuda()
+                if ao is None:
+                    ao = wl.frame_ao_rays(w, hits.view(np.float32), si)
+                    d_ao = torch.from_numpy(ao).cuda()
                 rng = np.random.default_rng(7)
                 sample = np.sort(rng.choice(n_eye, size=min(1000000, n_eye), replace=False))
-                sc_res["t_error_vs_fp64"] = t_error_fp64(w.eye_rays[sample], hits[sample], w.verts,
-                                                         si.astype(np.uint32), np.zeros(1, np.int64))
+                t_err = t_error_fp64(w.eye_rays[sample], hits[sample], w.verts, si.astype(np.uint32),
+                                     np.zeros(1, np.int64))
             n_ao = len(ao)
             d_any = torch.empty(n_ao, dtype=torch.uint8, device="cuda")
             for _ in range(3):
@@ -647,9 +648,21 @@ def run_precision(ctx, args) -> dict:
         for k in out:
             out[k].pop("_hits")
             out[k].pop("_any")
+        return out, ao, d_ao, t_err
+
+    for scene_name in ("heightfield", "soup"):
+        w = wl.config2(scene_name, args.width, args.height, args.soup_tris)
+        d_eye = torch.from_numpy(w.eye_rays).cuda()
+        n_eye = len(w.eye_rays)
+        sc_res = {"workload": w.name, "tris": int(w.params["tris"])}
+        out, ao, d_ao, t_err = trace_layouts(w, d_eye, n_eye, E.TRI_MOLLER_TRUMBORE, None, None)
+        sc_res["t_error_vs_fp64"] = t_err
         sc_res["eye_rays"] = n_eye
         sc_res["ao_rays"] = int(len(ao))
         sc_res["layouts"] = out
+        wt_out, _, _, wt_err = trace_layouts(w, d_eye, n_eye, E.TRI_WATERTIGHT, ao, d_ao)
+        sc_res["watertight"] = {"t_error_vs_fp64": wt_err, "layouts": wt_out,
+                                "note": "the same rays with the FP32 watertight test in every layout"}
         res["scenes"][scene_name] = sc_res
         del d_eye, d_ao
         torch.cuda.empty_cache()
@@ -1683,6 +1696,11 @@ def summarize(line: dict):
             for lay, e in sc["layouts"].items():
                 cfg[f"c2_{name}_{lay}_mrays_s"] = e["mrays_s"]
                 bad += sum(v for k, v in e.items() if "mismatch" in k)
+            if "watertight" in sc:
+                wt = sc["watertight"]
+                cfg[f"c2_{name}_watertight_t_max_rel_vs_fp64"] = wt["t_error_vs_fp64"]["max_rel"]
+                cfg[f"c2_{name}_watertight_bvh4_f16_mrays_s"] = wt["layouts"]["bvh4_f16"]["mrays_s"]
+                bad += sum(v for e in wt["layouts"].values() for k, v in e.items() if "mismatch" in k)
         cfg["c2_hit_mismatches"] = int(bad)
     if "l2_window" in line:
         for e in line["l2_window"]["sweep"][:-1]:
