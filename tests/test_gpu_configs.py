@@ -226,3 +226,43 @@ def test_config3_all_256_scenes(native):
             _compare_nearest(got[a:b], wk, layout)
             np.testing.assert_array_equal(got_any[a:b], want_any[k], err_msg=f"{layout} scene {k}")
         s.close()
+
+
+def test_config1_full_frame_headline_tree(native):
+    """C1 on the benchmark's tree (cubic Morton grid, largest-first collapse,
+    FP16 nodes, leaf merge 1): every eye ray (nearest) and every AO ray (any)
+    against the oracle's reference tree.  The trees sort the triangles
+    differently, so hits are compared by original triangle index: hit/miss
+    and any-hit exact, another triangle only at a tie within 1e-5 relative t."""
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    w = wl.config1()
+    o = orc.OracleBVH(w.verts, w.idx)
+    want = o.trace(w.eye_rays)
+    ao = wl.frame_ao_rays(w, want, o.sorted_indices())
+    want_any = o.trace(ao, any_hit=True)
+    for layout in ("bvh4_f16", "bvh4"):
+        s = SceneRT(layout=layout)
+        s.set_bvh4_merge(1)
+        s.set_morton_frame(E.MORTON_CUBIC)
+        s.set_bvh4_collapse(E.BVH4_COLLAPSE_LARGEST_FIRST)
+        gid = s.AddGeom_Triangles3f(w.verts, w.verts.shape[0], w.idx, w.idx.size, vByteStride=16)
+        s.AddInstance(gid)
+        s.CommitScene()
+        g = _trace_device(s, 0, w.eye_rays).copy()
+        wv = np.ascontiguousarray(want).view(np.uint32).reshape(-1, 8).copy()
+        hg, hw = g[:, 3] != MISS, wv[:, 3] != MISS
+        np.testing.assert_array_equal(hg, hw, err_msg=layout)
+        g[hg, 1] = s.export(gid, E.EXPORT_PRIM_INDICES)[g[hg, 1]]
+        wv[hw, 1] = o.prim_indices()[wv[hw, 1]]
+        same = g[:, 1] == wv[:, 1]
+        np.testing.assert_array_equal(g[same], wv[same], err_msg=layout)
+        tg = g[~same, 0].view(np.float32).astype(np.float64)
+        tw = wv[~same, 0].view(np.float32).astype(np.float64)
+        assert np.all(np.abs(tg - tw) <= 1e-5 * np.abs(tw)), layout
+        assert np.count_nonzero(~same) <= max(2, g.shape[0] // 100000), layout
+        np.testing.assert_array_equal(_trace_device(s, 1, ao), want_any, err_msg=layout)
+        s.close()

@@ -252,3 +252,27 @@ def test_cubic_morton_frame_scenes(native):
         assert srv.wait(srv.submit_array(ids[k], 1, rays, flags))[0] == 0
         np.testing.assert_array_equal(flags.astype(bool), orc.OracleBVH(v, idx).trace(rays, any_hit=True))
     srv.close()
+
+    # 4-wide scenes on the cubic grid with the largest-first collapse: any-hit
+    # flags are the reference's, nearest hits the oracle's on the same grid
+    # up to ties within 1e-5 relative t
+    srv = E.Server(slot_rays=1 << 18, slots=2, layout="bvh4_f16", bvh4_merge=1, morton_frame=E.MORTON_CUBIC,
+                   bvh4_collapse=E.BVH4_COLLAPSE_LARGEST_FIRST)
+    with pytest.raises(E.HrtError):
+        E.Server(slot_rays=4096, slots=1, bvh4_collapse=5)
+    ids = [srv.add_scene(v, idx, evictable=False) for v, idx in scenes]
+    assert all(srv.scene_state(i, timeout=120) == E.SCENE_READY for i in ids)
+    for k, (v, idx) in enumerate(scenes):
+        rays = np.concatenate([wl.rays_at_triangles(60 + k, v, idx, 3000, jitter=0.03), wl.sphere_rays(k, 1000)])
+        want = orc.OracleBVH(v, idx, cubic=True).trace(rays).view(np.uint32).reshape(-1, 8)
+        out = _out(0, len(rays))
+        assert srv.wait(srv.submit_array(ids[k], 0, rays, out))[0] == 0
+        np.testing.assert_array_equal(out[:, 3] != MISS, want[:, 3] != MISS)
+        same = out[:, 1] == want[:, 1]
+        np.testing.assert_array_equal(out[same, 0], want[same, 0])
+        tg, tw = out[~same, 0].view(np.float32).astype(np.float64), want[~same, 0].view(np.float32).astype(np.float64)
+        assert np.all(np.abs(tg - tw) <= 1e-5 * np.abs(tw)) and np.count_nonzero(~same) <= 2
+        flags = _out(1, len(rays))
+        assert srv.wait(srv.submit_array(ids[k], 1, rays, flags))[0] == 0
+        np.testing.assert_array_equal(flags.astype(bool), orc.OracleBVH(v, idx).trace(rays, any_hit=True))
+    srv.close()
