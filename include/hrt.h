@@ -593,9 +593,11 @@ int hrt_vsgf_write(const char* path, const float* vpos4, uint64_t nVert, const u
 
 /* BVH blobs: every device array of a built geometry in one file, so that a
  * geometry is restored by copies alone, without a build (a warm start for
- * resident scenes).  A blob loads only into a scene of the layout it was
- * built for (HRT_ERR_STATE otherwise); hrt_geom_load appends a geometry and
- * returns its id. */
+ * resident scenes).  A blob loads only into a scene of the layout and
+ * triangle test it was built for (HRT_ERR_STATE otherwise); hrt_geom_load
+ * appends a geometry and returns its id.  The geometry keeps the build
+ * options it was built with (merge bound, collapse rule, Morton frame), so a
+ * later refit rebuilds it the same way whatever the loading scene's options. */
 int hrt_geom_save(const hrt_scene* scene, uint32_t geomId, const char* path);
 int hrt_geom_load(hrt_scene* scene, const char* path, uint32_t* geomId);
 
