@@ -1369,6 +1369,11 @@ def run_engine(args):
     e2e_s = time_steps(e2e_step_sync)
     e2e_value = job_rate(rays_per_step, 1e3 * e2e_s) / 1e6
     e2e_async_value = job_rate(rays_per_step, 1e3 * e2e_async_s) / 1e6
+    # the two calls of the synchronous step timed on their own (wall clock)
+    e2e_eye_s = time_steps(lambda: ctx.check(L.hrt_query_nearest_host(scene._h, C.c_void_p(pin_eye.ptr), n_eye,
+                                                                      C.c_void_p(pin_hits.ptr)), "e2e"))
+    e2e_ao_s = time_steps(lambda: ctx.check(L.hrt_query_any_host(scene._h, C.c_void_p(pin_ao.ptr), n_ao,
+                                                                 C.c_void_p(pin_any.ptr)), "e2e"))
     got_any = pin_any.array(np.uint8)[:n_ao].copy()
 
     # split frame: every rank's results gathered on rank 0 through host
@@ -1578,6 +1583,7 @@ def run_engine(args):
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(RAY_BYTES * (n_eye + n_ao)),
                 "api": "hrt_query_nearest_host + hrt_query_any_host, page-locked arrays",
                 "async_two_streams_value": round(e2e_async_value, 3),
+                "nearest_call_ms": round(1e3 * e2e_eye_s, 4), "any_call_ms": round(1e3 * e2e_ao_s, 4),
                 "d2h_bytes_per_step": int(32 * n_eye + n_ao)},
         "e2e_device_raygen": raygen_e2e,
         "gpu_launches": 2 * args.steps,
