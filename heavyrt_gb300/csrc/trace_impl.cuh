@@ -158,7 +158,7 @@ __device__ __forceinline__ void wt_setup(float dx, float dy, float dz, WtRay& w)
   }
   w.sx = __fdiv_rn(pick3(dx, dy, dz, w.kx), dk);
   w.sy = __fdiv_rn(pick3(dx, dy, dz, w.ky), dk);
-  w.sz = __fdiv_rn(1.0f, dk);
+  w.sz = __frcp_rn(dk);  // correctly rounded: the value of 1.0f / dk
 }
 
 // A ray in the frame of the geometry being traversed.  `w` is the watertight
@@ -177,7 +177,7 @@ struct Ray
 __device__ __forceinline__ float safe_inv(float d)
 {
   const float ooeps = 1.0e-36f;
-  return __fdiv_rn(1.0f, fabsf(d) > ooeps ? d : copysignf(ooeps, d));
+  return __frcp_rn(fabsf(d) > ooeps ? d : copysignf(ooeps, d));  // correctly rounded, as 1.0f / d
 }
 
 // RayBoxIntersection2, core/raytrace_common.h:67-80 (differences, products and
