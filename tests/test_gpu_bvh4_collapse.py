@@ -168,3 +168,64 @@ def test_batch_refit_and_blob_keep_the_rule(native, tmp_path):
     with pytest.raises(E.HrtError):
         t.set_bvh4_collapse(2)
     t.close()
+
+
+def test_tree_options_with_watertight_test_and_instances(native):
+    """The benchmark's tree (cubic grid, largest-first collapse) under the
+    watertight triangle test against the oracle's watertight traversal of
+    the same grid; and transformed instances of such a geometry through the
+    instance tree equal to the instance-by-instance traversal."""
+    from heavyrt_gb300 import SceneRT
+    from heavyrt_gb300 import engine as E
+    from heavyrt_gb300 import workload as wl
+    from oracle import oracle as orc
+
+    hv, hidx, _ = wl.heightfield(41, 128, 96)
+    rays = np.concatenate([wl.camera_rays((0.0, -2.5, 1.5), (0, 0, 0), (0, 0, 1), 60.0, 160, 90),
+                           wl.rays_at_triangles(7, hv, hidx, 10000, jitter=0.01)])
+    oc = orc.OracleBVH(hv, hidx, cubic=True)
+    want = oc.trace(rays, watertight=True)
+    want_any = oc.trace(rays, any_hit=True, watertight=True)
+    for layout in ("bvh4", "bvh4_f16", "bvh4_q8"):
+        s = SceneRT(layout=layout, triangle_test=E.TRI_WATERTIGHT)
+        s.set_bvh4_merge(1)
+        s.set_morton_frame(E.MORTON_CUBIC)
+        s.set_bvh4_collapse(E.BVH4_COLLAPSE_LARGEST_FIRST)
+        gid = s.AddGeom_Triangles3f(hv, hv.shape[0], hidx, hidx.size, vByteStride=16)
+        s.AddInstance(gid)
+        s.CommitScene()
+        _within_tolerance(s.RayQuery_NearestHit(rays), want, f"watertight {layout}")
+        np.testing.assert_array_equal(s.RayQuery_AnyHit(rays), want_any, err_msg=layout)
+        s.close()
+    oc.close()
+
+    v, idx = wl.soup(43, 3000, off=0.05)
+    rng = np.random.default_rng(8)
+    mats = []
+    for _ in range(6):
+        m = np.eye(4, dtype=np.float32)
+        a = rng.uniform(0, 2 * np.pi)
+        m[:2, :2] = [[np.cos(a), -np.sin(a)], [np.sin(a), np.cos(a)]]
+        m[:3, :3] *= rng.uniform(0.4, 1.2)
+        m[:3, 3] = rng.uniform(-1.5, 1.5, 3)
+        mats.append(m)
+    srays = wl.sphere_rays(9, 20000, 4.0)
+    res = {}
+    for tlas in (1, 0):
+        s = SceneRT(layout="bvh4_f16")
+        s.set_bvh4_merge(1)
+        s.set_morton_frame(E.MORTON_CUBIC)
+        s.set_bvh4_collapse(E.BVH4_COLLAPSE_LARGEST_FIRST)
+        s.set_tlas(bool(tlas))
+        g = s.AddGeom_Triangles3f(v, v.shape[0], idx, idx.size, vByteStride=16)
+        for m in mats:
+            s.AddInstance(g, m)
+        s.CommitScene()
+        res[tlas] = (_u32(s.RayQuery_NearestHit(srays)), s.RayQuery_AnyHit(srays))
+        s.close()
+    (a, aa), (b, bb) = res[1], res[0]
+    np.testing.assert_array_equal(aa, bb)
+    assert (a[:, 3] != MISS).sum() > 1000
+    diff = np.any(a != b, axis=1)
+    np.testing.assert_array_equal(a[diff, 0], b[diff, 0])  # only exact ties between instances may differ
+    assert diff.sum() <= 2
